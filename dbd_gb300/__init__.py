@@ -1,0 +1,205 @@
+"""dbd_gb300 -- GB300-native out-of-core SpGEMM (C = A*B, CSR) behind DBD's interface.
+
+Host-side mirror of the reference's stage functions (ZIP:dbd/src/SSpMM.hpp:126-149)
+over the C ABI of libdbd (include/dbd.h):
+
+    read_CSR(path)                      -> readInput.cpp:18  read_CSR
+    ctx = Context(cpu_gib, gpu_gib)     -> main.cpp:152      initialize (+ preProc.cu:23 initialize_GPU)
+    ctx.initialize_A(A), initialize_B   -> preProc.cu:28-46
+    ctx.divide_Blocks()                 -> main.cpp:259      divide_Blocks (+ get_UpperBound)
+    ctx.distribute_Workload(scope, dir) -> distributeWorkload.cpp:25 distribute_Workload
+    ctx.spgemm(A, B, scope)             -> one call of all of the above
+
+Errors: the reference prints to stderr and returns -1 / exits; here every
+failure raises DBDError carrying the library's error code and message.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _ffi
+from .csr import CSR
+
+__all__ = ["CSR", "Context", "DBDError", "read_CSR", "write_CSR", "lib_path", "SCOPES"]
+
+SCOPES = dict(_ffi.SCOPES)
+
+
+def lib_path():
+    return _ffi.LIB_PATH
+
+
+class DBDError(RuntimeError):
+    def __init__(self, code, msg=""):
+        self.code = code
+        name = _ffi.ERR_NAMES.get(code, str(code))
+        super().__init__(f"{name}: {msg}" if msg else name)
+
+
+def _check(rc, ctx=None):
+    if rc != _ffi.DBD_OK:
+        msg = ""
+        if ctx is not None:
+            m = _ffi.load().dbd_last_error(ctx)
+            msg = m.decode() if m else ""
+        raise DBDError(rc, msg)
+
+
+def _scope(scope):
+    if isinstance(scope, str):
+        return SCOPES[scope]
+    return int(scope)
+
+
+def read_CSR(path):
+    """Reads <path>.dcsr, <path>.csr (reference layout) or converts <path> (.mtx/.dat)."""
+    lib = _ffi.load()
+    h = _ffi.CsrHost()
+    _check(lib.dbd_read_csr(os.fsencode(path), C.byref(h)))
+    try:
+        n, nnz = h.n_rows, h.nnz
+        ptr = np.ctypeslib.as_array(C.cast(h.row_ptr, C.POINTER(C.c_int32)), shape=(n + 1,)).copy()
+        if nnz:
+            idx = np.ctypeslib.as_array(C.cast(h.col_idx, C.POINTER(C.c_int32)), shape=(nnz,)).copy()
+            val = np.ctypeslib.as_array(C.cast(h.val, C.POINTER(C.c_double)), shape=(nnz,)).copy()
+        else:
+            idx = np.zeros(0, np.int32)
+            val = np.zeros(0, np.float64)
+        return CSR(h.n_rows, h.n_cols, ptr, idx, val)
+    finally:
+        lib.dbd_csr_host_free(C.byref(h))
+
+
+def write_CSR(path, m, fp64=True):
+    """Writes m as .dcsr (fp64=True) or in the reference .csr layout (float32 values)."""
+    lib = _ffi.load()
+    v, _keep = m.view()
+    _check(lib.dbd_write_csr(os.fsencode(path), C.byref(v), 1 if fp64 else 0))
+
+
+class Result:
+    """Product of one multiply: C (host CSR with int64 row_ptr) and the stats."""
+
+    def __init__(self, C_, stats):
+        self.C = C_
+        self.stats = stats
+
+    @property
+    def gflops(self):
+        t = self.stats["t_total"]
+        return 2.0 * self.stats["products"] / t / 1e9 if t > 0 else float("nan")
+
+
+class Context:
+    """A libdbd context: device, budgets, streams, buffers (one per host thread)."""
+
+    def __init__(self, cpu_gib=28.0, gpu_gib=22.0, rows_per_block=4096, device=0, out_val_fp32=False,
+                 out_ptr32=False, verbose=False, io_rotate_gib=0.0):
+        self._lib = _ffi.load()
+        cfg = _ffi.Config()
+        self._lib.dbd_config_default(C.byref(cfg))
+        cfg.host_gib = float(cpu_gib)
+        cfg.gpu_gib = float(gpu_gib)
+        cfg.rows_per_block = int(rows_per_block)
+        cfg.device = int(device)
+        cfg.out_val_fp32 = int(bool(out_val_fp32))
+        cfg.out_ptr32 = int(bool(out_ptr32))
+        cfg.verbose = int(bool(verbose))
+        cfg.io_rotate_gib = float(io_rotate_gib)
+        h = C.c_void_p()
+        _check(self._lib.dbd_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.dbd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_handle):
+        """Runs the device pipeline on this cudaStream_t (an int), or the context's own (None)."""
+        _check(self._lib.dbd_set_stream(self._h, C.c_void_p(stream_handle) if stream_handle else None), self._h)
+
+    # ---- the reference's stage functions ----
+    def initialize_A(self, A):
+        v, keep = A.view()
+        self._keep = [keep]
+        _check(self._lib.dbd_load_a(self._h, C.byref(v)), self._h)
+
+    def initialize_B(self, B):
+        v, keep = B.view()
+        self._keep.append(keep)
+        _check(self._lib.dbd_load_b(self._h, C.byref(v)), self._h)
+
+    def divide_Blocks(self):
+        nb = C.c_int64()
+        _check(self._lib.dbd_divide_blocks(self._h, C.byref(nb)), self._h)
+        return nb.value
+
+    def block_info(self, num_blocks):
+        p = np.zeros(num_blocks, np.int64)
+        cat = np.zeros(num_blocks, np.int32)
+        _check(self._lib.dbd_block_info(self._h, p.ctypes.data, cat.ctypes.data), self._h)
+        return p, cat
+
+    def distribute_Workload(self, scope="kernel", out_dir="."):
+        _check(self._lib.dbd_distribute_workload(self._h, _scope(scope), os.fsencode(out_dir)), self._h)
+        return self.stats()
+
+    def stats(self):
+        st = _ffi.Stats()
+        _check(self._lib.dbd_get_stats(self._h, C.byref(st)), self._h)
+        return st.as_dict()
+
+    def result(self):
+        """Copies the last product to host numpy arrays."""
+        o = _ffi.CsrOut()
+        _check(self._lib.dbd_result(self._h, C.byref(o)), self._h)
+        ptr = np.empty(o.n_rows + 1, np.int64)
+        idx = np.empty(o.nnz, np.int32)
+        val = np.empty(o.nnz, np.float64)
+        _check(self._lib.dbd_result_copy(self._h, ptr.ctypes.data, idx.ctypes.data, val.ctypes.data), self._h)
+        return CSR(o.n_rows, o.n_cols, ptr, idx, val)
+
+    # ---- one-shot ----
+    def spgemm(self, A, B=None, scope="kernel", out_dir=".", fetch=True):
+        """C = A*B (B=None: A*A).  fetch=False leaves C where the scope put it."""
+        va, ka = A.view()
+        if B is None or B is A:
+            pb = None
+            kb = None
+        else:
+            vb, kb = B.view()
+            pb = C.byref(vb)
+        st = _ffi.Stats()
+        _check(self._lib.dbd_spgemm(self._h, C.byref(va), pb, _scope(scope), os.fsencode(out_dir), None,
+                                    C.byref(st)), self._h)
+        del ka, kb
+        stats = st.as_dict()
+        if not fetch or _scope(scope) == SCOPES["io"]:
+            return Result(None, stats)
+        return Result(self.result(), stats)
+
+    def spgemm_files(self, path_a, path_b=None, scope="io", out_dir="."):
+        st = _ffi.Stats()
+        _check(self._lib.dbd_spgemm_files(self._h, os.fsencode(path_a),
+                                          os.fsencode(path_b) if path_b else None, _scope(scope),
+                                          os.fsencode(out_dir), C.byref(st)), self._h)
+        return st.as_dict()

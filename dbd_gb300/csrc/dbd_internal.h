@@ -1,0 +1,101 @@
+// dbd_internal.h -- declarations shared by the host engine and the CUDA
+// kernels of libdbd.  Not part of the public ABI (include/dbd.h is).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dbd {
+
+// Device view of a CSR operand: int32 row_ptr/col_idx, FP64 values.
+struct CsrDev {
+    int64_t m = 0, n = 0, nnz = 0;
+    const int32_t *ptr = nullptr;
+    const int32_t *idx = nullptr;
+    const double *val = nullptr;
+};
+
+// Row categories.  The symbolic pass bins rows by their product count P_r
+// (an upper bound of the row's output size), the numeric pass by the exact
+// output size nnz_r that the symbolic pass found.  Lists of rows per bin keep
+// row order, so the rows of any run of row blocks form one contiguous range
+// of every bin.
+enum SymBin : uint8_t { SB_EMPTY = 0, SB_TINY, SB_HWARP, SB_HCTA, SB_WIDE, SB_COUNT };
+enum NumBin : uint8_t { NB_EMPTY = 0, NB_TINY, NB_HWARP, NB_HCTA_S, NB_HCTA_L, NB_DENSE, NB_COUNT };
+constexpr int kMaxBins = 8;
+constexpr int kTileRows = 256;     // granularity of the per-bin offset tables
+constexpr int kScanTile = 4096;    // rows per CTA of the row_ptr scan
+
+// Compile-time table sizes of the accumulators; the bin thresholds below
+// must keep every row inside its table at load factor <= 1/2.
+constexpr int kTinyMax = 32;                 // products held one per lane
+constexpr int kSymWarpTable = 1024, kSymWarpMax = 512;
+constexpr int kSymCtaTable = 8192, kSymCtaMax = 4096;
+constexpr int kNumWarpTable = 512, kNumWarpMax = 256;
+constexpr int kNumCtaSTable = 2048, kNumCtaSMax = 1024;
+constexpr int kNumCtaLTable = 8192, kNumCtaLMax = 4096;
+constexpr int kDenseWindow = 8192;           // FP64 columns per dense window (64 KiB)
+constexpr int kWideWindowBitsMax = 1 << 20;  // symbolic bitmap window (128 KiB)
+
+// Device-side error word values (kernels never trap; the host reads this).
+enum DevErr : int { DEV_OK = 0, DEV_TABLE_FULL = 1, DEV_COUNT_MISMATCH = 2, DEV_ROW_TOO_LONG = 3 };
+
+// Counter slots for dynamically scheduled kernels (zeroed per multiply).
+enum CounterSlot : int { CTR_SYM_TINY = 0, CTR_SYM_HWARP, CTR_SYM_HCTA, CTR_SYM_WIDE, CTR_COUNT = 16 };
+
+struct Binning {
+    uint8_t *bin = nullptr;     // m bin ids
+    int32_t *list = nullptr;    // m row ids grouped by bin
+    int32_t *hist = nullptr;    // ntiles * kMaxBins counts
+    int32_t *tileOff = nullptr; // (ntiles + 1) * kMaxBins absolute offsets into list
+    int32_t *binStart = nullptr;// kMaxBins + 1
+};
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---- launchers (k_analysis.cu) ----
+void launch_row_products(const CsrDev &A, const int32_t *Bp, int64_t *rowP, uint8_t *symBin,
+                         int *err, cudaStream_t s, int num_sms);
+void launch_block_products(int64_t m, const int64_t *rowP, int64_t rows_per_block,
+                           int64_t *blockP, cudaStream_t s);
+void launch_bin_lists(int64_t m, const Binning &b, int nbins, cudaStream_t s);
+void launch_num_bins(int64_t m, const int32_t *Ap, const int64_t *rowP, const int32_t *rowNnz,
+                     uint8_t *numBin, cudaStream_t s, int num_sms);
+void launch_row_scan(int64_t m, const int32_t *rowNnz, int64_t *part, int64_t *Cp, cudaStream_t s);
+void launch_check_sorted(const CsrDev &B, int *unsorted, cudaStream_t s, int num_sms);
+
+// ---- launchers (k_spgemm.cu) ----
+struct SymArgs {
+    CsrDev A, B;
+    const int32_t *list;
+    const int32_t *binStart;
+    int32_t *rowNnz;
+    uint32_t *ctr;
+    int *err;
+};
+// Launches the symbolic kernel of every non-empty bin; binStartHost holds the
+// bin boundaries of the row list (copied from the device after binning).
+void launch_symbolic_bins(const SymArgs &a, const int32_t *binStartHost, cudaStream_t s, int *launches);
+void launch_f32_to_f64(const float *src, double *dst, int64_t n, cudaStream_t s);
+void launch_validate_ptr(const int32_t *ptr, int64_t m, int64_t nnz, int *flag, cudaStream_t s);
+void launch_validate_idx(const int32_t *idx, int64_t nnz, int64_t ncols, int *flag, cudaStream_t s);
+
+struct NumArgs {
+    CsrDev A, B;
+    const int32_t *list;
+    const int64_t *Cp;
+    int64_t outBase;      // Cp value stored at out[0]
+    int32_t *Ci;
+    double *Cv;
+    int32_t *cursor;      // nnz(A) scratch for the dense windows
+    int bSorted;          // B's rows have ascending columns
+    int *err;
+};
+// Runs the numeric kernels of bin b over list[lo, hi).
+void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,
+                        int *launches);
+
+// One-time kernel attribute setup (dynamic shared memory limits).
+void init_kernel_attributes();
+
+}  // namespace dbd

@@ -1,0 +1,1056 @@
+// engine.cpp -- host side of libdbd: context, budgets, the row-block
+// pipeline and the dynamic block distributor, and the C ABI of include/dbd.h.
+//
+// Reference structure (ZIP:dbd/src): main.cpp drives initialize ->
+// read_CSR -> initialize_A/B -> divide_Blocks -> distribute_Workload; the
+// distributor (distributeWorkload.cpp:25-223) hands row blocks to a CPU and a
+// GPU pthread through plain bool flags polled every 2 us, the GPU thread
+// (computeGPU.cu:15-98) runs its kernels and blocking cudaMemcpys per block on
+// the default stream, and a writer pthread (writeFile.cpp) fwrites finished
+// blocks in order.
+//
+// GB300 design: the whole matrix is categorised and symbolically sized on the
+// device first; then consecutive row blocks are grouped into output chunks
+// sized by the device budget.  Each chunk's numeric kernels run on the
+// compute stream, its device->host copy on a copy stream (event-chained, so
+// chunk i+1 computes while chunk i copies), and in the +I/O scope a writer
+// thread appends finished chunks to Idx.output / Val.output in block order
+// while the next chunks compute.  There is no CPU compute path.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <errno.h>
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <cuda_runtime.h>
+
+#include "../../include/dbd.h"
+#include "dbd_internal.h"
+#include "dbd_io.h"
+
+using namespace dbd;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+double seconds_since(Clock::time_point t0) {
+    return std::chrono::duration<double>(Clock::now() - t0).count();
+}
+
+constexpr double kGiB = 1024.0 * 1024.0 * 1024.0;
+
+// Device allocation that only grows.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+// Pinned host allocation that only grows.
+struct HostBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMallocHost(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct Operand {
+    CsrDev dev;
+    DevBuf ptr, idx, val, tmp;
+    bool loaded = false;
+    int sorted = 0;
+};
+
+// A chunk: rows [r0, r1) (multiples of the tile size or m) and their output.
+struct Chunk {
+    int64_t r0, r1;
+    int64_t c0, c1;  // Cp[r0], Cp[r1]
+};
+
+struct WriteJob {
+    int64_t chunk;
+    int slot;
+    int64_t n;
+    cudaEvent_t ready;
+};
+
+}  // namespace
+
+struct dbd_ctx {
+    dbd_config cfg;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr, copy_stream = nullptr, stream = nullptr;
+    std::string last_error;
+
+    Operand A, B;
+    bool b_is_a = false;
+
+    // work arrays
+    DevBuf rowP, symBin, numBin, rowNnz, symList, numList, hist, symTileOff, numTileOff, symStart,
+        numStart, part, Cp, cursor, err, blockP, flags;
+    DevBuf Ci, Cv;           // resident product or device output ring
+    int64_t m = 0, ncols = 0, nnzC = 0, products = 0;
+    int64_t nblocks = 0, ntiles = 0;
+    bool divided = false;
+    std::vector<int64_t> blockP_h;
+    std::vector<int32_t> blockCat_h;
+    int32_t symStart_h[kMaxBins + 1] = {0};
+    int32_t numStart_h[kMaxBins + 1] = {0};
+    std::vector<int32_t> numTileOff_h;
+
+    // host result / ring
+    HostBuf hCp, hCi, hCv;
+    bool host_full = false;  // hCp/hCi/hCv hold the complete product
+    bool dev_resident = false;
+    dbd_scope last_scope = DBD_SCOPE_KERNEL;
+
+    cudaEvent_t evStart = nullptr, evPre = nullptr, evSym = nullptr, evEnd = nullptr;
+    cudaEvent_t evNumA = nullptr, evNumB = nullptr;
+    dbd_stats stats;
+    int launches = 0;
+};
+
+namespace {
+
+int set_err(dbd_ctx *c, int code, const std::string &msg) {
+    if (c) c->last_error = msg;
+    return code;
+}
+
+int cuda_fail(dbd_ctx *c, cudaError_t e, const char *what) {
+    const int code = (e == cudaErrorMemoryAllocation) ? DBD_ERR_OOM_DEVICE : DBD_ERR_CUDA;
+    return set_err(c, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(ctx, call)                                               \
+    do {                                                            \
+        cudaError_t _e = (call);                                    \
+        if (_e != cudaSuccess) return cuda_fail((ctx), _e, #call);  \
+    } while (0)
+
+int check_device_err(dbd_ctx *c, const char *stage) {
+    int h = 0;
+    CK(c, cudaMemcpyAsync(&h, c->err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (h != DEV_OK) {
+        const char *what = h == DEV_TABLE_FULL       ? "hash table full"
+                           : h == DEV_COUNT_MISMATCH ? "numeric/symbolic count mismatch"
+                           : h == DEV_ROW_TOO_LONG   ? "a row has more than 2^31 products"
+                                                     : "unknown";
+        return set_err(c, DBD_ERR_DEVICE_CHECK, std::string(stage) + ": device check failed: " + what);
+    }
+    return DBD_OK;
+}
+
+// Host-side validation of a host CSR operand (O(n + nnz)).
+int validate_host(dbd_ctx *c, const dbd_csr_view *v, const char *name) {
+    if (v->n_rows < 0 || v->n_cols < 0 || v->nnz < 0 || v->n_rows >= INT32_MAX || v->n_cols > INT32_MAX ||
+        v->nnz > INT32_MAX)
+        return set_err(c, DBD_ERR_INVALID, std::string(name) + ": size out of range");
+    if (!v->row_ptr || (v->nnz > 0 && (!v->col_idx || !v->val)))
+        return set_err(c, DBD_ERR_INVALID, std::string(name) + ": null array");
+    if (v->on_device) return DBD_OK;
+    if (v->row_ptr[0] != 0 || v->row_ptr[v->n_rows] != v->nnz)
+        return set_err(c, DBD_ERR_INVALID, std::string(name) + ": row_ptr does not span [0, nnz]");
+    for (int64_t r = 0; r < v->n_rows; ++r)
+        if (v->row_ptr[r + 1] < v->row_ptr[r])
+            return set_err(c, DBD_ERR_INVALID, std::string(name) + ": row_ptr decreases");
+    for (int64_t i = 0; i < v->nnz; ++i)
+        if (v->col_idx[i] < 0 || v->col_idx[i] >= v->n_cols)
+            return set_err(c, DBD_ERR_INVALID, std::string(name) + ": column index out of range");
+    return DBD_OK;
+}
+
+int load_operand(dbd_ctx *c, Operand &op, const dbd_csr_view *v, const char *name) {
+    int rc = validate_host(c, v, name);
+    if (rc) return rc;
+    op.loaded = false;
+    CsrDev d;
+    d.m = v->n_rows;
+    d.n = v->n_cols;
+    d.nnz = v->nnz;
+    const size_t ne = (size_t)v->nnz;
+    if (v->on_device) {
+        // Validate on the device: row_ptr first, then indices (only once the
+        // row_ptr is known to span [0, nnz]).
+        CK(c, c->flags.ensure(4 * sizeof(int)));
+        CK(c, cudaMemsetAsync(c->flags.p, 0, 4 * sizeof(int), c->stream));
+        launch_validate_ptr(v->row_ptr, v->n_rows, v->nnz, c->flags.as<int>(), c->stream);
+        int hf[4];
+        CK(c, cudaMemcpyAsync(hf, c->flags.p, sizeof(hf), cudaMemcpyDeviceToHost, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        if (hf[0]) return set_err(c, DBD_ERR_INVALID, std::string(name) + ": malformed row_ptr");
+        launch_validate_idx(v->col_idx, v->nnz, v->n_cols, c->flags.as<int>() + 1, c->stream);
+        CK(c, cudaMemcpyAsync(hf, c->flags.p, sizeof(hf), cudaMemcpyDeviceToHost, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        if (hf[1]) return set_err(c, DBD_ERR_INVALID, std::string(name) + ": column index out of range");
+        d.ptr = v->row_ptr;
+        d.idx = v->col_idx;
+        if (v->val_fp32) {
+            CK(c, op.val.ensure(sizeof(double) * ne));
+            launch_f32_to_f64((const float *)v->val, op.val.as<double>(), v->nnz, c->stream);
+            d.val = op.val.as<double>();
+        } else {
+            d.val = (const double *)v->val;
+        }
+    } else {
+        CK(c, op.ptr.ensure(sizeof(int32_t) * (size_t)(v->n_rows + 1)));
+        CK(c, op.idx.ensure(sizeof(int32_t) * ne));
+        CK(c, op.val.ensure(sizeof(double) * ne));
+        CK(c, cudaMemcpyAsync(op.ptr.p, v->row_ptr, sizeof(int32_t) * (size_t)(v->n_rows + 1),
+                              cudaMemcpyHostToDevice, c->stream));
+        CK(c, cudaMemcpyAsync(op.idx.p, v->col_idx, sizeof(int32_t) * ne, cudaMemcpyHostToDevice, c->stream));
+        if (v->val_fp32) {
+            CK(c, op.tmp.ensure(sizeof(float) * ne));
+            CK(c, cudaMemcpyAsync(op.tmp.p, v->val, sizeof(float) * ne, cudaMemcpyHostToDevice, c->stream));
+            launch_f32_to_f64(op.tmp.as<float>(), op.val.as<double>(), v->nnz, c->stream);
+        } else {
+            CK(c, cudaMemcpyAsync(op.val.p, v->val, sizeof(double) * ne, cudaMemcpyHostToDevice, c->stream));
+        }
+        d.ptr = op.ptr.as<int32_t>();
+        d.idx = op.idx.as<int32_t>();
+        d.val = op.val.as<double>();
+    }
+    op.dev = d;
+    // B's rows ascending lets the dense windows use cursors.
+    CK(c, c->flags.ensure(4 * sizeof(int)));
+    CK(c, cudaMemsetAsync(c->flags.as<int>() + 2, 0, sizeof(int), c->stream));
+    launch_check_sorted(d, c->flags.as<int>() + 2, c->stream, c->num_sms);
+    int unsorted = 0;
+    CK(c, cudaMemcpyAsync(&unsorted, c->flags.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    op.sorted = unsorted ? 0 : 1;
+    op.loaded = true;
+    c->divided = false;
+    return DBD_OK;
+}
+
+const CsrDev &opB(dbd_ctx *c) { return c->b_is_a ? c->A.dev : c->B.dev; }
+int opB_sorted(dbd_ctx *c) { return c->b_is_a ? c->A.sorted : c->B.sorted; }
+
+// ---- stage 1: work estimate, segmentation, categorisation ----------------
+
+int divide_blocks(dbd_ctx *c) {
+    if (!c->A.loaded || (!c->b_is_a && !c->B.loaded))
+        return set_err(c, DBD_ERR_INVALID, "load A and B before dividing blocks");
+    const CsrDev &A = c->A.dev;
+    const CsrDev &B = opB(c);
+    if (A.n != B.m) return set_err(c, DBD_ERR_INVALID, "inner dimensions differ (A.n_cols != B.n_rows)");
+    const auto t0 = Clock::now();
+    c->launches = 0;
+    c->m = A.m;
+    c->ncols = B.n;
+    const int64_t m = A.m;
+    const int64_t rpb = c->cfg.rows_per_block;
+    c->nblocks = m > 0 ? ceil_div(m, rpb) : 0;
+    c->ntiles = ceil_div(m, kTileRows);
+    const size_t mm = (size_t)std::max<int64_t>(m, 1);
+    const size_t nt = (size_t)c->ntiles;
+    CK(c, c->rowP.ensure(sizeof(int64_t) * mm));
+    CK(c, c->symBin.ensure(mm));
+    CK(c, c->numBin.ensure(mm));
+    CK(c, c->rowNnz.ensure(sizeof(int32_t) * mm));
+    CK(c, c->symList.ensure(sizeof(int32_t) * mm));
+    CK(c, c->numList.ensure(sizeof(int32_t) * mm));
+    CK(c, c->hist.ensure(sizeof(int32_t) * kMaxBins * (nt + 1)));
+    CK(c, c->symTileOff.ensure(sizeof(int32_t) * kMaxBins * (nt + 1)));
+    CK(c, c->numTileOff.ensure(sizeof(int32_t) * kMaxBins * (nt + 1)));
+    CK(c, c->symStart.ensure(sizeof(int32_t) * (kMaxBins + 1)));
+    CK(c, c->numStart.ensure(sizeof(int32_t) * (kMaxBins + 1)));
+    CK(c, c->part.ensure(sizeof(int64_t) * (size_t)(ceil_div(m, kScanTile) + 1)));
+    CK(c, c->Cp.ensure(sizeof(int64_t) * (mm + 1)));
+    CK(c, c->cursor.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(A.nnz, 1)));
+    CK(c, c->err.ensure(sizeof(int)));
+    CK(c, c->blockP.ensure(sizeof(int64_t) * (size_t)std::max<int64_t>(c->nblocks, 1)));
+
+    CK(c, cudaEventRecord(c->evStart, c->stream));
+    CK(c, cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+    launch_row_products(A, B.ptr, c->rowP.as<int64_t>(), c->symBin.as<uint8_t>(), c->err.as<int>(), c->stream,
+                        c->num_sms);
+    launch_block_products(m, c->rowP.as<int64_t>(), rpb, c->blockP.as<int64_t>(), c->stream);
+    Binning sb{c->symBin.as<uint8_t>(), c->symList.as<int32_t>(), c->hist.as<int32_t>(),
+               c->symTileOff.as<int32_t>(), c->symStart.as<int32_t>()};
+    launch_bin_lists(m, sb, SB_COUNT, c->stream);
+    c->launches += 5;
+    CK(c, cudaGetLastError());
+    c->blockP_h.assign((size_t)c->nblocks, 0);
+    if (c->nblocks)
+        CK(c, cudaMemcpyAsync(c->blockP_h.data(), c->blockP.p, sizeof(int64_t) * (size_t)c->nblocks,
+                              cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(c->symStart_h, c->symStart.p, sizeof(c->symStart_h), cudaMemcpyDeviceToHost,
+                          c->stream));
+    CK(c, cudaEventRecord(c->evPre, c->stream));
+    int rc = check_device_err(c, "work estimate");
+    if (rc) return rc;
+
+    // Segmenter + categoriser on the per-block products (host, O(blocks)).
+    int64_t total = 0, mx = 0;
+    for (int64_t b = 0; b < c->nblocks; ++b) {
+        total += c->blockP_h[(size_t)b];
+        mx = std::max(mx, c->blockP_h[(size_t)b]);
+    }
+    c->products = total;
+    int32_t crit = 0;
+    if (c->nblocks > 0) {
+        const int64_t avg = (total / c->nblocks) / rpb;
+        float var = 0.0f;
+        for (int64_t b = 0; b < c->nblocks; ++b) {
+            const int64_t d = avg - c->blockP_h[(size_t)b] / rpb;
+            var += (float)(d * d);
+        }
+        var /= (float)c->nblocks;
+        crit = (int32_t)(1.28f * std::sqrt(var)) + (int32_t)avg;
+    }
+    c->blockCat_h.assign((size_t)c->nblocks, 0);
+    memset(&c->stats, 0, sizeof(c->stats));
+    for (int64_t b = 0; b < c->nblocks; ++b) {
+        const int64_t avgb = c->blockP_h[(size_t)b] / rpb;
+        const int cat = avgb > crit ? 0 : (avgb <= 64 ? 1 : 2);
+        c->blockCat_h[(size_t)b] = cat;
+        c->stats.blocks_per_category[cat]++;
+    }
+    c->stats.products = total;
+    c->stats.n_blocks = c->nblocks;
+    c->stats.max_block_products = mx;
+    c->stats.criteria = crit;
+    for (int q = 0; q < SB_COUNT; ++q) c->stats.sym_rows_per_bin[q] = c->symStart_h[q + 1] - c->symStart_h[q];
+    c->stats.t_preprocess = seconds_since(t0);
+    c->divided = true;
+    if (c->cfg.verbose)
+        printf("Divide Matrix A into %lld Blocks (Block Size: %lld)\n\n", (long long)c->nblocks, (long long)rpb);
+    return DBD_OK;
+}
+
+// ---- stage 2: symbolic over all rows, row_ptr, numeric bins --------------
+
+int symbolic(dbd_ctx *c) {
+    const int64_t m = c->m;
+    CK(c, cudaMemsetAsync(c->rowNnz.p, 0, sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1), c->stream));
+    SymArgs sa;
+    sa.A = c->A.dev;
+    sa.B = opB(c);
+    sa.list = c->symList.as<int32_t>();
+    sa.binStart = c->symStart.as<int32_t>();
+    sa.rowNnz = c->rowNnz.as<int32_t>();
+    sa.ctr = nullptr;
+    sa.err = c->err.as<int>();
+    launch_symbolic_bins(sa, c->symStart_h, c->stream, &c->launches);
+    launch_row_scan(m, c->rowNnz.as<int32_t>(), c->part.as<int64_t>(), c->Cp.as<int64_t>(), c->stream);
+    launch_num_bins(m, c->A.dev.ptr, c->rowP.as<int64_t>(), c->rowNnz.as<int32_t>(), c->numBin.as<uint8_t>(),
+                    c->stream, c->num_sms);
+    Binning nb{c->numBin.as<uint8_t>(), c->numList.as<int32_t>(), c->hist.as<int32_t>(),
+               c->numTileOff.as<int32_t>(), c->numStart.as<int32_t>()};
+    launch_bin_lists(m, nb, NB_COUNT, c->stream);
+    c->launches += 7;
+    CK(c, cudaGetLastError());
+    CK(c, cudaMemcpyAsync(&c->nnzC, c->Cp.as<int64_t>() + m, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(c->numStart_h, c->numStart.p, sizeof(c->numStart_h), cudaMemcpyDeviceToHost, c->stream));
+    c->numTileOff_h.assign((size_t)kMaxBins * (size_t)(c->ntiles + 1), 0);
+    CK(c, cudaMemcpyAsync(c->numTileOff_h.data(), c->numTileOff.p, sizeof(int32_t) * c->numTileOff_h.size(),
+                          cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaEventRecord(c->evSym, c->stream));
+    int rc = check_device_err(c, "symbolic");
+    if (rc) return rc;
+    for (int q = 0; q < NB_COUNT; ++q) c->stats.rows_per_bin[q] = c->numStart_h[q + 1] - c->numStart_h[q];
+    c->stats.nnz_c = c->nnzC;
+    if (c->nnzC > INT64_MAX / 16) return set_err(c, DBD_ERR_OVERFLOW, "nnz(C) too large");
+    return DBD_OK;
+}
+
+// Numeric kernels of every bin restricted to rows [r0, r1).
+void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *Ci, double *Cv) {
+    NumArgs na;
+    na.A = c->A.dev;
+    na.B = opB(c);
+    na.list = c->numList.as<int32_t>();
+    na.Cp = c->Cp.as<int64_t>();
+    na.outBase = outBase;
+    na.Ci = Ci;
+    na.Cv = Cv;
+    na.cursor = c->cursor.as<int32_t>();
+    na.bSorted = opB_sorted(c);
+    na.err = c->err.as<int>();
+    const int64_t t0 = r0 / kTileRows;
+    const int64_t t1 = (r1 >= c->m) ? c->ntiles : r1 / kTileRows;
+    // Heaviest bins first so that their long CTAs start early.
+    static const int order[] = {NB_DENSE, NB_HCTA_L, NB_HCTA_S, NB_HWARP, NB_TINY};
+    for (int b : order) {
+        const int32_t lo = c->numTileOff_h[(size_t)t0 * kMaxBins + b];
+        const int32_t hi = c->numTileOff_h[(size_t)t1 * kMaxBins + b];
+        launch_numeric_bin(na, b, lo, hi, c->stream, &c->launches);
+    }
+}
+
+// Chunks of consecutive row blocks whose output fits cap_entries.
+int plan_chunks(dbd_ctx *c, const std::vector<int64_t> &cpBlk, int64_t cap_entries, std::vector<Chunk> &out) {
+    out.clear();
+    const int64_t nb = c->nblocks;
+    const int64_t rpb = c->cfg.rows_per_block;
+    int64_t b = 0;
+    while (b < nb) {
+        int64_t e = b + 1;
+        if (cpBlk[(size_t)e] - cpBlk[(size_t)b] > cap_entries)
+            return set_err(c, DBD_ERR_BUDGET, "one row block's output exceeds the device output buffer");
+        while (e < nb && cpBlk[(size_t)e + 1] - cpBlk[(size_t)b] <= cap_entries) ++e;
+        Chunk ch;
+        ch.r0 = b * rpb;
+        ch.r1 = std::min(c->m, e * rpb);
+        ch.c0 = cpBlk[(size_t)b];
+        ch.c1 = cpBlk[(size_t)e];
+        out.push_back(ch);
+        b = e;
+    }
+    return DBD_OK;
+}
+
+// ---- the writer thread (+I/O) -------------------------------------------
+
+struct Writer {
+    int fd_idx = -1, fd_val = -1;
+    int64_t off_idx = 0, off_val = 0;
+    int64_t wrap_idx = 0, wrap_val = 0;  // 0: no wrap
+    bool val_fp32 = false;
+    std::vector<float> f32;
+    double busy = 0.0;
+    int64_t bytes = 0;
+    std::atomic<int> error{0};
+    std::string msg;
+
+    int pwrite_all(int fd, const void *src, int64_t n, int64_t &off, int64_t wrap) {
+        const char *p = (const char *)src;
+        while (n > 0) {
+            int64_t at = off, lim = n;
+            if (wrap > 0) {
+                at = off % wrap;
+                lim = std::min<int64_t>(n, wrap - at);
+            }
+            const size_t step = (size_t)std::min<int64_t>(lim, 1 << 30);
+            const ssize_t w = ::pwrite(fd, p, step, (off_t)at);
+            if (w <= 0) {
+                if (w < 0 && errno == EINTR) continue;
+                msg = std::string("pwrite: ") + (w < 0 ? strerror(errno) : "short write");
+                return DBD_ERR_IO;
+            }
+            p += w;
+            n -= w;
+            off += w;
+            bytes += w;
+        }
+        return DBD_OK;
+    }
+
+    int write_chunk(const int32_t *ci, const double *cv, int64_t n) {
+        const auto t0 = Clock::now();
+        int rc = pwrite_all(fd_idx, ci, n * 4, off_idx, wrap_idx);
+        if (!rc) {
+            if (val_fp32) {
+                f32.resize((size_t)n);
+                for (int64_t i = 0; i < n; ++i) f32[(size_t)i] = (float)cv[i];
+                rc = pwrite_all(fd_val, f32.data(), n * 4, off_val, wrap_val);
+            } else {
+                rc = pwrite_all(fd_val, cv, n * 8, off_val, wrap_val);
+            }
+        }
+        busy += seconds_since(t0);
+        return rc;
+    }
+};
+
+std::string join_path(const char *dir, const char *name) {
+    std::string d = (dir && *dir) ? dir : ".";
+    if (d.back() != '/') d += '/';
+    return d + name;
+}
+
+// ---- stage 3: the distributor --------------------------------------------
+
+int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
+    if (!c->divided) {
+        int rc = divide_blocks(c);
+        if (rc) return rc;
+    }
+    c->divided = false;  // the bin lists are consumed by this multiply
+    const auto t0 = Clock::now();
+    int rc = symbolic(c);
+    if (rc) return rc;
+    const int64_t m = c->m, nnz = c->nnzC;
+    const double gpu_budget = c->cfg.gpu_gib * kGiB;
+    const double host_budget = c->cfg.host_gib * kGiB;
+    size_t free_b = 0, total_b = 0;
+    CK(c, cudaMemGetInfo(&free_b, &total_b));
+    // Device memory already held by operands and work arrays.
+    const double used = (double)(c->A.ptr.cap + c->A.idx.cap + c->A.val.cap + c->B.ptr.cap + c->B.idx.cap +
+                                 c->B.val.cap + c->rowP.cap + c->symBin.cap + c->numBin.cap + c->rowNnz.cap +
+                                 c->symList.cap + c->numList.cap + c->hist.cap + c->symTileOff.cap +
+                                 c->numTileOff.cap + c->part.cap + c->Cp.cap + c->cursor.cap);
+    const double dev_avail = std::min(gpu_budget - used, (double)free_b - 512.0 * 1024 * 1024);
+    const double out_bytes = 12.0 * (double)nnz;
+    const bool resident = out_bytes <= std::max(0.0, dev_avail) && scope == DBD_SCOPE_KERNEL;
+    const bool host_fits = out_bytes + 8.0 * (double)(m + 1) <= host_budget;
+
+    std::vector<Chunk> chunks;
+    int64_t cap_entries = nnz;
+    const int nslots_dev = 2;
+    if (resident) {
+        Chunk ch{0, m, 0, nnz};
+        chunks.push_back(ch);
+    } else {
+        // Output chunks: at most 1 GiB of output (so copies overlap compute)
+        // and at most a share of the remaining device budget per ring slot.
+        const double slot_bytes = std::min(std::max(0.0, dev_avail) / nslots_dev, 1.0 * kGiB);
+        cap_entries = std::max<int64_t>((int64_t)(slot_bytes / 12.0), 1);
+        std::vector<int64_t> cpBlk((size_t)c->nblocks + 1);
+        // Cp at block boundaries (strided copy of one int64 per block).
+        if (c->nblocks > 0) {
+            const size_t pitch = sizeof(int64_t) * (size_t)c->cfg.rows_per_block;
+            CK(c, cudaMemcpy2DAsync(cpBlk.data(), sizeof(int64_t), c->Cp.p, pitch, sizeof(int64_t),
+                                    (size_t)c->nblocks, cudaMemcpyDeviceToHost, c->stream));
+        }
+        cpBlk[(size_t)c->nblocks] = nnz;
+        CK(c, cudaStreamSynchronize(c->stream));
+        int64_t maxblk = 0;
+        for (int64_t b = 0; b < c->nblocks; ++b) maxblk = std::max(maxblk, cpBlk[(size_t)b + 1] - cpBlk[(size_t)b]);
+        if (maxblk > cap_entries) {
+            if ((double)maxblk * 12.0 * nslots_dev > std::max(0.0, dev_avail))
+                return set_err(c, DBD_ERR_BUDGET, "a row block's output does not fit the GPU budget");
+            cap_entries = maxblk;
+        }
+        rc = plan_chunks(c, cpBlk, cap_entries, chunks);
+        if (rc) return rc;
+    }
+    c->stats.n_chunks = (int32_t)chunks.size();
+    const int nslots = resident ? 1 : nslots_dev;
+    const size_t slot_entries = resident ? (size_t)std::max<int64_t>(nnz, 1) : (size_t)cap_entries;
+    CK(c, c->Ci.ensure(sizeof(int32_t) * slot_entries * nslots));
+    CK(c, c->Cv.ensure(sizeof(double) * slot_entries * nslots));
+    c->dev_resident = resident;
+
+    // Host side of D2H / IO.
+    c->host_full = false;
+    int nhslots = 0;
+    if (scope == DBD_SCOPE_D2H && host_fits) {
+        CK(c, c->hCp.ensure(sizeof(int64_t) * (size_t)(m + 1)));
+        CK(c, c->hCi.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1)));
+        CK(c, c->hCv.ensure(sizeof(double) * (size_t)std::max<int64_t>(nnz, 1)));
+        c->host_full = true;
+    } else if (scope != DBD_SCOPE_KERNEL) {
+        nhslots = scope == DBD_SCOPE_IO ? 3 : 2;
+        const double ring = (double)nhslots * 12.0 * (double)slot_entries;
+        if (ring > host_budget) return set_err(c, DBD_ERR_BUDGET, "host budget smaller than the output ring");
+        CK(c, c->hCi.ensure(sizeof(int32_t) * slot_entries * nhslots));
+        CK(c, c->hCv.ensure(sizeof(double) * slot_entries * nhslots));
+        CK(c, c->hCp.ensure(sizeof(int64_t) * (size_t)(m + 1)));
+    }
+
+    // Writer thread state.
+    Writer wr;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<WriteJob> jobs;
+    std::vector<int64_t> slot_owner((size_t)std::max(nhslots, 1), -1);  // chunk using host slot, -1 free
+    bool done = false;
+    std::thread th;
+    if (scope == DBD_SCOPE_IO) {
+        const std::string pi = join_path(out_dir, "Idx.output"), pv = join_path(out_dir, "Val.output");
+        unlink(join_path(out_dir, "Ptr.output").c_str());
+        wr.fd_idx = open(pi.c_str(), O_CREAT | O_TRUNC | O_WRONLY, 0644);
+        wr.fd_val = open(pv.c_str(), O_CREAT | O_TRUNC | O_WRONLY, 0644);
+        if (wr.fd_idx < 0 || wr.fd_val < 0) {
+            if (wr.fd_idx >= 0) close(wr.fd_idx);
+            if (wr.fd_val >= 0) close(wr.fd_val);
+            return set_err(c, DBD_ERR_IO, "cannot create output files in " + std::string(out_dir ? out_dir : "."));
+        }
+        wr.val_fp32 = c->cfg.out_val_fp32 != 0;
+        if (c->cfg.io_rotate_gib > 0) {
+            const int64_t rot = (int64_t)(c->cfg.io_rotate_gib * kGiB);
+            const int64_t vb = wr.val_fp32 ? 4 : 8;
+            wr.wrap_idx = std::max<int64_t>(4096, (rot * 4 / (4 + vb)) / 4096 * 4096);
+            wr.wrap_val = std::max<int64_t>(4096, (rot * vb / (4 + vb)) / 4096 * 4096);
+        }
+        th = std::thread([&]() {
+            for (;;) {
+                WriteJob j;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    cv.wait(lk, [&] { return done || !jobs.empty(); });
+                    if (jobs.empty()) return;
+                    j = jobs.front();
+                    jobs.pop_front();
+                }
+                if (cudaEventSynchronize(j.ready) != cudaSuccess && !wr.error) {
+                    wr.error = DBD_ERR_CUDA;
+                    wr.msg = "writer: copy event failed";
+                }
+                if (!wr.error) {
+                    const size_t so = (size_t)j.slot * slot_entries;
+                    int e = wr.write_chunk(c->hCi.as<int32_t>() + so, c->hCv.as<double>() + so, j.n);
+                    if (e) wr.error = e;
+                }
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    slot_owner[(size_t)j.slot] = -1;
+                }
+                cv.notify_all();
+            }
+        });
+    }
+
+    // Events per chunk for the two-stream pipeline.
+    std::vector<cudaEvent_t> evNum(chunks.size()), evCopy(chunks.size());
+    for (size_t i = 0; i < chunks.size(); ++i) {
+        cudaEventCreateWithFlags(&evNum[i], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&evCopy[i], cudaEventDisableTiming);
+    }
+    double t_d2h_issue = 0.0;
+    int64_t bytes_d2h = 0;
+    CK(c, cudaEventRecord(c->evNumA, c->stream));
+    int loop_rc = DBD_OK;
+    for (size_t i = 0; i < chunks.size() && !loop_rc; ++i) {
+        const Chunk &ch = chunks[i];
+        const int ds = resident ? 0 : (int)(i % nslots);
+        int32_t *dCi = c->Ci.as<int32_t>() + (resident ? 0 : (size_t)ds * slot_entries);
+        double *dCv = c->Cv.as<double>() + (resident ? 0 : (size_t)ds * slot_entries);
+        // The device slot is free once its previous chunk's copy finished.
+        if (!resident && i >= (size_t)nslots && scope != DBD_SCOPE_KERNEL)
+            cudaStreamWaitEvent(c->stream, evCopy[i - nslots], 0);
+        numeric_rows(c, ch.r0, ch.r1, ch.c0, dCi, dCv);
+        cudaEventRecord(evNum[i], c->stream);
+        if (scope == DBD_SCOPE_KERNEL) continue;
+        const int64_t n = ch.c1 - ch.c0;
+        int32_t *hCi;
+        double *hCv;
+        int hs = 0;
+        if (c->host_full) {
+            hCi = c->hCi.as<int32_t>() + ch.c0;
+            hCv = c->hCv.as<double>() + ch.c0;
+        } else {
+            hs = (int)(i % nhslots);
+            if (scope == DBD_SCOPE_IO) {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return slot_owner[(size_t)hs] < 0 || wr.error; });
+                slot_owner[(size_t)hs] = (int64_t)i;
+            } else if (i >= (size_t)nhslots) {
+                // d2h scope with a ring: the host slot is overwritten, as the
+                // reference's bin/d2h reuses one pinned buffer (preProc.cu:94-95).
+            }
+            hCi = c->hCi.as<int32_t>() + (size_t)hs * slot_entries;
+            hCv = c->hCv.as<double>() + (size_t)hs * slot_entries;
+        }
+        const auto ti = Clock::now();
+        cudaStreamWaitEvent(c->copy_stream, evNum[i], 0);
+        if (n > 0) {
+            cudaError_t e1 = cudaMemcpyAsync(hCi, dCi, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost,
+                                             c->copy_stream);
+            cudaError_t e2 = cudaMemcpyAsync(hCv, dCv, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost,
+                                             c->copy_stream);
+            if (e1 != cudaSuccess || e2 != cudaSuccess) loop_rc = cuda_fail(c, e1 != cudaSuccess ? e1 : e2, "D2H");
+        }
+        cudaEventRecord(evCopy[i], c->copy_stream);
+        bytes_d2h += 12 * n;
+        t_d2h_issue += seconds_since(ti);
+        if (scope == DBD_SCOPE_IO) {
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                jobs.push_back(WriteJob{(int64_t)i, hs, n, evCopy[i]});
+            }
+            cv.notify_all();
+        }
+    }
+    CK(c, cudaEventRecord(c->evNumB, c->stream));
+    // Row pointer of C to the host for D2H / IO.
+    if (scope != DBD_SCOPE_KERNEL) {
+        cudaStreamWaitEvent(c->copy_stream, c->evSym, 0);
+        CK(c, cudaMemcpyAsync(c->hCp.p, c->Cp.p, sizeof(int64_t) * (size_t)(m + 1), cudaMemcpyDeviceToHost,
+                              c->copy_stream));
+        bytes_d2h += 8 * (m + 1);
+    }
+    cudaError_t se = cudaStreamSynchronize(c->stream);
+    cudaError_t ce = cudaStreamSynchronize(c->copy_stream);
+    if (scope == DBD_SCOPE_IO) {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            done = true;
+        }
+        cv.notify_all();
+        th.join();
+    }
+    for (size_t i = 0; i < chunks.size(); ++i) {
+        cudaEventDestroy(evNum[i]);
+        cudaEventDestroy(evCopy[i]);
+    }
+    if (loop_rc) return loop_rc;
+    if (se != cudaSuccess) return cuda_fail(c, se, "compute stream");
+    if (ce != cudaSuccess) return cuda_fail(c, ce, "copy stream");
+    rc = check_device_err(c, "numeric");
+    if (rc) {
+        if (wr.fd_idx >= 0) close(wr.fd_idx);
+        if (wr.fd_val >= 0) close(wr.fd_val);
+        return rc;
+    }
+    if (scope == DBD_SCOPE_IO) {
+        int rc2 = wr.error;
+        std::string msg = wr.msg;
+        // Ptr.output (write_Ptr, writeFile.cpp:177-196).
+        const auto tp = Clock::now();
+        if (!rc2) {
+            const std::string pp = join_path(out_dir, "Ptr.output");
+            const int fd = open(pp.c_str(), O_CREAT | O_TRUNC | O_WRONLY, 0644);
+            if (fd < 0) {
+                rc2 = DBD_ERR_IO;
+                msg = "cannot create Ptr.output";
+            } else {
+                int64_t off = 0;
+                if (c->cfg.out_ptr32) {
+                    if (nnz > INT32_MAX) {
+                        rc2 = DBD_ERR_OVERFLOW;
+                        msg = "nnz(C) does not fit a 32-bit Ptr.output";
+                    } else {
+                        std::vector<int32_t> p32((size_t)m + 1);
+                        const int64_t *p = c->hCp.as<int64_t>();
+                        for (int64_t r = 0; r <= m; ++r) p32[(size_t)r] = (int32_t)p[r];
+                        rc2 = wr.pwrite_all(fd, p32.data(), 4 * (m + 1), off, 0);
+                    }
+                } else {
+                    rc2 = wr.pwrite_all(fd, c->hCp.p, 8 * (m + 1), off, 0);
+                }
+                wr.busy += seconds_since(tp);
+                const auto tf = Clock::now();
+                if (!rc2 && (fsync(fd) != 0 || fsync(wr.fd_idx) != 0 || fsync(wr.fd_val) != 0)) {
+                    rc2 = DBD_ERR_IO;
+                    msg = std::string("fsync: ") + strerror(errno);
+                }
+                c->stats.t_fsync = seconds_since(tf);
+                if (close(fd) != 0 && !rc2) {
+                    rc2 = DBD_ERR_IO;
+                    msg = "close Ptr.output";
+                }
+            }
+        }
+        if (close(wr.fd_idx) != 0 && !rc2) rc2 = DBD_ERR_IO;
+        if (close(wr.fd_val) != 0 && !rc2) rc2 = DBD_ERR_IO;
+        c->stats.t_write_file = wr.busy;
+        c->stats.bytes_written = wr.bytes;
+        if (rc2) return set_err(c, rc2, msg.empty() ? "output write failed" : msg);
+    }
+    c->stats.t_kernel_exec = seconds_since(t0);
+    c->stats.t_total = c->stats.t_preprocess + c->stats.t_kernel_exec;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->evStart, c->evNumB);
+    c->stats.t_device_ms = ms;
+    float msn = 0.f;
+    cudaEventElapsedTime(&msn, c->evNumA, c->evNumB);
+    c->stats.t_numeric_ms = msn;
+    float mss = 0.f;
+    cudaEventElapsedTime(&mss, c->evPre, c->evNumB);
+    c->stats.t_compute_gpu = mss / 1000.0;
+    c->stats.t_d2h = t_d2h_issue;
+    c->stats.bytes_d2h = bytes_d2h;
+    c->stats.gpu_launches = c->launches;
+    c->last_scope = scope;
+    return DBD_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+void dbd_config_default(dbd_config *cfg) {
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->host_gib = 28.0;
+    cfg->gpu_gib = 22.0;
+    cfg->rows_per_block = 4096;
+    cfg->device = 0;
+}
+
+const char *dbd_error_string(int code) {
+    switch (code) {
+        case DBD_OK: return "ok";
+        case DBD_ERR_INVALID: return "invalid argument";
+        case DBD_ERR_OOM_DEVICE: return "out of device memory";
+        case DBD_ERR_OOM_HOST: return "out of host memory";
+        case DBD_ERR_BUDGET: return "does not fit the memory budget";
+        case DBD_ERR_IO: return "I/O error";
+        case DBD_ERR_CUDA: return "CUDA error";
+        case DBD_ERR_TIMEOUT: return "timeout";
+        case DBD_ERR_OVERFLOW: return "overflow";
+        case DBD_ERR_DEVICE_CHECK: return "device consistency check failed";
+        case DBD_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown error";
+    }
+}
+
+const char *dbd_last_error(const dbd_ctx *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+int dbd_create(const dbd_config *cfg_in, dbd_ctx **out) {
+    if (!out) return DBD_ERR_INVALID;
+    *out = nullptr;
+    dbd_config cfg;
+    if (cfg_in) cfg = *cfg_in; else dbd_config_default(&cfg);
+    if (cfg.rows_per_block <= 0 || cfg.rows_per_block % kTileRows != 0 || cfg.host_gib <= 0 || cfg.gpu_gib <= 0)
+        return DBD_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DBD_ERR_NO_DEVICE;
+    if (cfg.device < 0 || cfg.device >= ndev) return DBD_ERR_INVALID;
+    if (cudaSetDevice(cfg.device) != cudaSuccess) return DBD_ERR_CUDA;
+    dbd_ctx *c = new (std::nothrow) dbd_ctx();
+    if (!c) return DBD_ERR_OOM_HOST;
+    c->cfg = cfg;
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, cfg.device);
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return DBD_ERR_CUDA;
+    }
+    c->stream = c->own_stream;
+    cudaEventCreate(&c->evStart);
+    cudaEventCreate(&c->evPre);
+    cudaEventCreate(&c->evSym);
+    cudaEventCreate(&c->evEnd);
+    cudaEventCreate(&c->evNumA);
+    cudaEventCreate(&c->evNumB);
+    init_kernel_attributes();
+    if (cudaGetLastError() != cudaSuccess) {
+        dbd_destroy(c);
+        return DBD_ERR_CUDA;
+    }
+    *out = c;
+    return DBD_OK;
+}
+
+void dbd_destroy(dbd_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->cfg.device);
+    if (c->own_stream) cudaStreamSynchronize(c->own_stream);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    for (DevBuf *b : {&c->A.ptr, &c->A.idx, &c->A.val, &c->A.tmp, &c->B.ptr, &c->B.idx, &c->B.val, &c->B.tmp,
+                      &c->rowP, &c->symBin, &c->numBin, &c->rowNnz, &c->symList, &c->numList, &c->hist,
+                      &c->symTileOff, &c->numTileOff, &c->symStart, &c->numStart, &c->part, &c->Cp, &c->cursor,
+                      &c->err, &c->blockP, &c->flags, &c->Ci, &c->Cv})
+        b->release();
+    c->hCp.release();
+    c->hCi.release();
+    c->hCv.release();
+    for (cudaEvent_t e : {c->evStart, c->evPre, c->evSym, c->evEnd, c->evNumA, c->evNumB})
+        if (e) cudaEventDestroy(e);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    delete c;
+}
+
+int dbd_set_stream(dbd_ctx *c, void *stream) {
+    if (!c) return DBD_ERR_INVALID;
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return DBD_OK;
+}
+
+int dbd_read_csr(const char *path, dbd_csr_host *out) {
+    if (!path || !out) return DBD_ERR_INVALID;
+    std::string err;
+    int rc = read_csr_file(path, out, &err);
+    if (rc) fprintf(stderr, "dbd_read_csr: %s\n", err.c_str());
+    return rc;
+}
+
+int dbd_write_csr(const char *path, const dbd_csr_view *m, int fp64) {
+    if (!path || !m) return DBD_ERR_INVALID;
+    std::string err;
+    int rc = write_csr_file(path, m, fp64, &err);
+    if (rc) fprintf(stderr, "dbd_write_csr: %s\n", err.c_str());
+    return rc;
+}
+
+int dbd_load_a(dbd_ctx *c, const dbd_csr_view *a) {
+    if (!c || !a) return DBD_ERR_INVALID;
+    cudaSetDevice(c->cfg.device);
+    c->b_is_a = false;
+    return load_operand(c, c->A, a, "A");
+}
+
+int dbd_load_b(dbd_ctx *c, const dbd_csr_view *b) {
+    if (!c || !b) return DBD_ERR_INVALID;
+    cudaSetDevice(c->cfg.device);
+    c->b_is_a = false;
+    return load_operand(c, c->B, b, "B");
+}
+
+int dbd_divide_blocks(dbd_ctx *c, int64_t *num_blocks) {
+    if (!c) return DBD_ERR_INVALID;
+    cudaSetDevice(c->cfg.device);
+    int rc = divide_blocks(c);
+    if (!rc && num_blocks) *num_blocks = c->nblocks;
+    return rc;
+}
+
+int dbd_block_info(const dbd_ctx *c, int64_t *products, int32_t *category) {
+    if (!c) return DBD_ERR_INVALID;
+    for (size_t b = 0; b < c->blockP_h.size(); ++b) {
+        if (products) products[b] = c->blockP_h[b];
+        if (category) category[b] = c->blockCat_h[b];
+    }
+    return DBD_OK;
+}
+
+int dbd_distribute_workload(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
+    if (!c || scope < DBD_SCOPE_KERNEL || scope > DBD_SCOPE_IO) return DBD_ERR_INVALID;
+    cudaSetDevice(c->cfg.device);
+    return distribute(c, scope, out_dir);
+}
+
+int dbd_result(dbd_ctx *c, dbd_csr_out *o) {
+    if (!c || !o) return DBD_ERR_INVALID;
+    memset(o, 0, sizeof(*o));
+    o->n_rows = c->m;
+    o->n_cols = c->ncols;
+    o->nnz = c->nnzC;
+    if (c->last_scope == DBD_SCOPE_KERNEL) {
+        if (!c->dev_resident) return set_err(c, DBD_ERR_BUDGET, "the product was streamed, not kept on the device");
+        o->row_ptr = c->Cp.as<int64_t>();
+        o->col_idx = c->Ci.as<int32_t>();
+        o->val = c->Cv.as<double>();
+        o->on_device = 1;
+        o->owner = 2;
+        return DBD_OK;
+    }
+    if (!c->host_full) return set_err(c, DBD_ERR_BUDGET, "the product did not fit the host budget");
+    o->row_ptr = c->hCp.as<int64_t>();
+    o->col_idx = c->hCi.as<int32_t>();
+    o->val = c->hCv.as<double>();
+    o->owner = 2;
+    return DBD_OK;
+}
+
+int dbd_result_copy(dbd_ctx *c, int64_t *row_ptr, int32_t *col_idx, double *val) {
+    if (!c) return DBD_ERR_INVALID;
+    dbd_csr_out o;
+    int rc = dbd_result(c, &o);
+    if (rc) return rc;
+    const cudaMemcpyKind k = o.on_device ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+    if (row_ptr) CK(c, cudaMemcpy(row_ptr, o.row_ptr, sizeof(int64_t) * (size_t)(o.n_rows + 1), k));
+    if (o.nnz > 0) {
+        if (col_idx) CK(c, cudaMemcpy(col_idx, o.col_idx, sizeof(int32_t) * (size_t)o.nnz, k));
+        if (val) CK(c, cudaMemcpy(val, o.val, sizeof(double) * (size_t)o.nnz, k));
+    }
+    return DBD_OK;
+}
+
+int dbd_get_stats(const dbd_ctx *c, dbd_stats *st) {
+    if (!c || !st) return DBD_ERR_INVALID;
+    *st = c->stats;
+    return DBD_OK;
+}
+
+int dbd_spgemm(dbd_ctx *c, const dbd_csr_view *a, const dbd_csr_view *b, dbd_scope scope, const char *out_dir,
+               dbd_csr_out *out, dbd_stats *st) {
+    if (!c || !a) return DBD_ERR_INVALID;
+    cudaSetDevice(c->cfg.device);
+    int rc = load_operand(c, c->A, a, "A");
+    if (rc) return rc;
+    if (!b || b == a) {
+        c->b_is_a = true;
+    } else {
+        c->b_is_a = false;
+        rc = load_operand(c, c->B, b, "B");
+        if (rc) return rc;
+    }
+    rc = divide_blocks(c);
+    if (rc) return rc;
+    rc = distribute(c, scope, out_dir);
+    if (rc) return rc;
+    if (st) *st = c->stats;
+    if (out) {
+        if (scope == DBD_SCOPE_IO) {
+            memset(out, 0, sizeof(*out));
+            out->n_rows = c->m;
+            out->n_cols = c->ncols;
+            out->nnz = c->nnzC;
+            return DBD_OK;
+        }
+        return dbd_result(c, out);
+    }
+    return DBD_OK;
+}
+
+int dbd_spgemm_files(dbd_ctx *c, const char *path_a, const char *path_b, dbd_scope scope, const char *out_dir,
+                     dbd_stats *st) {
+    if (!c || !path_a) return DBD_ERR_INVALID;
+    dbd_csr_host ha, hb;
+    memset(&hb, 0, sizeof(hb));
+    int rc = dbd_read_csr(path_a, &ha);
+    if (rc) return set_err(c, rc, std::string("cannot read ") + path_a);
+    const bool same = !path_b || strcmp(path_a, path_b) == 0;
+    if (!same) {
+        rc = dbd_read_csr(path_b, &hb);
+        if (rc) {
+            dbd_csr_host_free(&ha);
+            return set_err(c, rc, std::string("cannot read ") + path_b);
+        }
+    }
+    if (c->cfg.verbose) {
+        printf("Input: %s\n\tNumber of Rows:\t\t%lld\n\tNumber of Columns:\t%lld\n\tNumber of Edges:\t%lld\n\n",
+               path_a, (long long)ha.n_rows, (long long)ha.n_cols, (long long)ha.nnz);
+    }
+    dbd_csr_view va{ha.n_rows, ha.n_cols, ha.nnz, ha.row_ptr, ha.col_idx, ha.val, 0, 0};
+    dbd_csr_view vb{hb.n_rows, hb.n_cols, hb.nnz, hb.row_ptr, hb.col_idx, hb.val, 0, 0};
+    rc = dbd_spgemm(c, &va, same ? nullptr : &vb, scope, out_dir, nullptr, st);
+    dbd_csr_host_free(&ha);
+    dbd_csr_host_free(&hb);
+    return rc;
+}
+
+void dbd_csr_free(dbd_csr_out *o) {
+    if (!o) return;
+    if (o->owner == 1) {
+        free(o->row_ptr);
+        free(o->col_idx);
+        free(o->val);
+    }
+    memset(o, 0, sizeof(*o));
+}
+
+}  // extern "C"

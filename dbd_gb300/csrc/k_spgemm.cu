@@ -1,0 +1,615 @@
+// k_spgemm.cu -- symbolic and numeric SpGEMM kernels per row category.
+//
+// Replaces the reference's expansion kernels rowproduct_{sparse,dense,ddense}
+// (dbd/for_small_datasets/src/computeGPU.cu:135-294), its global-memory dense
+// merge (:296-329) and its compaction kernel collect (:331-341).  The
+// reference writes every intermediate product to HBM and re-reads it for an
+// FP32 atomic merge into a dense global row, deciding structure by value
+// (|partial sum| < 1e-4).  Here no intermediate product touches HBM:
+//
+//   tiny rows   (P_r <= 32)     one warp per row, products held one per lane,
+//                               duplicates found with __match_any_sync and
+//                               summed in Gustavson order (bit-exact FP64)
+//   warp / CTA hash rows        open-addressing hash tables in shared memory
+//                               (keys int32, values FP64), compacted and
+//                               bitonic-sorted in place by column
+//   wide rows   (symbolic)      shared-memory bitmap over column windows
+//   dense rows  (numeric)       shared-memory FP64 dense window of 8192
+//                               columns swept across the row with per-entry
+//                               cursors into B, written out in column order
+//
+// Structure is decided by index only (a column belongs to a row as soon as a
+// product lands on it).  Products are rounded to FP64 before accumulation
+// (__dmul_rn, no FMA contraction), so the tiny path reproduces the sequential
+// oracle bit for bit and the other paths differ only by summation order.
+#include "dbd_internal.h"
+
+#include <algorithm>
+#include <climits>
+
+namespace dbd {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int32_t EMPTY = -1;
+
+constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
+
+__device__ __forceinline__ uint32_t hslot(int32_t c, int shift) {
+    return ((uint32_t)c * 0x9E3779B1u) >> shift;
+}
+
+__device__ __forceinline__ void raise(int *err, int code) { atomicCAS(err, 0, code); }
+
+// One warp's view of up to 32 consecutive entries of an A row, for the
+// flattened enumeration of their products: product t (0 <= t < total) comes
+// from the lane whose inclusive length prefix first exceeds t.
+struct Chunk {
+    int32_t bs;    // first position of B_k in B.idx
+    int32_t len;   // |B_k|
+    int32_t incl;  // inclusive prefix of len over lanes
+    double a;      // A value of this lane's entry
+    int32_t total; // products of the chunk
+};
+
+__device__ __forceinline__ Chunk load_chunk(const CsrDev &A, const CsrDev &B, int32_t e,
+                                            int32_t eEnd, int lane) {
+    Chunk c;
+    c.bs = 0;
+    c.len = 0;
+    c.a = 0.0;
+    if (e + lane < eEnd) {
+        const int32_t k = A.idx[e + lane];
+        c.bs = B.ptr[k];
+        c.len = B.ptr[k + 1] - c.bs;
+        c.a = A.val[e + lane];
+    }
+    int32_t x = c.len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int32_t y = __shfl_up_sync(FULL, x, d);
+        if (lane >= d) x += y;
+    }
+    c.incl = x;
+    c.total = __shfl_sync(FULL, x, 31);
+    return c;
+}
+
+// Owner lane of product t (all 32 lanes must call; t may be out of range).
+__device__ __forceinline__ int chunk_owner(const Chunk &c, int32_t t) {
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        const int32_t v = __shfl_sync(FULL, c.incl, lo + step - 1);
+        if (v <= t) lo += step;
+    }
+    return lo;
+}
+
+// Position in B of product t (all lanes call; result valid when t < total).
+__device__ __forceinline__ int32_t chunk_pos(const Chunk &c, int32_t t, double *a_out) {
+    const int o = chunk_owner(c, t);
+    const int32_t incl_o = __shfl_sync(FULL, c.incl, o);
+    const int32_t len_o = __shfl_sync(FULL, c.len, o);
+    const int32_t bs_o = __shfl_sync(FULL, c.bs, o);
+    if (a_out) *a_out = __shfl_sync(FULL, c.a, o);
+    return bs_o + (t - (incl_o - len_o));
+}
+
+template <int GROUP, int ROWS>
+__device__ __forceinline__ void group_sync() {
+    if constexpr (ROWS > 1) {
+        static_assert(GROUP == 32, "multi-row CTAs use one warp per row");
+        __syncwarp();
+    } else {
+        __syncthreads();
+    }
+}
+
+template <int TABLE>
+__device__ __forceinline__ int hash_insert_key(int32_t *keys, int32_t col, int *err) {
+    constexpr int SHIFT = 32 - ilog2(TABLE);
+    uint32_t h = hslot(col, SHIFT);
+#pragma unroll 1
+    for (int probe = 0; probe < TABLE; ++probe) {
+        const int32_t k = ((volatile int32_t *)keys)[h];
+        if (k == col) return 0;
+        if (k == EMPTY) {
+            const int32_t old = atomicCAS(&keys[h], EMPTY, col);
+            if (old == EMPTY) return 1;
+            if (old == col) return 0;
+        }
+        h = (h + 1) & (TABLE - 1);
+    }
+    raise(err, DEV_TABLE_FULL);
+    return 0;
+}
+
+template <int TABLE>
+__device__ __forceinline__ int hash_insert_slot(int32_t *keys, int32_t col, int *err) {
+    constexpr int SHIFT = 32 - ilog2(TABLE);
+    uint32_t h = hslot(col, SHIFT);
+#pragma unroll 1
+    for (int probe = 0; probe < TABLE; ++probe) {
+        const int32_t k = ((volatile int32_t *)keys)[h];
+        if (k == col) return (int)h;
+        if (k == EMPTY) {
+            const int32_t old = atomicCAS(&keys[h], EMPTY, col);
+            if (old == EMPTY || old == col) return (int)h;
+        }
+        h = (h + 1) & (TABLE - 1);
+    }
+    raise(err, DEV_TABLE_FULL);
+    return -1;
+}
+
+__device__ __forceinline__ int warp_sum_i(int v) {
+#pragma unroll
+    for (int d = 16; d; d >>= 1) v += __shfl_xor_sync(FULL, v, d);
+    return v;
+}
+
+// ======================================================================
+// Symbolic kernels: rowNnz[row] = number of distinct columns of C's row.
+// ======================================================================
+
+// Tiny rows: one warp per row, all products at once (P_r <= 32, |A_r| <= 32).
+__global__ void __launch_bounds__(256) k_sym_tiny(SymArgs a, int32_t begin, int32_t count) {
+    const int lane = threadIdx.x & 31;
+    const int64_t item = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (item >= count) return;
+    const int32_t row = a.list[begin + item];
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    const Chunk c = load_chunk(a.A, a.B, e0, e1, lane);
+    const bool valid = lane < c.total;
+    const int32_t j = chunk_pos(c, lane, nullptr);
+    const uint32_t key = valid ? (uint32_t)a.B.idx[j] : (0x80000000u | (uint32_t)lane);
+    const unsigned grp = __match_any_sync(FULL, key);
+    const bool leader = valid && (lane == __ffs(grp) - 1);
+    const unsigned lm = __ballot_sync(FULL, leader);
+    if (lane == 0) a.rowNnz[row] = __popc(lm);
+}
+
+// Hash rows: GROUP threads per row, ROWS rows per CTA, TABLE keys per row.
+template <int GROUP, int ROWS, int TABLE>
+__global__ void __launch_bounds__(GROUP *ROWS) k_sym_hash(SymArgs a, int32_t begin, int32_t count) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int GW = GROUP / 32;
+    __shared__ int red[ROWS][GW];
+    const int g = threadIdx.x / GROUP, gt = threadIdx.x % GROUP;
+    const int lane = threadIdx.x & 31, gw = gt >> 5;
+    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    if (item >= count) return;
+    int32_t *keys = reinterpret_cast<int32_t *>(smem) + (size_t)g * TABLE;
+    const int32_t row = a.list[begin + item];
+    for (int i = gt; i < TABLE; i += GROUP) keys[i] = EMPTY;
+    group_sync<GROUP, ROWS>();
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    int cnt = 0;
+    for (int32_t e = e0 + gw * 32; e < e1; e += GROUP) {
+        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+            const int32_t t = t0 + lane;
+            const int32_t j = chunk_pos(c, t, nullptr);
+            if (t < c.total) cnt += hash_insert_key<TABLE>(keys, a.B.idx[j], a.err);
+        }
+    }
+    cnt = warp_sum_i(cnt);
+    if constexpr (GW == 1) {
+        if (gt == 0) a.rowNnz[row] = cnt;
+    } else {
+        if (lane == 0) red[g][gw] = cnt;
+        __syncthreads();
+        if (gt == 0) {
+            int s = 0;
+            for (int i = 0; i < GW; ++i) s += red[g][i];
+            a.rowNnz[row] = s;
+        }
+    }
+}
+
+// Wide rows: one CTA per row, a shared bitmap over windows of winBits columns.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, int64_t ncols,
+                                                      int winBits) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t *bm = reinterpret_cast<uint32_t *>(smem);
+    __shared__ int red[THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int32_t row = a.list[begin + blockIdx.x];
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    const int words = winBits >> 5;
+    int cnt = 0;
+    for (int64_t c_lo = 0; c_lo < ncols; c_lo += winBits) {
+        for (int i = threadIdx.x; i < words; i += THREADS) bm[i] = 0u;
+        __syncthreads();
+        for (int32_t e = e0 + w * 32; e < e1; e += THREADS) {
+            const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+            for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+                const int32_t t = t0 + lane;
+                const int32_t j = chunk_pos(c, t, nullptr);
+                if (t < c.total) {
+                    const int64_t rel = (int64_t)a.B.idx[j] - c_lo;
+                    if (rel >= 0 && rel < winBits) {
+                        const uint32_t bit = 1u << (rel & 31);
+                        const uint32_t old = atomicOr(&bm[rel >> 5], bit);
+                        cnt += (old & bit) ? 0 : 1;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    cnt = warp_sum_i(cnt);
+    if (lane == 0) red[w] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int i = 0; i < THREADS / 32; ++i) s += red[i];
+        a.rowNnz[row] = s;
+    }
+}
+
+// ======================================================================
+// Numeric kernels: columns ascending, values in FP64.
+// ======================================================================
+
+__global__ void __launch_bounds__(256) k_num_tiny(NumArgs a, int32_t lo, int32_t count) {
+    const int lane = threadIdx.x & 31;
+    const int64_t item = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (item >= count) return;
+    const int32_t row = a.list[lo + item];
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    const Chunk c = load_chunk(a.A, a.B, e0, e1, lane);
+    const bool valid = lane < c.total;
+    double av;
+    const int32_t j = chunk_pos(c, lane, &av);
+    int32_t col = -1;
+    double p = 0.0;
+    if (valid) {
+        col = a.B.idx[j];
+        p = __dmul_rn(av, a.B.val[j]);
+    }
+    const uint32_t key = valid ? (uint32_t)col : (0x80000000u | (uint32_t)lane);
+    const unsigned grp = __match_any_sync(FULL, key);
+    const bool leader = valid && (lane == __ffs(grp) - 1);
+    const unsigned lm = __ballot_sync(FULL, leader);
+    double acc = 0.0;
+    int rank = 0;
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+        const double pq = __shfl_sync(FULL, p, q);
+        const int32_t cq = __shfl_sync(FULL, col, q);
+        if ((grp >> q) & 1u) acc = __dadd_rn(acc, pq);
+        if (((lm >> q) & 1u) && cq < col) ++rank;
+    }
+    const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+    const int64_t base = a.Cp[row] - a.outBase;
+    if (leader && rank < expect) {
+        a.Ci[base + rank] = col;
+        a.Cv[base + rank] = acc;
+    }
+    if (lane == 0 && __popc(lm) != expect) raise(a.err, DEV_COUNT_MISMATCH);
+}
+
+// Bitonic sort of n64[0, N) ascending by GROUP threads (N a power of two).
+template <int GROUP, int ROWS>
+__device__ __forceinline__ void group_bitonic(uint64_t *buf, int N, int gt) {
+    for (int k = 2; k <= N; k <<= 1) {
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int i = gt; i < N; i += GROUP) {
+                const int ixj = i ^ jj;
+                if (ixj > i) {
+                    const uint64_t x = buf[i], y = buf[ixj];
+                    const bool up = (i & k) == 0;
+                    if ((x > y) == up) {
+                        buf[i] = y;
+                        buf[ixj] = x;
+                    }
+                }
+            }
+            group_sync<GROUP, ROWS>();
+        }
+    }
+}
+
+// Hash rows: keys int32[TABLE] then values double[TABLE] per row; the sort
+// buffer (TABLE/2 packed (column, slot) pairs) reuses the key array.
+template <int GROUP, int ROWS, int TABLE>
+__global__ void __launch_bounds__(GROUP *ROWS) k_num_hash(NumArgs a, int32_t lo, int32_t count) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int GW = GROUP / 32;
+    constexpr int KPT = TABLE / GROUP;
+    constexpr int NMAX = TABLE / 2;
+    static_assert(KPT >= 1 && TABLE % GROUP == 0, "table must split evenly");
+    __shared__ int gcnt[ROWS];
+    const int g = threadIdx.x / GROUP, gt = threadIdx.x % GROUP;
+    const int lane = threadIdx.x & 31, gw = gt >> 5;
+    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    if (item >= count) return;
+    unsigned char *base_ptr = smem + (size_t)g * (12 * (size_t)TABLE);
+    int32_t *keys = reinterpret_cast<int32_t *>(base_ptr);
+    double *vals = reinterpret_cast<double *>(base_ptr + 4 * (size_t)TABLE);
+    uint64_t *sbuf = reinterpret_cast<uint64_t *>(base_ptr);
+    const int32_t row = a.list[lo + item];
+    for (int i = gt; i < TABLE; i += GROUP) {
+        keys[i] = EMPTY;
+        vals[i] = 0.0;
+    }
+    if (gt == 0) gcnt[g] = 0;
+    group_sync<GROUP, ROWS>();
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    for (int32_t e = e0 + gw * 32; e < e1; e += GROUP) {
+        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+            const int32_t t = t0 + lane;
+            double av;
+            const int32_t j = chunk_pos(c, t, &av);
+            if (t < c.total) {
+                const int s = hash_insert_slot<TABLE>(keys, a.B.idx[j], a.err);
+                if (s >= 0) atomicAdd(&vals[s], __dmul_rn(av, a.B.val[j]));
+            }
+        }
+    }
+    group_sync<GROUP, ROWS>();
+    int32_t mk[KPT];
+#pragma unroll
+    for (int q = 0; q < KPT; ++q) mk[q] = keys[gt + q * GROUP];
+    group_sync<GROUP, ROWS>();
+#pragma unroll
+    for (int q = 0; q < KPT; ++q) {
+        const bool occ = mk[q] != EMPTY;
+        const unsigned bal = __ballot_sync(FULL, occ);
+        int wbase = 0;
+        if (lane == 0 && bal) wbase = atomicAdd(&gcnt[g], __popc(bal));
+        wbase = __shfl_sync(FULL, wbase, 0);
+        if (occ) {
+            const int pos = wbase + __popc(bal & ((1u << lane) - 1u));
+            if (pos < NMAX)
+                sbuf[pos] = ((uint64_t)(uint32_t)mk[q] << 32) | (uint32_t)(gt + q * GROUP);
+        }
+    }
+    group_sync<GROUP, ROWS>();
+    const int n = gcnt[g];
+    const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+    if (gt == 0 && (n != expect || n > NMAX)) raise(a.err, DEV_COUNT_MISMATCH);
+    const int nn = min(n, NMAX);
+    int N = 1;
+    while (N < nn) N <<= 1;
+    for (int i = nn + gt; i < N; i += GROUP) sbuf[i] = ~0ull;
+    group_sync<GROUP, ROWS>();
+    group_bitonic<GROUP, ROWS>(sbuf, N, gt);
+    const int64_t obase = a.Cp[row] - a.outBase;
+    const int wn = (int)min((int64_t)nn, expect);
+    for (int i = gt; i < wn; i += GROUP) {
+        const uint64_t v = sbuf[i];
+        a.Ci[obase + i] = (int32_t)(v >> 32);
+        a.Cv[obase + i] = vals[(uint32_t)v];
+    }
+}
+
+template <int THREADS>
+__device__ __forceinline__ int32_t block_min_i32(int32_t v, int32_t *sh) {
+#pragma unroll
+    for (int d = 16; d; d >>= 1) v = min(v, __shfl_xor_sync(FULL, v, d));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int32_t r = INT_MAX;
+#pragma unroll
+    for (int i = 0; i < THREADS / 32; ++i) r = min(r, sh[i]);
+    __syncthreads();
+    return r;
+}
+
+template <int THREADS>
+__device__ __forceinline__ int32_t block_excl_scan_small(int32_t v, int32_t *total, int32_t *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int32_t y = __shfl_up_sync(FULL, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    int32_t base = 0, tot = 0;
+#pragma unroll
+    for (int i = 0; i < THREADS / 32; ++i) {
+        const int32_t s = sh[i];
+        if (i < w) base += s;
+        tot += s;
+    }
+    __syncthreads();
+    *total = tot;
+    return base + x - v;
+}
+
+// Dense rows: one CTA per row sweeps windows of W columns; each thread owns
+// A entries and keeps a cursor into their B row (B rows ascending), so every
+// product is visited once.  Without sorted B rows every window rescans the
+// B rows and filters.
+template <int THREADS, int W, bool SORTED>
+__global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    static_assert(W / 32 <= THREADS, "one bitmap word per thread");
+    double *dense = reinterpret_cast<double *>(smem);
+    uint32_t *bits = reinterpret_cast<uint32_t *>(smem + 8 * (size_t)W);
+    __shared__ int32_t sh[THREADS / 32];
+    const int tid = threadIdx.x;
+    const int32_t row = a.list[lo + blockIdx.x];
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+    const int64_t obase = a.Cp[row] - a.outBase;
+
+    int32_t mymin = INT_MAX;
+    for (int32_t e = e0 + tid; e < e1; e += THREADS) {
+        const int32_t k = a.A.idx[e];
+        const int32_t s = a.B.ptr[k], t = a.B.ptr[k + 1];
+        if constexpr (SORTED) {
+            a.cursor[e] = s;
+            if (s < t) mymin = min(mymin, a.B.idx[s]);
+        } else {
+            for (int32_t q = s; q < t; ++q) mymin = min(mymin, a.B.idx[q]);
+        }
+    }
+    int32_t cmin = block_min_i32<THREADS>(mymin, sh);
+    int64_t run = 0;
+    while (cmin != INT_MAX) {
+        const int32_t c_lo = (cmin / W) * W;
+        const int64_t c_hi = (int64_t)c_lo + W;
+        for (int i = tid; i < W; i += THREADS) dense[i] = 0.0;
+        for (int i = tid; i < W / 32; i += THREADS) bits[i] = 0u;
+        __syncthreads();
+        mymin = INT_MAX;
+        for (int32_t e = e0 + tid; e < e1; e += THREADS) {
+            const int32_t k = a.A.idx[e];
+            const double av = a.A.val[e];
+            const int32_t t = a.B.ptr[k + 1];
+            if constexpr (SORTED) {
+                int32_t cur = a.cursor[e];
+                while (cur < t) {
+                    const int32_t c = a.B.idx[cur];
+                    if (c >= c_hi) {
+                        mymin = min(mymin, c);
+                        break;
+                    }
+                    const int rel = c - c_lo;
+                    atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[cur]));
+                    atomicOr(&bits[rel >> 5], 1u << (rel & 31));
+                    ++cur;
+                }
+                a.cursor[e] = cur;
+            } else {
+                for (int32_t q = a.B.ptr[k]; q < t; ++q) {
+                    const int32_t c = a.B.idx[q];
+                    if (c >= c_lo && c < c_hi) {
+                        const int rel = c - c_lo;
+                        atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[q]));
+                        atomicOr(&bits[rel >> 5], 1u << (rel & 31));
+                    } else if (c >= c_hi) {
+                        mymin = min(mymin, c);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        uint32_t word = tid < W / 32 ? bits[tid] : 0u;
+        int32_t tot;
+        const int32_t off = block_excl_scan_small<THREADS>(__popc(word), &tot, sh);
+        int64_t pos = run + off;
+        while (word) {
+            const int b = __ffs(word) - 1;
+            word &= word - 1u;
+            const int rel = tid * 32 + b;
+            if (pos < expect) {
+                a.Ci[obase + pos] = c_lo + rel;
+                a.Cv[obase + pos] = dense[rel];
+            }
+            ++pos;
+        }
+        run += tot;
+        cmin = block_min_i32<THREADS>(mymin, sh);
+    }
+    if (tid == 0 && run != expect) raise(a.err, DEV_COUNT_MISMATCH);
+}
+
+// Shared-memory sizes of each configuration.
+constexpr int kSymWarpRows = 8;
+constexpr int kNumWarpRows = 4;
+constexpr size_t kSmemSymWarp = (size_t)kSymWarpRows * kSymWarpTable * 4;
+constexpr size_t kSmemSymCta = (size_t)kSymCtaTable * 4;
+constexpr size_t kSmemNumWarp = (size_t)kNumWarpRows * kNumWarpTable * 12;
+constexpr size_t kSmemNumCtaS = (size_t)kNumCtaSTable * 12;
+constexpr size_t kSmemNumCtaL = (size_t)kNumCtaLTable * 12;
+constexpr size_t kSmemDense = (size_t)kDenseWindow * 8 + kDenseWindow / 8;
+constexpr int kDenseThreads = 512;
+constexpr int kWideThreads = 512;
+
+}  // namespace
+
+void init_kernel_attributes() {
+    cudaFuncSetAttribute(k_sym_hash<32, kSymWarpRows, kSymWarpTable>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemSymWarp);
+    cudaFuncSetAttribute(k_sym_hash<256, 1, kSymCtaTable>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemSymCta);
+    cudaFuncSetAttribute(k_sym_wide<kWideThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kWideWindowBitsMax / 8);
+    cudaFuncSetAttribute(k_num_hash<32, kNumWarpRows, kNumWarpTable>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumWarp);
+    cudaFuncSetAttribute(k_num_hash<256, 1, kNumCtaSTable>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumCtaS);
+    cudaFuncSetAttribute(k_num_hash<512, 1, kNumCtaLTable>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumCtaL);
+    cudaFuncSetAttribute(k_num_dense<kDenseThreads, kDenseWindow, true>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDense);
+    cudaFuncSetAttribute(k_num_dense<kDenseThreads, kDenseWindow, false>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDense);
+}
+
+static int wide_window_bits(int64_t ncols) {
+    int64_t w = 32;
+    while (w < ncols && w < kWideWindowBitsMax) w <<= 1;
+    return (int)w;
+}
+
+// Symbolic launches need the bin boundaries on the host (binStartHost).
+void launch_symbolic_bins(const SymArgs &a, const int32_t *binStartHost, cudaStream_t s,
+                          int *launches) {
+    const int32_t *bs = binStartHost;
+    auto cnt = [&](int b) { return bs[b + 1] - bs[b]; };
+    if (int32_t n = cnt(SB_TINY)) {
+        k_sym_tiny<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(a, bs[SB_TINY], n);
+        ++*launches;
+    }
+    if (int32_t n = cnt(SB_HWARP)) {
+        k_sym_hash<32, kSymWarpRows, kSymWarpTable>
+            <<<(unsigned)ceil_div(n, kSymWarpRows), 32 * kSymWarpRows, kSmemSymWarp, s>>>(
+                a, bs[SB_HWARP], n);
+        ++*launches;
+    }
+    if (int32_t n = cnt(SB_HCTA)) {
+        k_sym_hash<256, 1, kSymCtaTable><<<(unsigned)n, 256, kSmemSymCta, s>>>(a, bs[SB_HCTA], n);
+        ++*launches;
+    }
+    if (int32_t n = cnt(SB_WIDE)) {
+        const int wb = wide_window_bits(a.B.n);
+        k_sym_wide<kWideThreads><<<(unsigned)n, kWideThreads, (size_t)wb / 8, s>>>(a, bs[SB_WIDE],
+                                                                                 a.B.n, wb);
+        ++*launches;
+    }
+}
+
+void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,
+                        int *launches) {
+    const int32_t n = hi - lo;
+    if (n <= 0) return;
+    switch (bin) {
+        case NB_TINY:
+            k_num_tiny<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(a, lo, n);
+            break;
+        case NB_HWARP:
+            k_num_hash<32, kNumWarpRows, kNumWarpTable>
+                <<<(unsigned)ceil_div(n, kNumWarpRows), 32 * kNumWarpRows, kSmemNumWarp, s>>>(a, lo, n);
+            break;
+        case NB_HCTA_S:
+            k_num_hash<256, 1, kNumCtaSTable><<<(unsigned)n, 256, kSmemNumCtaS, s>>>(a, lo, n);
+            break;
+        case NB_HCTA_L:
+            k_num_hash<512, 1, kNumCtaLTable><<<(unsigned)n, 512, kSmemNumCtaL, s>>>(a, lo, n);
+            break;
+        case NB_DENSE:
+            if (a.bSorted)
+                k_num_dense<kDenseThreads, kDenseWindow, true>
+                    <<<(unsigned)n, kDenseThreads, kSmemDense, s>>>(a, lo);
+            else
+                k_num_dense<kDenseThreads, kDenseWindow, false>
+                    <<<(unsigned)n, kDenseThreads, kSmemDense, s>>>(a, lo);
+            break;
+        default:
+            return;
+    }
+    ++*launches;
+}
+
+}  // namespace dbd

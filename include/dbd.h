@@ -1,0 +1,234 @@
+/*
+ * dbd.h -- C ABI of libdbd, a GB300-native (sm_103a) out-of-core row-block
+ * SpGEMM, C = A*B in CSR, that stands in for DBD's SSpMM / compute / d2h path.
+ *
+ * The reference is a program, not a library: its interface is the argv
+ * contract of bin/SSpMM, bin/compute, bin/d2h (ZIP:dbd/src/main.cpp:152-187),
+ * the .csr input and Ptr/Idx/Val.output files, and the process-global
+ * function set of ZIP:dbd/src/SSpMM.hpp:126-149.  Each entry point below names
+ * the reference function it replaces.  The CLI binaries built with this
+ * library (bin/SSpMM, bin/compute, bin/d2h, bin/debug) are thin callers of
+ * dbd_spgemm_files().
+ *
+ * Conventions
+ *   - Every function returns int: DBD_OK (0) or a negative DBD_ERR_* code;
+ *     dbd_error_string() names it and dbd_last_error() gives the message of the
+ *     last failure on a context.
+ *   - Input CSR: int32 row_ptr (n_rows+1) and col_idx (nnz), values FP64 or
+ *     FP32 (val_fp32 = 1, the reference's .csr layout; promoted to FP64 on
+ *     upload).  Columns inside a row need not be sorted.  Pointers are host
+ *     memory unless on_device = 1.
+ *   - Output CSR: int64 row_ptr, int32 col_idx, FP64 values; columns of each
+ *     row ascending and unique; structure decided by index only.
+ *   - A context owns its device memory, pinned host buffers, streams and the
+ *     writer thread; it is not thread-safe (use one per host thread).  Every
+ *     call returns with all its device work and file writes complete.
+ */
+#ifndef DBD_H
+#define DBD_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes.  The reference returns -1 with a stderr line for budget and
+ * allocation failures (ZIP:dbd/src/main.cpp:211-226, preProc.cu:57-60) and
+ * checks no CUDA or I/O return code; here every failure is reported. */
+#define DBD_OK                 0
+#define DBD_ERR_INVALID       -1  /* bad argument or malformed CSR */
+#define DBD_ERR_OOM_DEVICE    -2  /* cudaMalloc failed */
+#define DBD_ERR_OOM_HOST      -3  /* malloc / cudaMallocHost failed */
+#define DBD_ERR_BUDGET        -4  /* the product does not fit the GPU/host budgets */
+#define DBD_ERR_IO            -5  /* open/read/write/fsync failed or short */
+#define DBD_ERR_CUDA          -6  /* a CUDA runtime call failed */
+#define DBD_ERR_TIMEOUT       -7  /* a bounded wait gave up */
+#define DBD_ERR_OVERFLOW      -8  /* an index or count does not fit its type */
+#define DBD_ERR_DEVICE_CHECK  -9  /* a kernel's own consistency check fired */
+#define DBD_ERR_NO_DEVICE    -10  /* no CUDA device / library built without one */
+
+/* Timing scopes of the reference's three binaries (README "Result"):
+ * KERNEL = bin/compute, D2H = bin/d2h, IO = bin/SSpMM. */
+typedef enum {
+    DBD_SCOPE_KERNEL = 0,
+    DBD_SCOPE_D2H = 1,
+    DBD_SCOPE_IO = 2
+} dbd_scope;
+
+typedef struct dbd_ctx dbd_ctx;
+
+/* Read-only CSR operand (struct csr, ZIP:dbd/src/SSpMM.hpp:36-44, with FP64
+ * values and an explicit placement flag). */
+typedef struct {
+    int64_t n_rows;
+    int64_t n_cols;
+    int64_t nnz;
+    const int32_t *row_ptr;   /* n_rows + 1 entries */
+    const int32_t *col_idx;   /* nnz entries */
+    const void *val;          /* nnz doubles, or floats when val_fp32 */
+    int32_t val_fp32;
+    int32_t on_device;        /* 1: the three arrays are device pointers */
+} dbd_csr_view;
+
+/* Product matrix.  The library fills it; arrays it allocated are released by
+ * dbd_csr_free().  For DBD_SCOPE_KERNEL the arrays are device pointers owned
+ * by the context and valid until its next multiply (on_device = 1). */
+typedef struct {
+    int64_t n_rows;
+    int64_t n_cols;
+    int64_t nnz;
+    int64_t *row_ptr;         /* n_rows + 1 */
+    int32_t *col_idx;         /* nnz */
+    double *val;              /* nnz */
+    int32_t on_device;
+    int32_t owner;            /* 0: caller, 1: library host allocation, 2: context device memory */
+} dbd_csr_out;
+
+/* Budgets and layout (the argv of ZIP:dbd/src/main.cpp:152-187 plus the
+ * compile-time ROWS_IN_BLOCK of SSpMM.hpp:16-23). */
+typedef struct {
+    double host_gib;          /* host DRAM budget for result buffers; reference default 28 */
+    double gpu_gib;           /* device budget; reference default 22 */
+    int64_t rows_per_block;   /* 4096 (for_small_datasets) or 512 (for_large_datasets) */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t out_val_fp32;     /* Val.output as float32 (reference layout) instead of FP64 */
+    int32_t out_ptr32;        /* Ptr.output as int32 (reference layout; fails if nnz(C) >= 2^31) */
+    int32_t verbose;          /* print the reference's progress lines */
+    double io_rotate_gib;     /* > 0: +I/O output files wrap after this many GiB (disk smaller than C) */
+} dbd_config;
+
+/* Number of row bins the categoriser produces for the symbolic and numeric
+ * kernels (see dbd_stats.rows_per_bin). */
+#define DBD_NUM_BINS 8
+
+/* Counters and times of the last multiply.  Times are seconds. */
+typedef struct {
+    double t_preprocess;      /* work estimate + segmentation + categorisation ("Preprocessing", main.cpp:101) */
+    double t_compute_gpu;     /* device time of the multiply ("Compute GPU", main.cpp:103) */
+    double t_write_file;      /* writer thread busy time ("Write File", main.cpp:104) */
+    double t_kernel_exec;     /* distributor wall time of the scope ("Kernel Execution", main.cpp:105) */
+    double t_total;           /* t_preprocess + t_kernel_exec ("Total Execution", main.cpp:106) */
+    double t_d2h;             /* device->host copy busy time */
+    double t_fsync;           /* time spent in fsync at the end of +I/O */
+    double t_device_ms;       /* CUDA-event time of the whole device pipeline, ms */
+    double t_numeric_ms;      /* CUDA-event time of the numeric kernels, ms */
+    int64_t products;         /* intermediate products P = sum |B_k| over A's entries */
+    int64_t nnz_c;
+    int64_t n_blocks;
+    int64_t max_block_products;
+    int32_t criteria;         /* categoriser threshold (distributeWorkload.cpp:249-264) */
+    int32_t n_chunks;         /* device output chunks streamed */
+    int64_t blocks_per_category[3]; /* 0 dense, 1 light, 2 either (distributeWorkload.cpp:266-270) */
+    int64_t rows_per_bin[DBD_NUM_BINS];   /* numeric bins: empty, tiny, warp-hash, cta-hash S, cta-hash L, dense */
+    int64_t sym_rows_per_bin[DBD_NUM_BINS];
+    int64_t bytes_d2h;
+    int64_t bytes_written;
+    int64_t gpu_launches;     /* kernels this library launched for the multiply */
+} dbd_stats;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+
+/* Default budgets: host 28 GiB, GPU 22 GiB, 4096 rows per block, device 0. */
+void dbd_config_default(dbd_config *cfg);
+
+/* Creates a context on cfg->device and warms it up.
+ * Replaces initialize + initialize_GPU (ZIP:dbd/src/main.cpp:152-187,
+ * dbd/for_small_datasets/src/preProc.cu:23-26). */
+int dbd_create(const dbd_config *cfg, dbd_ctx **out);
+
+/* Releases everything the context owns.
+ * Replaces free_Resource + free_GPU (main.cpp:123-150, computeGPU.cu:101-132). */
+void dbd_destroy(dbd_ctx *ctx);
+
+/* Uses this CUDA stream (a cudaStream_t cast to void*) for the device
+ * pipeline instead of the context's own; NULL restores the context's. */
+int dbd_set_stream(dbd_ctx *ctx, void *stream);
+
+const char *dbd_error_string(int code);
+const char *dbd_last_error(const dbd_ctx *ctx);
+
+/* ---- files -------------------------------------------------------------- */
+
+/* Host CSR read from disk; free with dbd_csr_host_free(). */
+typedef struct {
+    int64_t n_rows, n_cols, nnz;
+    int32_t *row_ptr;
+    int32_t *col_idx;
+    double *val;
+    int32_t src_fp32;         /* 1: the file held float32 values */
+} dbd_csr_host;
+
+/* Reads <path>.dcsr (FP64 layout of this library) or <path>.csr (the
+ * reference layout: int32 nr, nc, ne; int32 ptr[nr+1]; int32 idx[ne];
+ * float32 val[ne]); if neither exists, converts the Matrix Market / .dat file
+ * at <path> the way the reference does and caches it as <path>.csr.
+ * Replaces read_CSR / make_CSR (ZIP:dbd/src/readInput.cpp:18-176). */
+int dbd_read_csr(const char *path, dbd_csr_host *out);
+void dbd_csr_host_free(dbd_csr_host *m);
+
+/* Writes <path> in the reference .csr layout (fp64 = 0, values rounded to
+ * float32) or the .dcsr FP64 layout (fp64 = 1).
+ * Replaces the cache write of make_CSR (readInput.cpp:166-175). */
+int dbd_write_csr(const char *path, const dbd_csr_view *m, int fp64);
+
+/* ---- the reference's stage functions ------------------------------------ */
+
+/* Uploads A (resp. B) to the device; device views are used in place.
+ * Replaces initialize_A / initialize_B (preProc.cu:28-46). */
+int dbd_load_a(dbd_ctx *ctx, const dbd_csr_view *a);
+int dbd_load_b(dbd_ctx *ctx, const dbd_csr_view *b);
+
+/* Work estimate, row-block segmentation and categorisation of the loaded
+ * A*B.  Returns the number of row blocks in *num_blocks.
+ * Replaces divide_Blocks + get_UpperBound (main.cpp:259-310,
+ * preProc.cu:142-156). */
+int dbd_divide_blocks(dbd_ctx *ctx, int64_t *num_blocks);
+
+/* Per-block products (block_Info, main.cpp:279) and category
+ * (analyze_Block, distributeWorkload.cpp:266-270) of the last
+ * dbd_divide_blocks; arrays of num_blocks entries (either may be NULL). */
+int dbd_block_info(const dbd_ctx *ctx, int64_t *products, int32_t *category);
+
+/* Runs the multiply over all row blocks in the given scope: the device
+ * result (KERNEL), plus the complete C in pinned host memory (D2H), plus
+ * Ptr.output / Idx.output / Val.output in out_dir (IO).
+ * Replaces distribute_Workload + compute_GPU + write_File + write_Ptr
+ * (distributeWorkload.cpp:25-223, computeGPU.cu:15-98,
+ * writeFile.cpp:13-196). */
+int dbd_distribute_workload(dbd_ctx *ctx, dbd_scope scope, const char *out_dir);
+
+/* The product of the last dbd_distribute_workload: device arrays for KERNEL,
+ * pinned host arrays for D2H when C fit the host budget.  Owned by the
+ * context (valid until its next multiply). */
+int dbd_result(dbd_ctx *ctx, dbd_csr_out *c);
+
+/* Copies the product of the last multiply (device- or host-resident) into
+ * caller-provided host arrays sized from dbd_result: row_ptr n_rows+1,
+ * col_idx and val nnz entries.  For FFI callers that cannot read device
+ * memory; the reference hands results back only through Ptr/Idx/Val.output. */
+int dbd_result_copy(dbd_ctx *ctx, int64_t *row_ptr, int32_t *col_idx, double *val);
+
+int dbd_get_stats(const dbd_ctx *ctx, dbd_stats *st);
+
+/* ---- one-shot entry points ----------------------------------------------- */
+
+/* C = A*B: load, divide, distribute, and (c != NULL) hand back the product:
+ * for DBD_SCOPE_KERNEL a device view owned by the context, for D2H/IO a host
+ * copy the caller frees with dbd_csr_free() (when C fits host memory). */
+int dbd_spgemm(dbd_ctx *ctx, const dbd_csr_view *a, const dbd_csr_view *b,
+               dbd_scope scope, const char *out_dir, dbd_csr_out *c, dbd_stats *st);
+
+/* The argv-equivalent of bin/SSpMM | compute | d2h: path_b may be NULL for
+ * A*A (main.cpp:152-176). */
+int dbd_spgemm_files(dbd_ctx *ctx, const char *path_a, const char *path_b,
+                     dbd_scope scope, const char *out_dir, dbd_stats *st);
+
+void dbd_csr_free(dbd_csr_out *c);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DBD_H */

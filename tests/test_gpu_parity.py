@@ -1,0 +1,283 @@
+"""GPU parity: libdbd through its C ABI against the oracle.
+
+Structure (row_ptr, col_idx) must be bit-exact.  Values are FP64 and must
+satisfy |c - oracle| <= 1e-12 * sum|a_ik * b_kj| per entry (the oracle computes
+that scale; it equals 1e-12 relative wherever no cancellation occurs).  Rows
+on the register path (<= 32 products) are summed in the oracle's order and
+must match bit for bit.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+import dbd_gb300 as dbd
+from dbd_gb300 import generators as gen
+from dbd_gb300.csr import CSR
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def check(C, A, B, orc, exact=False):
+    Cp, Ci, Cv, Ca = orc.spgemm(A, B, with_abs=True)
+    assert C.n_rows == A.n_rows and C.n_cols == B.n_cols
+    assert np.array_equal(C.row_ptr, Cp), "row_ptr"
+    assert np.array_equal(C.col_idx, Ci), "col_idx"
+    err = np.abs(C.val - Cv)
+    if exact:
+        assert np.array_equal(C.val.view(np.uint64), Cv.view(np.uint64))
+    assert np.all(err <= TOL * Ca), f"max err {err.max()} scale {Ca[np.argmax(err)]}"
+    rel = err / np.maximum(np.abs(Cv), 1e-300)
+    return float(rel.max(initial=0.0)), float(rel.mean()) if rel.size else 0.0
+
+
+def bins_used(st):
+    return [i for i, v in enumerate(st["rows_per_bin"]) if v]
+
+
+def test_laplacian256_kernel_scope_bit_exact(ctx, orc):
+    L = gen.laplacian_2d(256)
+    res = ctx.spgemm(L, scope="kernel")
+    check(res.C, L, L, orc, exact=True)
+    st = res.stats
+    assert st["products"] == 1629192 and st["nnz_c"] == 846852
+    assert st["n_blocks"] == 16
+    assert st["gpu_launches"] > 0
+
+
+@pytest.mark.parametrize("scope", ["d2h", "io"])
+def test_laplacian256_other_scopes(ctx, orc, scope, tmp_path):
+    L = gen.laplacian_2d(256)
+    res = ctx.spgemm(L, scope=scope, out_dir=str(tmp_path))
+    if scope == "d2h":
+        check(res.C, L, L, orc, exact=True)
+    else:
+        Cp, Ci, Cv = orc.spgemm(L)
+        ptr = np.fromfile(tmp_path / "Ptr.output", np.int64)
+        idx = np.fromfile(tmp_path / "Idx.output", np.int32)
+        val = np.fromfile(tmp_path / "Val.output", np.float64)
+        assert np.array_equal(ptr, Cp) and np.array_equal(idx, Ci) and np.array_equal(val, Cv)
+        assert res.stats["bytes_written"] == 8 * (L.n_rows + 1) + 12 * Cv.size
+
+
+def test_io_reference_layout(orc, tmp_path):
+    """DBD_OUT_FP32 / ptr32: the reference's int32 Ptr, int32 Idx, float32 Val."""
+    L = gen.laplacian_2d(64)
+    with dbd.Context(cpu_gib=4, gpu_gib=4, out_val_fp32=True, out_ptr32=True) as c:
+        c.spgemm(L, scope="io", out_dir=str(tmp_path))
+    Cp, Ci, Cv = orc.spgemm(L)
+    assert np.array_equal(np.fromfile(tmp_path / "Ptr.output", np.int32), Cp.astype(np.int32))
+    assert np.array_equal(np.fromfile(tmp_path / "Idx.output", np.int32), Ci)
+    assert np.array_equal(np.fromfile(tmp_path / "Val.output", np.float32), Cv.astype(np.float32))
+
+
+@pytest.mark.parametrize("name", ["kat_bhsparse.npz", "cage4_ref.npz", "lap16_ref.npz", "rmat9_ref.npz",
+                                  "quirk_ref.npz"])
+def test_golden_operands(ctx, orc, name):
+    d = np.load(os.path.join(GOLDEN, name))
+    A = CSR(*d["a_shape"], d["a_ptr"], d["a_idx"], d["a_val"])
+    B = CSR(*d["b_shape"], d["b_ptr"], d["b_idx"], d["b_val"])
+    res = ctx.spgemm(A, B, scope="kernel")
+    check(res.C, A, B, orc)
+    if name != "quirk_ref.npz":
+        Cp_r, Ci_r, Cv_r, dups = orc.canonicalise(d["off"], d["cnt"], d["idx"], d["val"])
+        assert dups == 0
+        assert np.array_equal(res.C.row_ptr, Cp_r) and np.array_equal(res.C.col_idx, Ci_r)
+        assert np.allclose(res.C.val, Cv_r, rtol=2e-6, atol=0)
+
+
+def test_cage4_from_reference_csr_file(ctx, orc):
+    M = dbd.read_CSR(os.path.join(GOLDEN, "cage4"))
+    res = ctx.spgemm(M, scope="kernel")
+    check(res.C, M, M, orc)
+
+
+@pytest.mark.parametrize("scale,ef,seed", [(10, 8, 1), (12, 8, 2), (14, 8, 3), (13, 16, 4)])
+def test_rmat_small(ctx, orc, scale, ef, seed):
+    A = gen.rmat(scale, ef, seed=seed)
+    res = ctx.spgemm(A, scope="kernel")
+    check(res.C, A, A, orc)
+
+
+def test_every_numeric_bin_exercised(ctx, orc):
+    """A matrix whose rows fall in every bin (tiny, warp hash, both CTA hash
+    sizes, dense windows), rectangular with n > one dense window."""
+    rng = np.random.default_rng(11)
+    m, k, n = 600, 3000, 20000
+    rows, cols = [], []
+    lens = np.concatenate([rng.integers(1, 3, 200), rng.integers(5, 20, 150), rng.integers(40, 80, 100),
+                           rng.integers(150, 300, 100), rng.integers(1500, 2500, 50)])
+    rng.shuffle(lens)
+    for r in range(m):
+        c = rng.choice(k, size=int(lens[r]), replace=False)
+        rows.append(np.full(c.size, r))
+        cols.append(c)
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    A = gen._from_coo(m, k, rows, cols, rng.uniform(-1, 1, rows.size))
+    br, bc = gen._distinct_cols(rng, rng.poisson(6, k).astype(np.int64), n)
+    B = gen._from_coo(k, n, br, bc, rng.uniform(-1, 1, br.size))
+    res = ctx.spgemm(A, B, scope="kernel")
+    check(res.C, A, B, orc)
+    used = bins_used(res.stats)
+    assert set(used) >= {1, 2, 3, 4, 5}, res.stats["rows_per_bin"]
+
+
+def test_dense_rows_unsorted_b(ctx, orc):
+    """Dense-window rows with B rows out of column order take the rescanning path."""
+    rng = np.random.default_rng(5)
+    A = gen.uniform_rows(64, 1500, seed=1, n_cols=4000, dist="uniform")
+    B = gen.uniform_rows(4000, 12, seed=2, n_cols=30000, dist="uniform")
+    perm_idx = B.col_idx.copy()
+    for r in range(B.n_rows):
+        s, e = B.row_ptr[r], B.row_ptr[r + 1]
+        p = rng.permutation(e - s)
+        perm_idx[s:e] = B.col_idx[s:e][p]
+        B.val[s:e] = B.val[s:e][p]
+    B = CSR(B.n_rows, B.n_cols, B.row_ptr, perm_idx, B.val)
+    res = ctx.spgemm(A, B, scope="kernel")
+    check(res.C, A, B, orc)
+    assert res.stats["rows_per_bin"][5] > 0
+
+
+def test_edge_cases(ctx, orc):
+    z = np.zeros(0)
+    cases = [
+        (CSR(0, 5, np.zeros(1, np.int32), np.zeros(0, np.int32), z), CSR(5, 3, np.zeros(6, np.int32), np.zeros(0, np.int32), z)),
+        (CSR(4, 4, np.zeros(5, np.int32), np.zeros(0, np.int32), z), None),
+        (CSR(1, 1, np.array([0, 1], np.int32), np.array([0], np.int32), np.array([3.0])), None),
+        (CSR(3, 2, np.array([0, 2, 2, 4], np.int32), np.array([1, 0, 0, 1], np.int32), np.array([1., 2., 3., 4.])),
+         CSR(2, 7, np.array([0, 3, 3], np.int32), np.array([6, 0, 2], np.int32), np.array([1., -1., .5]))),
+        # duplicate columns inside a row of A and of B
+        (CSR(2, 3, np.array([0, 3, 4], np.int32), np.array([1, 1, 2, 0], np.int32), np.array([1., 2., 3., 4.])),
+         CSR(3, 3, np.array([0, 1, 3, 4], np.int32), np.array([2, 1, 1, 0], np.int32), np.array([1., 1., 1., 1.]))),
+    ]
+    for A, B in cases:
+        Bx = A if B is None else B
+        res = ctx.spgemm(A, B, scope="kernel")
+        check(res.C, A, Bx, orc)
+
+
+def test_fp32_operands_promoted(ctx, orc):
+    A = gen.rmat(11, 8, seed=9)
+    A32 = CSR(A.n_rows, A.n_cols, A.row_ptr, A.col_idx, A.val.astype(np.float32))
+    res = ctx.spgemm(A32, scope="kernel")
+    A64 = CSR(A.n_rows, A.n_cols, A.row_ptr, A.col_idx, A.val.astype(np.float32).astype(np.float64))
+    check(res.C, A64, A64, orc)
+
+
+def test_device_resident_operands(ctx, orc):
+    torch = pytest.importorskip("torch")
+    A = gen.rmat(12, 8, seed=4)
+    p = torch.from_numpy(A.row_ptr).cuda()
+    i = torch.from_numpy(A.col_idx).cuda()
+    v = torch.from_numpy(A.val).cuda()
+    D = CSR.from_device(A.n_rows, A.n_cols, A.nnz, p.data_ptr(), i.data_ptr(), v.data_ptr())
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        res = ctx.spgemm(D, scope="kernel")
+    finally:
+        ctx.set_stream(None)
+    check(res.C, A, A, orc)
+
+
+def test_invalid_operands_rejected(ctx):
+    bad = CSR(2, 2, np.array([0, 1, 2], np.int32), np.array([0, 5], np.int32), np.array([1.0, 1.0]))
+    with pytest.raises(dbd.DBDError) as ei:
+        ctx.spgemm(bad)
+    assert ei.value.code == -1
+    A = CSR(2, 3, np.array([0, 1, 2], np.int32), np.array([0, 1], np.int32), np.array([1.0, 1.0]))
+    with pytest.raises(dbd.DBDError):
+        ctx.spgemm(A, A)  # 2x3 * 2x3
+    torch = pytest.importorskip("torch")
+    p = torch.tensor([0, 2, 1], dtype=torch.int32, device="cuda")  # decreasing row_ptr
+    i = torch.tensor([0, 1], dtype=torch.int32, device="cuda")
+    v = torch.ones(2, dtype=torch.float64, device="cuda")
+    D = CSR.from_device(2, 2, 2, p.data_ptr(), i.data_ptr(), v.data_ptr())
+    with pytest.raises(dbd.DBDError) as ei:
+        ctx.spgemm(D)
+    assert ei.value.code == -1
+
+
+def test_out_of_core_chunks_and_ring(orc, tmp_path):
+    """Small budgets force several device output chunks, a host ring and the
+    writer's ordered appends; files must still hold the exact product."""
+    A = gen.uniform_rows(1 << 14, 10, seed=6, dist="uniform")
+    Cp, Ci, Cv, Ca = orc.spgemm(A, with_abs=True)
+    out_bytes = 12 * Cv.size
+    gib = 1024 ** 3
+    work = 4 << 20  # operands and work arrays of this size, generously
+    with dbd.Context(cpu_gib=1, gpu_gib=(work + 0.5 * out_bytes) / gib, rows_per_block=512) as c:
+        res = c.spgemm(A, scope="io", out_dir=str(tmp_path))
+        assert res.stats["n_chunks"] >= 3
+        ptr = np.fromfile(tmp_path / "Ptr.output", np.int64)
+        idx = np.fromfile(tmp_path / "Idx.output", np.int32)
+        val = np.fromfile(tmp_path / "Val.output", np.float64)
+        assert np.array_equal(ptr, Cp) and np.array_equal(idx, Ci)
+        assert np.all(np.abs(val - Cv) <= TOL * Ca)
+        res = c.spgemm(A, scope="d2h")
+        assert res.stats["n_chunks"] >= 3
+        check(res.C, A, A, orc)
+
+
+def test_io_rotation_bounds_file_size(tmp_path):
+    A = gen.rmat(13, 8, seed=7)
+    with dbd.Context(cpu_gib=1, gpu_gib=0.06, rows_per_block=512, io_rotate_gib=0.001) as c:
+        res = c.spgemm(A, scope="io", out_dir=str(tmp_path))
+    assert os.path.getsize(tmp_path / "Idx.output") <= 0.001 * 1024 ** 3
+    assert res.stats["bytes_written"] >= 12 * res.stats["nnz_c"]
+
+
+def test_stage_functions_mirror_reference(orc):
+    """initialize_A/B -> divide_Blocks -> distribute_Workload, as main.cpp drives them."""
+    A = gen.rmat(13, 8, seed=8)
+    with dbd.Context(cpu_gib=4, gpu_gib=4, rows_per_block=4096) as c:
+        c.initialize_A(A)
+        c.initialize_B(A)
+        nb = c.divide_Blocks()
+        assert nb == 2
+        prods, cats = c.block_info(nb)
+        rp, tot = orc.row_products(A, A)
+        upp = orc.exclusive_scan(rp)
+        _, info, _ = orc.divide_blocks(A.n_rows, upp, 4096)
+        assert np.array_equal(prods, info)
+        crit = orc.criteria(info, 4096, tot)
+        assert [orc.analyze_block(crit, int(p // 4096)) for p in prods] == cats.tolist()
+        st = c.distribute_Workload("kernel")
+        assert st["criteria"] == crit
+        check(c.result(), A, A, orc)
+
+
+def test_cli_binaries(tmp_path, orc):
+    L = gen.laplacian_2d(32)
+    dbd.write_CSR(str(tmp_path / "lap.dcsr"), L, fp64=True)
+    for name in ("compute", "d2h", "SSpMM", "debug"):
+        out = subprocess.run([os.path.join(ROOT, "dbd_gb300", "bin", name), "4", "4", "lap"], cwd=tmp_path,
+                             capture_output=True, text=True, timeout=120)
+        assert out.returncode == 0, out.stderr
+        for line in ("Preprocessing\t\t", "Compute GPU\t\t", "Kernel Execution\t", "Total Execution\t\t"):
+            assert line in out.stdout
+    Cp, Ci, Cv = orc.spgemm(L)
+    assert np.array_equal(np.fromfile(tmp_path / "Idx.output", np.int32), Ci)
+    out = subprocess.run([os.path.join(ROOT, "dbd_gb300", "bin", "SSpMM")], cwd=tmp_path, capture_output=True,
+                         text=True, timeout=60)
+    assert out.returncode != 0 and "Invalid Arguments." in out.stdout
+
+
+def test_rmat18_full_size_properties(ctx, orc):
+    """The scale-18 workload at full size: structure equal to the oracle's,
+    values within the tolerance, per-row sums (a size-independent checksum)
+    equal to A*(A*1)."""
+    A = gen.rmat(18, 8, seed=0)
+    res = ctx.spgemm(A, scope="kernel")
+    C = res.C
+    assert res.stats["products"] == 867505158
+    relmax, relmean = check(C, A, A, orc)
+    S = A.to_scipy()
+    ones = np.ones(A.n_cols)
+    rows = np.add.reduceat(np.concatenate([C.val, [0.0]]), np.minimum(C.row_ptr[:-1], C.val.size))
+    rows[np.diff(C.row_ptr) == 0] = 0.0
+    assert np.allclose(rows, S @ (S @ ones), rtol=1e-10)
+    print(f"rmat18: nnz(C)={C.nnz} max rel err {relmax:.3e} mean {relmean:.3e}")
