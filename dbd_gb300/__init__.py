@@ -95,7 +95,7 @@ class Context:
     """A libdbd context: device, budgets, streams, buffers (one per host thread)."""
 
     def __init__(self, cpu_gib=28.0, gpu_gib=22.0, rows_per_block=4096, device=0, out_val_fp32=False,
-                 out_ptr32=False, verbose=False, io_rotate_gib=0.0):
+                 out_ptr32=False, verbose=False, io_rotate_gib=0.0, time_kernels=False):
         self._lib = _ffi.load()
         cfg = _ffi.Config()
         self._lib.dbd_config_default(C.byref(cfg))
@@ -106,6 +106,7 @@ class Context:
         cfg.out_val_fp32 = int(bool(out_val_fp32))
         cfg.out_ptr32 = int(bool(out_ptr32))
         cfg.verbose = int(bool(verbose))
+        cfg.time_kernels = int(bool(time_kernels))
         cfg.io_rotate_gib = float(io_rotate_gib)
         h = C.c_void_p()
         _check(self._lib.dbd_create(C.byref(cfg), C.byref(h)))

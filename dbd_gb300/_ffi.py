@@ -40,7 +40,7 @@ class CsrHost(C.Structure):
 class Config(C.Structure):
     _fields_ = [("host_gib", C.c_double), ("gpu_gib", C.c_double), ("rows_per_block", C.c_int64),
                 ("device", C.c_int32), ("out_val_fp32", C.c_int32), ("out_ptr32", C.c_int32),
-                ("verbose", C.c_int32), ("io_rotate_gib", C.c_double)]
+                ("verbose", C.c_int32), ("time_kernels", C.c_int32), ("io_rotate_gib", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -51,7 +51,9 @@ class Stats(C.Structure):
                 ("max_block_products", C.c_int64), ("criteria", C.c_int32), ("n_chunks", C.c_int32),
                 ("blocks_per_category", C.c_int64 * 3), ("rows_per_bin", C.c_int64 * NUM_BINS),
                 ("sym_rows_per_bin", C.c_int64 * NUM_BINS), ("bytes_d2h", C.c_int64),
-                ("bytes_written", C.c_int64), ("gpu_launches", C.c_int64)]
+                ("bytes_written", C.c_int64), ("gpu_launches", C.c_int64), ("t_analysis_ms", C.c_double),
+                ("t_sym_bin_ms", C.c_double * NUM_BINS), ("t_scan_ms", C.c_double),
+                ("t_num_bin_ms", C.c_double * NUM_BINS)]
 
     def as_dict(self):
         d = {}

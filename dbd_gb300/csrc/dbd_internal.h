@@ -73,9 +73,8 @@ struct SymArgs {
     uint32_t *ctr;
     int *err;
 };
-// Launches the symbolic kernel of every non-empty bin; binStartHost holds the
-// bin boundaries of the row list (copied from the device after binning).
-void launch_symbolic_bins(const SymArgs &a, const int32_t *binStartHost, cudaStream_t s, int *launches);
+// Launches the symbolic kernel of bin `bin` over list[begin, begin + n).
+void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cudaStream_t s, int *launches);
 void launch_f32_to_f64(const float *src, double *dst, int64_t n, cudaStream_t s);
 void launch_validate_ptr(const int32_t *ptr, int64_t m, int64_t nnz, int *flag, cudaStream_t s);
 void launch_validate_idx(const int32_t *idx, int64_t nnz, int64_t ncols, int *flag, cudaStream_t s);

@@ -150,9 +150,66 @@ struct dbd_ctx {
     cudaEvent_t evNumA = nullptr, evNumB = nullptr;
     dbd_stats stats;
     int launches = 0;
+
+    // One stream per bin so that the kernels of different bins overlap.
+    cudaStream_t bin_streams[kMaxBins] = {};
+    // Event pools, reset at the start of every multiply (all earlier work is
+    // complete by then): timing events (time_kernels) and fork/join events.
+    std::vector<cudaEvent_t> tpool, spool;
+    size_t tused = 0, sused = 0;
+    struct Timed {
+        int kind;  // 0 symbolic bin, 1 numeric bin, 2 scan + numeric binning
+        int bin;
+        cudaEvent_t a, b;
+    };
+    std::vector<Timed> timed;
+
+    cudaEvent_t time_ev(cudaStream_t s) {
+        if (!cfg.time_kernels) return nullptr;
+        if (tused == tpool.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            tpool.push_back(e);
+        }
+        cudaEvent_t e = tpool[tused++];
+        cudaEventRecord(e, s);
+        return e;
+    }
+    cudaEvent_t sync_ev() {
+        if (sused == spool.size()) {
+            cudaEvent_t e;
+            cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+            spool.push_back(e);
+        }
+        return spool[sused++];
+    }
 };
 
 namespace {
+
+// Fork the context's stream into per-bin streams and join them back.
+struct Fork {
+    dbd_ctx *c;
+    cudaEvent_t start;
+    bool used[kMaxBins] = {};
+    explicit Fork(dbd_ctx *ctx) : c(ctx) {
+        start = c->sync_ev();
+        cudaEventRecord(start, c->stream);
+    }
+    cudaStream_t stream(int b) {
+        if (!used[b]) cudaStreamWaitEvent(c->bin_streams[b], start, 0);
+        used[b] = true;
+        return c->bin_streams[b];
+    }
+    void join() {
+        for (int b = 0; b < kMaxBins; ++b) {
+            if (!used[b]) continue;
+            cudaEvent_t e = c->sync_ev();
+            cudaEventRecord(e, c->bin_streams[b]);
+            cudaStreamWaitEvent(c->stream, e, 0);
+        }
+    }
+};
 
 int set_err(dbd_ctx *c, int code, const std::string &msg) {
     if (c) c->last_error = msg;
@@ -280,6 +337,8 @@ int divide_blocks(dbd_ctx *c) {
     if (A.n != B.m) return set_err(c, DBD_ERR_INVALID, "inner dimensions differ (A.n_cols != B.n_rows)");
     const auto t0 = Clock::now();
     c->launches = 0;
+    c->tused = c->sused = 0;
+    c->timed.clear();
     c->m = A.m;
     c->ncols = B.n;
     const int64_t m = A.m;
@@ -376,13 +435,26 @@ int symbolic(dbd_ctx *c) {
     sa.rowNnz = c->rowNnz.as<int32_t>();
     sa.ctr = nullptr;
     sa.err = c->err.as<int>();
-    launch_symbolic_bins(sa, c->symStart_h, c->stream, &c->launches);
+    // Bins run concurrently, one stream each (heaviest first).
+    static const int sorder[] = {SB_WIDE, SB_HCTA, SB_HWARP, SB_TINY};
+    Fork fk(c);
+    for (int b : sorder) {
+        const int32_t n = c->symStart_h[b + 1] - c->symStart_h[b];
+        if (n <= 0) continue;
+        cudaStream_t s = fk.stream(b);
+        cudaEvent_t e0 = c->time_ev(s);
+        launch_symbolic_bin(sa, b, c->symStart_h[b], n, s, &c->launches);
+        if (e0) c->timed.push_back({0, b, e0, c->time_ev(s)});
+    }
+    fk.join();
+    cudaEvent_t es = c->time_ev(c->stream);
     launch_row_scan(m, c->rowNnz.as<int32_t>(), c->part.as<int64_t>(), c->Cp.as<int64_t>(), c->stream);
     launch_num_bins(m, c->A.dev.ptr, c->rowP.as<int64_t>(), c->rowNnz.as<int32_t>(), c->numBin.as<uint8_t>(),
                     c->stream, c->num_sms);
     Binning nb{c->numBin.as<uint8_t>(), c->numList.as<int32_t>(), c->hist.as<int32_t>(),
                c->numTileOff.as<int32_t>(), c->numStart.as<int32_t>()};
     launch_bin_lists(m, nb, NB_COUNT, c->stream);
+    if (es) c->timed.push_back({2, 0, es, c->time_ev(c->stream)});
     c->launches += 7;
     CK(c, cudaGetLastError());
     CK(c, cudaMemcpyAsync(&c->nnzC, c->Cp.as<int64_t>() + m, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
@@ -414,13 +486,20 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     na.err = c->err.as<int>();
     const int64_t t0 = r0 / kTileRows;
     const int64_t t1 = (r1 >= c->m) ? c->ntiles : r1 / kTileRows;
-    // Heaviest bins first so that their long CTAs start early.
+    // Bins run concurrently, one stream each; heaviest first so that their
+    // long CTAs start early.
     static const int order[] = {NB_DENSE, NB_HCTA_L, NB_HCTA_S, NB_HWARP, NB_TINY};
+    Fork fk(c);
     for (int b : order) {
         const int32_t lo = c->numTileOff_h[(size_t)t0 * kMaxBins + b];
         const int32_t hi = c->numTileOff_h[(size_t)t1 * kMaxBins + b];
-        launch_numeric_bin(na, b, lo, hi, c->stream, &c->launches);
+        if (hi <= lo) continue;
+        cudaStream_t s = fk.stream(b);
+        cudaEvent_t e0 = c->time_ev(s);
+        launch_numeric_bin(na, b, lo, hi, s, &c->launches);
+        if (e0) c->timed.push_back({1, b, e0, c->time_ev(s)});
     }
+    fk.join();
 }
 
 // Chunks of consecutive row blocks whose output fits cap_entries.
@@ -788,6 +867,16 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     c->stats.t_d2h = t_d2h_issue;
     c->stats.bytes_d2h = bytes_d2h;
     c->stats.gpu_launches = c->launches;
+    float mta = 0.f;
+    cudaEventElapsedTime(&mta, c->evStart, c->evPre);
+    c->stats.t_analysis_ms = mta;
+    for (const auto &t : c->timed) {
+        float x = 0.f;
+        if (cudaEventElapsedTime(&x, t.a, t.b) != cudaSuccess) continue;
+        if (t.kind == 0) c->stats.t_sym_bin_ms[t.bin] += x;
+        else if (t.kind == 1) c->stats.t_num_bin_ms[t.bin] += x;
+        else c->stats.t_scan_ms += x;
+    }
     c->last_scope = scope;
     return DBD_OK;
 }
@@ -848,6 +937,12 @@ int dbd_create(const dbd_config *cfg_in, dbd_ctx **out) {
         return DBD_ERR_CUDA;
     }
     c->stream = c->own_stream;
+    for (int b = 0; b < kMaxBins; ++b) {
+        if (cudaStreamCreateWithFlags(&c->bin_streams[b], cudaStreamNonBlocking) != cudaSuccess) {
+            dbd_destroy(c);
+            return DBD_ERR_CUDA;
+        }
+    }
     cudaEventCreate(&c->evStart);
     cudaEventCreate(&c->evPre);
     cudaEventCreate(&c->evSym);
@@ -878,6 +973,14 @@ void dbd_destroy(dbd_ctx *c) {
     c->hCv.release();
     for (cudaEvent_t e : {c->evStart, c->evPre, c->evSym, c->evEnd, c->evNumA, c->evNumB})
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->tpool) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->spool) cudaEventDestroy(e);
+    for (int b = 0; b < kMaxBins; ++b) {
+        if (c->bin_streams[b]) {
+            cudaStreamSynchronize(c->bin_streams[b]);
+            cudaStreamDestroy(c->bin_streams[b]);
+        }
+    }
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     delete c;

@@ -553,31 +553,30 @@ static int wide_window_bits(int64_t ncols) {
     return (int)w;
 }
 
-// Symbolic launches need the bin boundaries on the host (binStartHost).
-void launch_symbolic_bins(const SymArgs &a, const int32_t *binStartHost, cudaStream_t s,
-                          int *launches) {
-    const int32_t *bs = binStartHost;
-    auto cnt = [&](int b) { return bs[b + 1] - bs[b]; };
-    if (int32_t n = cnt(SB_TINY)) {
-        k_sym_tiny<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(a, bs[SB_TINY], n);
-        ++*launches;
+// Symbolic kernel of bin b over list[begin, begin + n).
+void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cudaStream_t s,
+                         int *launches) {
+    if (n <= 0) return;
+    switch (bin) {
+        case SB_TINY:
+            k_sym_tiny<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(a, begin, n);
+            break;
+        case SB_HWARP:
+            k_sym_hash<32, kSymWarpRows, kSymWarpTable>
+                <<<(unsigned)ceil_div(n, kSymWarpRows), 32 * kSymWarpRows, kSmemSymWarp, s>>>(a, begin, n);
+            break;
+        case SB_HCTA:
+            k_sym_hash<256, 1, kSymCtaTable><<<(unsigned)n, 256, kSmemSymCta, s>>>(a, begin, n);
+            break;
+        case SB_WIDE: {
+            const int wb = wide_window_bits(a.B.n);
+            k_sym_wide<kWideThreads><<<(unsigned)n, kWideThreads, (size_t)wb / 8, s>>>(a, begin, a.B.n, wb);
+            break;
+        }
+        default:
+            return;
     }
-    if (int32_t n = cnt(SB_HWARP)) {
-        k_sym_hash<32, kSymWarpRows, kSymWarpTable>
-            <<<(unsigned)ceil_div(n, kSymWarpRows), 32 * kSymWarpRows, kSmemSymWarp, s>>>(
-                a, bs[SB_HWARP], n);
-        ++*launches;
-    }
-    if (int32_t n = cnt(SB_HCTA)) {
-        k_sym_hash<256, 1, kSymCtaTable><<<(unsigned)n, 256, kSmemSymCta, s>>>(a, bs[SB_HCTA], n);
-        ++*launches;
-    }
-    if (int32_t n = cnt(SB_WIDE)) {
-        const int wb = wide_window_bits(a.B.n);
-        k_sym_wide<kWideThreads><<<(unsigned)n, kWideThreads, (size_t)wb / 8, s>>>(a, bs[SB_WIDE],
-                                                                                 a.B.n, wb);
-        ++*launches;
-    }
+    ++*launches;
 }
 
 void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,

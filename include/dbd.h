@@ -96,6 +96,7 @@ typedef struct {
     int32_t out_val_fp32;     /* Val.output as float32 (reference layout) instead of FP64 */
     int32_t out_ptr32;        /* Ptr.output as int32 (reference layout; fails if nnz(C) >= 2^31) */
     int32_t verbose;          /* print the reference's progress lines */
+    int32_t time_kernels;     /* record CUDA events around every kernel family (dbd_stats.t_*_bin_ms) */
     double io_rotate_gib;     /* > 0: +I/O output files wrap after this many GiB (disk smaller than C) */
 } dbd_config;
 
@@ -126,6 +127,10 @@ typedef struct {
     int64_t bytes_d2h;
     int64_t bytes_written;
     int64_t gpu_launches;     /* kernels this library launched for the multiply */
+    double t_analysis_ms;     /* with time_kernels: work estimate + binning kernels */
+    double t_sym_bin_ms[DBD_NUM_BINS];  /* with time_kernels: symbolic kernel of each bin */
+    double t_scan_ms;         /* with time_kernels: row_ptr scan + numeric binning */
+    double t_num_bin_ms[DBD_NUM_BINS];  /* with time_kernels: numeric kernels of each bin, summed over chunks */
 } dbd_stats;
 
 /* ---- lifecycle ---------------------------------------------------------- */
