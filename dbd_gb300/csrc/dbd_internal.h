@@ -86,7 +86,7 @@ struct NumArgs {
     int64_t outBase;      // Cp value stored at out[0]
     int32_t *Ci;
     double *Cv;
-    int32_t *cursor;      // nnz(A) scratch for the dense windows
+    int32_t *state;       // 2 * nnz(A) scratch for the dense windows (cursor, next column)
     int bSorted;          // B's rows have ascending columns
     int *err;
 };

@@ -360,7 +360,7 @@ int divide_blocks(dbd_ctx *c) {
     CK(c, c->numStart.ensure(sizeof(int32_t) * (kMaxBins + 1)));
     CK(c, c->part.ensure(sizeof(int64_t) * (size_t)(ceil_div(m, kScanTile) + 1)));
     CK(c, c->Cp.ensure(sizeof(int64_t) * (mm + 1)));
-    CK(c, c->cursor.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(A.nnz, 1)));
+    CK(c, c->cursor.ensure(2 * sizeof(int32_t) * (size_t)std::max<int64_t>(A.nnz, 1)));
     CK(c, c->err.ensure(sizeof(int)));
     CK(c, c->blockP.ensure(sizeof(int64_t) * (size_t)std::max<int64_t>(c->nblocks, 1)));
 
@@ -481,7 +481,7 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     na.outBase = outBase;
     na.Ci = Ci;
     na.Cv = Cv;
-    na.cursor = c->cursor.as<int32_t>();
+    na.state = c->cursor.as<int32_t>();
     na.bSorted = opB_sorted(c);
     na.err = c->err.as<int>();
     const int64_t t0 = r0 / kTileRows;

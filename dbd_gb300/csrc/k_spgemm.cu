@@ -10,13 +10,21 @@
 //   tiny rows   (P_r <= 32)     one warp per row, products held one per lane,
 //                               duplicates found with __match_any_sync and
 //                               summed in Gustavson order (bit-exact FP64)
-//   warp / CTA hash rows        open-addressing hash tables in shared memory
-//                               (keys int32, values FP64), compacted and
-//                               bitonic-sorted in place by column
-//   wide rows   (symbolic)      shared-memory bitmap over column windows
-//   dense rows  (numeric)       shared-memory FP64 dense window of 8192
-//                               columns swept across the row with per-entry
-//                               cursors into B, written out in column order
+//   warp hash rows              one warp per row, open-addressing hash table
+//                               in shared memory (keys int32, values FP64)
+//   CTA hash rows               one CTA per row; the row's A entries and the
+//                               prefix of their B lengths are staged in shared
+//                               memory so that every thread takes consecutive
+//                               products (coalesced B loads, no idle warps);
+//                               compacted and bitonic-sorted in place
+//   wide rows   (symbolic)      shared bitmap over column windows, bits set
+//                               once per distinct word per warp step
+//   dense rows  (numeric)       shared FP64 dense window of 8192 columns
+//                               swept across the row; one warp per A entry
+//                               scans its sorted B row from a cursor, 32
+//                               products per step, the window's end found by
+//                               ballot; entries with nothing in the window are
+//                               skipped by their next column
 //
 // Structure is decided by index only (a column belongs to a row as soon as a
 // product lands on it).  Products are rounded to FP64 before accumulation
@@ -42,9 +50,11 @@ __device__ __forceinline__ uint32_t hslot(int32_t c, int shift) {
 
 __device__ __forceinline__ void raise(int *err, int code) { atomicCAS(err, 0, code); }
 
-// One warp's view of up to 32 consecutive entries of an A row, for the
-// flattened enumeration of their products: product t (0 <= t < total) comes
-// from the lane whose inclusive length prefix first exceeds t.
+// ---------------------------------------------------------------------------
+// Warp-level enumeration of the products of up to 32 consecutive A entries:
+// product t (0 <= t < total) comes from the lane whose inclusive length
+// prefix first exceeds t.
+// ---------------------------------------------------------------------------
 struct Chunk {
     int32_t bs;    // first position of B_k in B.idx
     int32_t len;   // |B_k|
@@ -53,8 +63,8 @@ struct Chunk {
     int32_t total; // products of the chunk
 };
 
-__device__ __forceinline__ Chunk load_chunk(const CsrDev &A, const CsrDev &B, int32_t e,
-                                            int32_t eEnd, int lane) {
+__device__ __forceinline__ Chunk load_chunk(const CsrDev &A, const CsrDev &B, int32_t e, int32_t eEnd,
+                                            int lane) {
     Chunk c;
     c.bs = 0;
     c.len = 0;
@@ -95,6 +105,104 @@ __device__ __forceinline__ int32_t chunk_pos(const Chunk &c, int32_t t, double *
     const int32_t bs_o = __shfl_sync(FULL, c.bs, o);
     if (a_out) *a_out = __shfl_sync(FULL, c.a, o);
     return bs_o + (t - (incl_o - len_o));
+}
+
+// ---------------------------------------------------------------------------
+// Block-level helpers.
+// ---------------------------------------------------------------------------
+template <int THREADS>
+__device__ __forceinline__ int32_t block_excl_scan(int32_t v, int32_t *total, int32_t *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int32_t y = __shfl_up_sync(FULL, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    int32_t base = 0, tot = 0;
+#pragma unroll
+    for (int i = 0; i < THREADS / 32; ++i) {
+        const int32_t s = sh[i];
+        if (i < w) base += s;
+        tot += s;
+    }
+    __syncthreads();
+    *total = tot;
+    return base + x - v;
+}
+
+template <int THREADS>
+__device__ __forceinline__ int32_t block_min_i32(int32_t v, int32_t *sh) {
+#pragma unroll
+    for (int d = 16; d; d >>= 1) v = min(v, __shfl_xor_sync(FULL, v, d));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int32_t r = INT_MAX;
+#pragma unroll
+    for (int i = 0; i < THREADS / 32; ++i) r = min(r, sh[i]);
+    __syncthreads();
+    return r;
+}
+
+template <int THREADS>
+__device__ __forceinline__ int block_sum_i(int v, int *sh) {
+#pragma unroll
+    for (int d = 16; d; d >>= 1) v += __shfl_xor_sync(FULL, v, d);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    int r = 0;
+#pragma unroll
+    for (int i = 0; i < THREADS / 32; ++i) r += sh[i];
+    __syncthreads();
+    return r;
+}
+
+// A batch of up to THREADS entries of one A row staged in shared memory:
+// pre[i] = exclusive prefix of |B_k| (pre[nb] = the batch's products),
+// bst[i] = first position of B_k, av[i] = A value.  Returns the products.
+template <int THREADS, bool VALS>
+__device__ __forceinline__ int32_t stage_entries(const CsrDev &A, const CsrDev &B, int32_t eb, int nb,
+                                                 int32_t *pre, int32_t *bst, double *av, int32_t *sh) {
+    const int tid = threadIdx.x;
+    int32_t len = 0;
+    if (tid < nb) {
+        const int32_t k = A.idx[eb + tid];
+        const int32_t s = B.ptr[k];
+        len = B.ptr[k + 1] - s;
+        bst[tid] = s;
+        if constexpr (VALS) av[tid] = A.val[eb + tid];
+    }
+    int32_t total;
+    const int32_t ex = block_excl_scan<THREADS>(len, &total, sh);
+    if (tid < nb) pre[tid] = ex;
+    if (tid == 0) pre[nb] = total;
+    __syncthreads();
+    return total;
+}
+
+// Largest i in [0, nb) with pre[i] <= t (an entry with at least one product).
+__device__ __forceinline__ int find_entry(const int32_t *pre, int nb, int32_t t) {
+    int lo = 0, hi = nb - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Sets bit `rel` of a shared bitmap for every lane in `active` with one
+// atomicOr per distinct word; returns the bits this call turned on (lane
+// leaders only, 0 elsewhere).
+__device__ __forceinline__ uint32_t set_bits_aggregated(uint32_t *bm, int64_t rel, unsigned active) {
+    const uint32_t w = (uint32_t)(rel >> 5);
+    const uint32_t bit = 1u << (rel & 31);
+    const unsigned grp = __match_any_sync(active, w);
+    const uint32_t all = __reduce_or_sync(grp, bit);
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) return all & ~atomicOr(&bm[w], all);
+    return 0u;
 }
 
 template <int GROUP, int ROWS>
@@ -150,6 +258,15 @@ __device__ __forceinline__ int warp_sum_i(int v) {
     return v;
 }
 
+// Shared-memory layout of the staged entries (after an 8-aligned prefix).
+template <int ECAP>
+struct StageLayout {
+    static constexpr size_t pre = 0;                              // int32[ECAP + 1]
+    static constexpr size_t bst = ((4 * (ECAP + 1)) + 7) / 8 * 8;  // int32[ECAP]
+    static constexpr size_t av = bst + ((4 * ECAP) + 7) / 8 * 8;  // double[ECAP]
+    static constexpr size_t bytes = av + 8 * ECAP;
+};
+
 // ======================================================================
 // Symbolic kernels: rowNnz[row] = number of distinct columns of C's row.
 // ======================================================================
@@ -171,23 +288,20 @@ __global__ void __launch_bounds__(256) k_sym_tiny(SymArgs a, int32_t begin, int3
     if (lane == 0) a.rowNnz[row] = __popc(lm);
 }
 
-// Hash rows: GROUP threads per row, ROWS rows per CTA, TABLE keys per row.
-template <int GROUP, int ROWS, int TABLE>
-__global__ void __launch_bounds__(GROUP *ROWS) k_sym_hash(SymArgs a, int32_t begin, int32_t count) {
+// Warp hash rows: one warp per row, ROWS rows per CTA, TABLE keys per row.
+template <int ROWS, int TABLE>
+__global__ void __launch_bounds__(32 * ROWS) k_sym_hash_warp(SymArgs a, int32_t begin, int32_t count) {
     extern __shared__ __align__(16) unsigned char smem[];
-    constexpr int GW = GROUP / 32;
-    __shared__ int red[ROWS][GW];
-    const int g = threadIdx.x / GROUP, gt = threadIdx.x % GROUP;
-    const int lane = threadIdx.x & 31, gw = gt >> 5;
+    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t item = (int64_t)blockIdx.x * ROWS + g;
     if (item >= count) return;
     int32_t *keys = reinterpret_cast<int32_t *>(smem) + (size_t)g * TABLE;
     const int32_t row = a.list[begin + item];
-    for (int i = gt; i < TABLE; i += GROUP) keys[i] = EMPTY;
-    group_sync<GROUP, ROWS>();
+    for (int i = lane; i < TABLE; i += 32) keys[i] = EMPTY;
+    __syncwarp();
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     int cnt = 0;
-    for (int32_t e = e0 + gw * 32; e < e1; e += GROUP) {
+    for (int32_t e = e0; e < e1; e += 32) {
         const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
         for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
             const int32_t t = t0 + lane;
@@ -196,59 +310,72 @@ __global__ void __launch_bounds__(GROUP *ROWS) k_sym_hash(SymArgs a, int32_t beg
         }
     }
     cnt = warp_sum_i(cnt);
-    if constexpr (GW == 1) {
-        if (gt == 0) a.rowNnz[row] = cnt;
-    } else {
-        if (lane == 0) red[g][gw] = cnt;
-        __syncthreads();
-        if (gt == 0) {
-            int s = 0;
-            for (int i = 0; i < GW; ++i) s += red[g][i];
-            a.rowNnz[row] = s;
+    if (lane == 0) a.rowNnz[row] = cnt;
+}
+
+// CTA hash rows: one CTA per row, products spread over all threads.
+template <int THREADS, int TABLE>
+__global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t begin) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    using L = StageLayout<THREADS>;
+    __shared__ int32_t sh[THREADS / 32];
+    int32_t *pre = reinterpret_cast<int32_t *>(smem + L::pre);
+    int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
+    int32_t *keys = reinterpret_cast<int32_t *>(smem + L::bytes);
+    const int tid = threadIdx.x;
+    const int32_t row = a.list[begin + blockIdx.x];
+    for (int i = tid; i < TABLE; i += THREADS) keys[i] = EMPTY;
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    int cnt = 0;
+    for (int32_t eb = e0; eb < e1; eb += THREADS) {
+        const int nb = min(THREADS, e1 - eb);
+        const int32_t total = stage_entries<THREADS, false>(a.A, a.B, eb, nb, pre, bst, nullptr, sh);
+        for (int32_t t = tid; t < total; t += THREADS) {
+            const int e = find_entry(pre, nb, t);
+            cnt += hash_insert_key<TABLE>(keys, a.B.idx[bst[e] + (t - pre[e])], a.err);
         }
+        __syncthreads();
     }
+    cnt = block_sum_i<THREADS>(cnt, sh);
+    if (tid == 0) a.rowNnz[row] = cnt;
 }
 
 // Wide rows: one CTA per row, a shared bitmap over windows of winBits columns.
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, int64_t ncols,
-                                                      int winBits) {
+__global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, int64_t ncols, int winBits) {
     extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t *bm = reinterpret_cast<uint32_t *>(smem);
-    __shared__ int red[THREADS / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    using L = StageLayout<THREADS>;
+    __shared__ int32_t sh[THREADS / 32];
+    int32_t *pre = reinterpret_cast<int32_t *>(smem + L::pre);
+    int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
+    uint32_t *bm = reinterpret_cast<uint32_t *>(smem + L::bytes);
+    const int tid = threadIdx.x;
     const int32_t row = a.list[begin + blockIdx.x];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     const int words = winBits >> 5;
     int cnt = 0;
     for (int64_t c_lo = 0; c_lo < ncols; c_lo += winBits) {
-        for (int i = threadIdx.x; i < words; i += THREADS) bm[i] = 0u;
-        __syncthreads();
-        for (int32_t e = e0 + w * 32; e < e1; e += THREADS) {
-            const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
-            for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
-                const int32_t t = t0 + lane;
-                const int32_t j = chunk_pos(c, t, nullptr);
-                if (t < c.total) {
-                    const int64_t rel = (int64_t)a.B.idx[j] - c_lo;
-                    if (rel >= 0 && rel < winBits) {
-                        const uint32_t bit = 1u << (rel & 31);
-                        const uint32_t old = atomicOr(&bm[rel >> 5], bit);
-                        cnt += (old & bit) ? 0 : 1;
-                    }
+        for (int i = tid; i < words; i += THREADS) bm[i] = 0u;
+        for (int32_t eb = e0; eb < e1; eb += THREADS) {
+            const int nb = min(THREADS, e1 - eb);
+            const int32_t total = stage_entries<THREADS, false>(a.A, a.B, eb, nb, pre, bst, nullptr, sh);
+            // Warp-uniform trip count: every lane reaches the aggregated update.
+            for (int32_t t0 = tid & ~31; t0 < total; t0 += THREADS) {
+                const int32_t t = t0 + (tid & 31);
+                int64_t rel = -1;
+                if (t < total) {
+                    const int e = find_entry(pre, nb, t);
+                    rel = (int64_t)a.B.idx[bst[e] + (t - pre[e])] - c_lo;
                 }
+                const bool in = rel >= 0 && rel < winBits;
+                const unsigned act = __ballot_sync(FULL, in);
+                if (in) cnt += __popc(set_bits_aggregated(bm, rel, act));
             }
+            __syncthreads();
         }
-        __syncthreads();
     }
-    cnt = warp_sum_i(cnt);
-    if (lane == 0) red[w] = cnt;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int s = 0;
-        for (int i = 0; i < THREADS / 32; ++i) s += red[i];
-        a.rowNnz[row] = s;
-    }
+    cnt = block_sum_i<THREADS>(cnt, sh);
+    if (tid == 0) a.rowNnz[row] = cnt;
 }
 
 // ======================================================================
@@ -293,7 +420,7 @@ __global__ void __launch_bounds__(256) k_num_tiny(NumArgs a, int32_t lo, int32_t
     if (lane == 0 && __popc(lm) != expect) raise(a.err, DEV_COUNT_MISMATCH);
 }
 
-// Bitonic sort of n64[0, N) ascending by GROUP threads (N a power of two).
+// Bitonic sort of buf[0, N) ascending by GROUP threads (N a power of two).
 template <int GROUP, int ROWS>
 __device__ __forceinline__ void group_bitonic(uint64_t *buf, int N, int gt) {
     for (int k = 2; k <= N; k <<= 1) {
@@ -314,45 +441,16 @@ __device__ __forceinline__ void group_bitonic(uint64_t *buf, int N, int gt) {
     }
 }
 
-// Hash rows: keys int32[TABLE] then values double[TABLE] per row; the sort
-// buffer (TABLE/2 packed (column, slot) pairs) reuses the key array.
+// Compacts the occupied slots of a (keys, vals) table into sbuf (which
+// aliases keys) as packed (column, slot) pairs, sorts them and writes the
+// row.  GROUP threads per row; all of them call.
 template <int GROUP, int ROWS, int TABLE>
-__global__ void __launch_bounds__(GROUP *ROWS) k_num_hash(NumArgs a, int32_t lo, int32_t count) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    constexpr int GW = GROUP / 32;
+__device__ __forceinline__ void table_write_sorted(NumArgs &a, int32_t row, int32_t *keys, const double *vals,
+                                                   int *gcnt, int gt) {
     constexpr int KPT = TABLE / GROUP;
     constexpr int NMAX = TABLE / 2;
-    static_assert(KPT >= 1 && TABLE % GROUP == 0, "table must split evenly");
-    __shared__ int gcnt[ROWS];
-    const int g = threadIdx.x / GROUP, gt = threadIdx.x % GROUP;
-    const int lane = threadIdx.x & 31, gw = gt >> 5;
-    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
-    if (item >= count) return;
-    unsigned char *base_ptr = smem + (size_t)g * (12 * (size_t)TABLE);
-    int32_t *keys = reinterpret_cast<int32_t *>(base_ptr);
-    double *vals = reinterpret_cast<double *>(base_ptr + 4 * (size_t)TABLE);
-    uint64_t *sbuf = reinterpret_cast<uint64_t *>(base_ptr);
-    const int32_t row = a.list[lo + item];
-    for (int i = gt; i < TABLE; i += GROUP) {
-        keys[i] = EMPTY;
-        vals[i] = 0.0;
-    }
-    if (gt == 0) gcnt[g] = 0;
-    group_sync<GROUP, ROWS>();
-    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
-    for (int32_t e = e0 + gw * 32; e < e1; e += GROUP) {
-        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
-        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
-            const int32_t t = t0 + lane;
-            double av;
-            const int32_t j = chunk_pos(c, t, &av);
-            if (t < c.total) {
-                const int s = hash_insert_slot<TABLE>(keys, a.B.idx[j], a.err);
-                if (s >= 0) atomicAdd(&vals[s], __dmul_rn(av, a.B.val[j]));
-            }
-        }
-    }
-    group_sync<GROUP, ROWS>();
+    const int lane = threadIdx.x & 31;
+    uint64_t *sbuf = reinterpret_cast<uint64_t *>(keys);
     int32_t mk[KPT];
 #pragma unroll
     for (int q = 0; q < KPT; ++q) mk[q] = keys[gt + q * GROUP];
@@ -362,16 +460,15 @@ __global__ void __launch_bounds__(GROUP *ROWS) k_num_hash(NumArgs a, int32_t lo,
         const bool occ = mk[q] != EMPTY;
         const unsigned bal = __ballot_sync(FULL, occ);
         int wbase = 0;
-        if (lane == 0 && bal) wbase = atomicAdd(&gcnt[g], __popc(bal));
+        if (lane == 0 && bal) wbase = atomicAdd(gcnt, __popc(bal));
         wbase = __shfl_sync(FULL, wbase, 0);
         if (occ) {
             const int pos = wbase + __popc(bal & ((1u << lane) - 1u));
-            if (pos < NMAX)
-                sbuf[pos] = ((uint64_t)(uint32_t)mk[q] << 32) | (uint32_t)(gt + q * GROUP);
+            if (pos < NMAX) sbuf[pos] = ((uint64_t)(uint32_t)mk[q] << 32) | (uint32_t)(gt + q * GROUP);
         }
     }
     group_sync<GROUP, ROWS>();
-    const int n = gcnt[g];
+    const int n = *gcnt;
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
     if (gt == 0 && (n != expect || n > NMAX)) raise(a.err, DEV_COUNT_MISMATCH);
     const int nn = min(n, NMAX);
@@ -389,68 +486,124 @@ __global__ void __launch_bounds__(GROUP *ROWS) k_num_hash(NumArgs a, int32_t lo,
     }
 }
 
-template <int THREADS>
-__device__ __forceinline__ int32_t block_min_i32(int32_t v, int32_t *sh) {
-#pragma unroll
-    for (int d = 16; d; d >>= 1) v = min(v, __shfl_xor_sync(FULL, v, d));
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-    __syncthreads();
-    int32_t r = INT_MAX;
-#pragma unroll
-    for (int i = 0; i < THREADS / 32; ++i) r = min(r, sh[i]);
-    __syncthreads();
-    return r;
+// Warp hash rows: keys int32[TABLE] then values double[TABLE] per row.
+template <int ROWS, int TABLE>
+__global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t lo, int32_t count) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int gcnt[ROWS];
+    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    if (item >= count) return;
+    unsigned char *base_ptr = smem + (size_t)g * (12 * (size_t)TABLE);
+    int32_t *keys = reinterpret_cast<int32_t *>(base_ptr);
+    double *vals = reinterpret_cast<double *>(base_ptr + 4 * (size_t)TABLE);
+    const int32_t row = a.list[lo + item];
+    for (int i = lane; i < TABLE; i += 32) {
+        keys[i] = EMPTY;
+        vals[i] = 0.0;
+    }
+    if (lane == 0) gcnt[g] = 0;
+    __syncwarp();
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    for (int32_t e = e0; e < e1; e += 32) {
+        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+            const int32_t t = t0 + lane;
+            double av;
+            const int32_t j = chunk_pos(c, t, &av);
+            if (t < c.total) {
+                const int s = hash_insert_slot<TABLE>(keys, a.B.idx[j], a.err);
+                if (s >= 0) atomicAdd(&vals[s], __dmul_rn(av, a.B.val[j]));
+            }
+        }
+    }
+    __syncwarp();
+    table_write_sorted<32, ROWS, TABLE>(a, row, keys, vals, &gcnt[g], lane);
 }
 
-template <int THREADS>
-__device__ __forceinline__ int32_t block_excl_scan_small(int32_t v, int32_t *total, int32_t *sh) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int32_t x = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int32_t y = __shfl_up_sync(FULL, x, d);
-        if (lane >= d) x += y;
+// CTA hash rows: one CTA per row, products spread over all threads.
+template <int THREADS, int TABLE>
+__global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    using L = StageLayout<THREADS>;
+    __shared__ int32_t sh[THREADS / 32];
+    __shared__ int gcnt;
+    int32_t *pre = reinterpret_cast<int32_t *>(smem + L::pre);
+    int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
+    double *av = reinterpret_cast<double *>(smem + L::av);
+    int32_t *keys = reinterpret_cast<int32_t *>(smem + L::bytes);
+    double *vals = reinterpret_cast<double *>(smem + L::bytes + 4 * (size_t)TABLE);
+    const int tid = threadIdx.x;
+    const int32_t row = a.list[lo + blockIdx.x];
+    for (int i = tid; i < TABLE; i += THREADS) {
+        keys[i] = EMPTY;
+        vals[i] = 0.0;
     }
-    if (lane == 31) sh[w] = x;
-    __syncthreads();
-    int32_t base = 0, tot = 0;
-#pragma unroll
-    for (int i = 0; i < THREADS / 32; ++i) {
-        const int32_t s = sh[i];
-        if (i < w) base += s;
-        tot += s;
+    if (tid == 0) gcnt = 0;
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    for (int32_t eb = e0; eb < e1; eb += THREADS) {
+        const int nb = min(THREADS, e1 - eb);
+        const int32_t total = stage_entries<THREADS, true>(a.A, a.B, eb, nb, pre, bst, av, sh);
+        for (int32_t t = tid; t < total; t += THREADS) {
+            const int e = find_entry(pre, nb, t);
+            const int32_t pos = bst[e] + (t - pre[e]);
+            const int s = hash_insert_slot<TABLE>(keys, a.B.idx[pos], a.err);
+            if (s >= 0) atomicAdd(&vals[s], __dmul_rn(av[e], a.B.val[pos]));
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    *total = tot;
-    return base + x - v;
+    table_write_sorted<THREADS, 1, TABLE>(a, row, keys, vals, &gcnt, tid);
 }
 
-// Dense rows: one CTA per row sweeps windows of W columns; each thread owns
-// A entries and keeps a cursor into their B row (B rows ascending), so every
-// product is visited once.  Without sorted B rows every window rescans the
-// B rows and filters.
-template <int THREADS, int W, bool SORTED>
+// Dense rows: one CTA per row sweeps windows of W columns.  The per-entry
+// state (cursor into the B row, its end, the A value, the next column at or
+// past the cursor) is staged in shared memory for THREADS entries at a time;
+// rows with more entries keep it in a.state between windows.  One warp per
+// entry scans its B row from the cursor 32 products per step; with B rows
+// ascending the products inside the window are a prefix found by ballot.
+// Without sorted B rows every window rescans whole B rows and filters.
+template <int THREADS, int W, int ECAP, bool SORTED>
 __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
     extern __shared__ __align__(16) unsigned char smem[];
     static_assert(W / 32 <= THREADS, "one bitmap word per thread");
+    constexpr int NW = THREADS / 32;
     double *dense = reinterpret_cast<double *>(smem);
     uint32_t *bits = reinterpret_cast<uint32_t *>(smem + 8 * (size_t)W);
-    __shared__ int32_t sh[THREADS / 32];
-    const int tid = threadIdx.x;
+    double *sav = reinterpret_cast<double *>(smem + 8 * (size_t)W + W / 8);
+    int32_t *scur = reinterpret_cast<int32_t *>(sav + ECAP);
+    int32_t *send = scur + ECAP;
+    int32_t *snext = send + ECAP;
+    __shared__ int32_t sh[NW];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int32_t row = a.list[lo + blockIdx.x];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    const int32_t nA = e1 - e0;
+    const bool resident = nA <= ECAP;
+    int32_t *gcur = a.state;             // cursor per A entry
+    int32_t *gnext = a.state + a.A.nnz;  // next column per A entry
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
     const int64_t obase = a.Cp[row] - a.outBase;
 
+    // Initial state of every entry.
     int32_t mymin = INT_MAX;
-    for (int32_t e = e0 + tid; e < e1; e += THREADS) {
-        const int32_t k = a.A.idx[e];
+    for (int32_t i = tid; i < nA; i += THREADS) {
+        const int32_t k = a.A.idx[e0 + i];
         const int32_t s = a.B.ptr[k], t = a.B.ptr[k + 1];
+        int32_t nx = INT_MAX;
         if constexpr (SORTED) {
-            a.cursor[e] = s;
-            if (s < t) mymin = min(mymin, a.B.idx[s]);
+            if (s < t) nx = a.B.idx[s];
         } else {
-            for (int32_t q = s; q < t; ++q) mymin = min(mymin, a.B.idx[q]);
+            for (int32_t q = s; q < t; ++q) nx = min(nx, a.B.idx[q]);
+        }
+        mymin = min(mymin, nx);
+        if (resident) {
+            scur[i] = s;
+            send[i] = t;
+            sav[i] = a.A.val[e0 + i];
+            snext[i] = nx;
+        } else {
+            gcur[e0 + i] = s;
+            gnext[e0 + i] = nx;
         }
     }
     int32_t cmin = block_min_i32<THREADS>(mymin, sh);
@@ -460,43 +613,86 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
         const int64_t c_hi = (int64_t)c_lo + W;
         for (int i = tid; i < W; i += THREADS) dense[i] = 0.0;
         for (int i = tid; i < W / 32; i += THREADS) bits[i] = 0u;
-        __syncthreads();
         mymin = INT_MAX;
-        for (int32_t e = e0 + tid; e < e1; e += THREADS) {
-            const int32_t k = a.A.idx[e];
-            const double av = a.A.val[e];
-            const int32_t t = a.B.ptr[k + 1];
-            if constexpr (SORTED) {
-                int32_t cur = a.cursor[e];
-                while (cur < t) {
-                    const int32_t c = a.B.idx[cur];
-                    if (c >= c_hi) {
-                        mymin = min(mymin, c);
-                        break;
-                    }
-                    const int rel = c - c_lo;
-                    atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[cur]));
-                    atomicOr(&bits[rel >> 5], 1u << (rel & 31));
-                    ++cur;
-                }
-                a.cursor[e] = cur;
-            } else {
-                for (int32_t q = a.B.ptr[k]; q < t; ++q) {
-                    const int32_t c = a.B.idx[q];
-                    if (c >= c_lo && c < c_hi) {
-                        const int rel = c - c_lo;
-                        atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[q]));
-                        atomicOr(&bits[rel >> 5], 1u << (rel & 31));
-                    } else if (c >= c_hi) {
-                        mymin = min(mymin, c);
-                    }
+        for (int32_t eb = 0; eb < nA; eb += ECAP) {
+            const int nb = min(ECAP, nA - eb);
+            if (!resident) {
+                for (int i = tid; i < nb; i += THREADS) {
+                    const int32_t e = e0 + eb + i;
+                    scur[i] = gcur[e];
+                    send[i] = a.B.ptr[a.A.idx[e] + 1];
+                    sav[i] = a.A.val[e];
+                    snext[i] = gnext[e];
                 }
             }
+            __syncthreads();
+            for (int i = warp; i < nb; i += NW) {
+                const int32_t nx = snext[i];
+                if (nx >= c_hi) {
+                    mymin = min(mymin, nx);
+                    continue;
+                }
+                int32_t cur = scur[i];
+                const int32_t end = send[i];
+                const double av = sav[i];
+                int32_t nxt = INT_MAX;
+                if constexpr (SORTED) {
+                    for (;;) {
+                        const int32_t p = cur + lane;
+                        const int32_t c = p < end ? a.B.idx[p] : INT_MAX;
+                        const bool v = c < c_hi;
+                        const unsigned m = __ballot_sync(FULL, v);
+                        if (v) {
+                            // cursors never point below the window (it starts at
+                            // the smallest next column); the guard keeps a
+                            // malformed row inside shared memory all the same
+                            const int rel = max(c - c_lo, 0);
+                            atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[p]));
+                            set_bits_aggregated(bits, rel, m);
+                        }
+                        const int n = __popc(m);
+                        cur += n;
+                        if (n < 32) {
+                            nxt = __shfl_sync(FULL, c, n);
+                            break;
+                        }
+                    }
+                } else {
+                    for (int32_t q0 = cur; q0 < end; q0 += 32) {
+                        const int32_t q = q0 + lane;
+                        const int32_t c = q < end ? a.B.idx[q] : INT_MAX;
+                        const bool v = c >= c_lo && c < c_hi;
+                        const unsigned m = __ballot_sync(FULL, v);
+                        if (v) {
+                            const int rel = c - c_lo;
+                            atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[q]));
+                            set_bits_aggregated(bits, rel, m);
+                        } else if (c >= c_hi) {
+                            nxt = min(nxt, c);
+                        }
+                    }
+#pragma unroll
+                    for (int d = 16; d; d >>= 1) nxt = min(nxt, __shfl_xor_sync(FULL, nxt, d));
+                }
+                mymin = min(mymin, nxt);
+                if (lane == 0) {
+                    if constexpr (SORTED) scur[i] = cur;
+                    snext[i] = nxt;
+                }
+            }
+            __syncthreads();
+            if (!resident) {
+                for (int i = tid; i < nb; i += THREADS) {
+                    const int32_t e = e0 + eb + i;
+                    gcur[e] = scur[i];
+                    gnext[e] = snext[i];
+                }
+                __syncthreads();
+            }
         }
-        __syncthreads();
         uint32_t word = tid < W / 32 ? bits[tid] : 0u;
         int32_t tot;
-        const int32_t off = block_excl_scan_small<THREADS>(__popc(word), &tot, sh);
+        const int32_t off = block_excl_scan<THREADS>(__popc(word), &tot, sh);
         int64_t pos = run + off;
         while (word) {
             const int b = __ffs(word) - 1;
@@ -514,36 +710,41 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
     if (tid == 0 && run != expect) raise(a.err, DEV_COUNT_MISMATCH);
 }
 
-// Shared-memory sizes of each configuration.
+// Configurations and their dynamic shared memory.
 constexpr int kSymWarpRows = 8;
 constexpr int kNumWarpRows = 4;
-constexpr size_t kSmemSymWarp = (size_t)kSymWarpRows * kSymWarpTable * 4;
-constexpr size_t kSmemSymCta = (size_t)kSymCtaTable * 4;
-constexpr size_t kSmemNumWarp = (size_t)kNumWarpRows * kNumWarpTable * 12;
-constexpr size_t kSmemNumCtaS = (size_t)kNumCtaSTable * 12;
-constexpr size_t kSmemNumCtaL = (size_t)kNumCtaLTable * 12;
-constexpr size_t kSmemDense = (size_t)kDenseWindow * 8 + kDenseWindow / 8;
+constexpr int kSymCtaThreads = 256;
+constexpr int kNumCtaSThreads = 256;
+constexpr int kNumCtaLThreads = 512;
 constexpr int kDenseThreads = 512;
+constexpr int kDenseStage = 256;
 constexpr int kWideThreads = 512;
+constexpr size_t kSmemSymWarp = (size_t)kSymWarpRows * kSymWarpTable * 4;
+constexpr size_t kSmemSymCta = StageLayout<kSymCtaThreads>::bytes + (size_t)kSymCtaTable * 4;
+constexpr size_t kSmemNumWarp = (size_t)kNumWarpRows * kNumWarpTable * 12;
+constexpr size_t kSmemNumCtaS = StageLayout<kNumCtaSThreads>::bytes + (size_t)kNumCtaSTable * 12;
+constexpr size_t kSmemNumCtaL = StageLayout<kNumCtaLThreads>::bytes + (size_t)kNumCtaLTable * 12;
+constexpr size_t kSmemDense = (size_t)kDenseWindow * 8 + kDenseWindow / 8 + (size_t)kDenseStage * 20;
+constexpr size_t kSmemWideBase = StageLayout<kWideThreads>::bytes;
 
 }  // namespace
 
 void init_kernel_attributes() {
-    cudaFuncSetAttribute(k_sym_hash<32, kSymWarpRows, kSymWarpTable>,
+    cudaFuncSetAttribute(k_sym_hash_warp<kSymWarpRows, kSymWarpTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemSymWarp);
-    cudaFuncSetAttribute(k_sym_hash<256, 1, kSymCtaTable>,
+    cudaFuncSetAttribute(k_sym_hash_cta<kSymCtaThreads, kSymCtaTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemSymCta);
     cudaFuncSetAttribute(k_sym_wide<kWideThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kWideWindowBitsMax / 8);
-    cudaFuncSetAttribute(k_num_hash<32, kNumWarpRows, kNumWarpTable>,
+                         (int)(kSmemWideBase + kWideWindowBitsMax / 8));
+    cudaFuncSetAttribute(k_num_hash_warp<kNumWarpRows, kNumWarpTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumWarp);
-    cudaFuncSetAttribute(k_num_hash<256, 1, kNumCtaSTable>,
+    cudaFuncSetAttribute(k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumCtaS);
-    cudaFuncSetAttribute(k_num_hash<512, 1, kNumCtaLTable>,
+    cudaFuncSetAttribute(k_num_hash_cta<kNumCtaLThreads, kNumCtaLTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumCtaL);
-    cudaFuncSetAttribute(k_num_dense<kDenseThreads, kDenseWindow, true>,
+    cudaFuncSetAttribute(k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, true>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDense);
-    cudaFuncSetAttribute(k_num_dense<kDenseThreads, kDenseWindow, false>,
+    cudaFuncSetAttribute(k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, false>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDense);
 }
 
@@ -562,15 +763,16 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
             k_sym_tiny<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(a, begin, n);
             break;
         case SB_HWARP:
-            k_sym_hash<32, kSymWarpRows, kSymWarpTable>
+            k_sym_hash_warp<kSymWarpRows, kSymWarpTable>
                 <<<(unsigned)ceil_div(n, kSymWarpRows), 32 * kSymWarpRows, kSmemSymWarp, s>>>(a, begin, n);
             break;
         case SB_HCTA:
-            k_sym_hash<256, 1, kSymCtaTable><<<(unsigned)n, 256, kSmemSymCta, s>>>(a, begin, n);
+            k_sym_hash_cta<kSymCtaThreads, kSymCtaTable><<<(unsigned)n, kSymCtaThreads, kSmemSymCta, s>>>(a, begin);
             break;
         case SB_WIDE: {
             const int wb = wide_window_bits(a.B.n);
-            k_sym_wide<kWideThreads><<<(unsigned)n, kWideThreads, (size_t)wb / 8, s>>>(a, begin, a.B.n, wb);
+            k_sym_wide<kWideThreads><<<(unsigned)n, kWideThreads, kSmemWideBase + (size_t)wb / 8, s>>>(
+                a, begin, a.B.n, wb);
             break;
         }
         default:
@@ -588,21 +790,23 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
             k_num_tiny<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(a, lo, n);
             break;
         case NB_HWARP:
-            k_num_hash<32, kNumWarpRows, kNumWarpTable>
+            k_num_hash_warp<kNumWarpRows, kNumWarpTable>
                 <<<(unsigned)ceil_div(n, kNumWarpRows), 32 * kNumWarpRows, kSmemNumWarp, s>>>(a, lo, n);
             break;
         case NB_HCTA_S:
-            k_num_hash<256, 1, kNumCtaSTable><<<(unsigned)n, 256, kSmemNumCtaS, s>>>(a, lo, n);
+            k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>
+                <<<(unsigned)n, kNumCtaSThreads, kSmemNumCtaS, s>>>(a, lo);
             break;
         case NB_HCTA_L:
-            k_num_hash<512, 1, kNumCtaLTable><<<(unsigned)n, 512, kSmemNumCtaL, s>>>(a, lo, n);
+            k_num_hash_cta<kNumCtaLThreads, kNumCtaLTable>
+                <<<(unsigned)n, kNumCtaLThreads, kSmemNumCtaL, s>>>(a, lo);
             break;
         case NB_DENSE:
             if (a.bSorted)
-                k_num_dense<kDenseThreads, kDenseWindow, true>
+                k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, true>
                     <<<(unsigned)n, kDenseThreads, kSmemDense, s>>>(a, lo);
             else
-                k_num_dense<kDenseThreads, kDenseWindow, false>
+                k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, false>
                     <<<(unsigned)n, kDenseThreads, kSmemDense, s>>>(a, lo);
             break;
         default:
