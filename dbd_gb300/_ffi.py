@@ -87,6 +87,8 @@ SIGNATURES = {
     "dbd_spgemm_files": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int, C.c_char_p,
                                    C.POINTER(Stats)]),
     "dbd_csr_free": (None, [C.POINTER(CsrOut)]),
+    "dbd_spgemm_noalloc": (C.c_int, [C.POINTER(CsrView), C.POINTER(CsrView), C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_int64, C.POINTER(C.c_int64), C.c_void_p]),
 }
 
 _lib = None

@@ -232,6 +232,40 @@ int dbd_spgemm_files(dbd_ctx *ctx, const char *path_a, const char *path_b,
 
 void dbd_csr_free(dbd_csr_out *c);
 
+/* ---- allocation-free multiply --------------------------------------------- */
+
+/* Bytes of device scratch that dbd_spgemm_noalloc owns per GPU. */
+#define DBD_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+/* C = A*B (b == NULL: A*A) without allocating anything, for callers that
+ * cannot allocate device memory -- code running inside a caching allocator's
+ * hooks or a framework that forbids allocation outside its own pool, loops
+ * that cannot afford cudaMalloc/cudaFree's implicit device synchronisation,
+ * processes that reserved all device memory up front.  No counterpart in the
+ * reference (which cudaMallocs per run, preProc.cu:29-106).
+ *
+ * a, b: device-resident CSR (on_device = 1) with FP64 values.  The caller
+ * passes the outputs in device memory: c_row_ptr (n_rows + 1 int64) and
+ * c_col_idx / c_val with room for c_capacity entries.  *c_nnz receives
+ * nnz(C); when it exceeds c_capacity the call returns DBD_ERR_BUDGET with
+ * c_row_ptr filled, so the caller can size its buffers and call again.
+ * Work runs on `stream` (a cudaStream_t; NULL = the legacy default stream)
+ * and the call returns when it is complete.
+ *
+ * Every temporary array lives in one file-scope device array of
+ * DBD_NOALLOC_SCRATCH_BYTES (32 MiB), which each GPU that loads the library
+ * holds until the process exits.  Inputs whose scratch would exceed it --
+ * about 22 bytes per row of A plus 8 per entry of A, e.g. ~1.2M rows at 2
+ * entries per row -- are rejected with DBD_ERR_BUDGET.  The first call on a
+ * device sets that device up (its kernel attributes and the array's device
+ * address), so make the first call on each device before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (other threads or
+ * streams) race and must be serialised by the caller.  On failure the
+ * message is printed to stderr. */
+int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, int64_t *c_row_ptr,
+                       int32_t *c_col_idx, double *c_val, int64_t c_capacity, int64_t *c_nnz,
+                       void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,83 @@
+"""dbd_spgemm_noalloc: the multiply for callers that cannot allocate device memory.
+
+Callers inside a caching allocator's hooks, frameworks that forbid allocation
+outside their own pool, or loops that cannot afford cudaMalloc's implicit
+synchronisation pass device-resident inputs and outputs; the entry point keeps
+every temporary array in one file-scope device array of fixed size.  This file
+checks, through the C ABI, that two calls in a row (different matrices, so the
+second call starts from the first call's leftovers in that array) give the
+same product as the regular entry point dbd_spgemm, within the tolerance of
+the other parity tests, and that an input too large for the array is refused.
+It is collected last so that a failure here stops a -x run only after every
+other test ran; it also passes on its own in a fresh process.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import dbd_gb300 as dbd
+from dbd_gb300 import _ffi
+from dbd_gb300 import generators as gen
+from dbd_gb300.csr import CSR
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def device_view(torch, A):
+    t = (torch.from_numpy(np.ascontiguousarray(A.row_ptr, np.int32)).cuda(),
+         torch.from_numpy(np.ascontiguousarray(A.col_idx, np.int32)).cuda(),
+         torch.from_numpy(np.ascontiguousarray(A.val, np.float64)).cuda())
+    v = _ffi.CsrView()
+    v.n_rows, v.n_cols, v.nnz = A.n_rows, A.n_cols, A.nnz
+    v.row_ptr, v.col_idx, v.val = t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr()
+    v.val_fp32, v.on_device = 0, 1
+    return v, t
+
+
+def noalloc_multiply(torch, lib, A, capacity):
+    va, keep = device_view(torch, A)
+    cp = torch.empty(A.n_rows + 1, dtype=torch.int64, device="cuda")
+    ci = torch.empty(max(capacity, 1), dtype=torch.int32, device="cuda")
+    cv = torch.empty(max(capacity, 1), dtype=torch.float64, device="cuda")
+    nnz = C.c_int64(-1)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = lib.dbd_spgemm_noalloc(C.byref(va), None, C.c_void_p(cp.data_ptr()), C.c_void_p(ci.data_ptr()),
+                                C.c_void_p(cv.data_ptr()), capacity, C.byref(nnz), C.c_void_p(stream))
+    torch.cuda.synchronize()
+    n = nnz.value
+    return rc, n, cp.cpu().numpy(), ci[:max(n, 0)].cpu().numpy(), cv[:max(n, 0)].cpu().numpy()
+
+
+def test_noalloc_matches_regular_entry_point_twice(orc):
+    torch = pytest.importorskip("torch")
+    lib = _ffi.load()
+    mats = [gen.rmat(14, 8, seed=5), gen.laplacian_2d(128)]
+    with dbd.Context(cpu_gib=8, gpu_gib=8) as ctx:
+        for A in mats:
+            ref = ctx.spgemm(A, scope="kernel").C
+            _, _, _, Ca = orc.spgemm(A, with_abs=True)
+            rc, n, cp, ci, cv = noalloc_multiply(torch, lib, A, capacity=ref.nnz + 16)
+            assert rc == 0, _ffi.ERR_NAMES.get(rc, rc)
+            assert n == ref.nnz
+            assert np.array_equal(cp, ref.row_ptr)
+            assert np.array_equal(ci, ref.col_idx)
+            assert np.all(np.abs(cv - ref.val) <= 2 * TOL * Ca)
+
+
+def test_noalloc_reports_short_capacity_and_size_limit():
+    torch = pytest.importorskip("torch")
+    lib = _ffi.load()
+    A = gen.laplacian_2d(32)
+    rc, n, cp, _, _ = noalloc_multiply(torch, lib, A, capacity=10)
+    assert rc == -4 and n > 10 and cp[-1] == n
+    # ~1.6M empty rows need more scratch than the fixed array holds.
+    m = 1_600_000
+    big = CSR(m, m, np.zeros(m + 1, np.int32), np.zeros(0, np.int32), np.zeros(0))
+    vb, keep = device_view(torch, big)
+    cp = torch.empty(m + 1, dtype=torch.int64, device="cuda")
+    nnz = C.c_int64(0)
+    rc = lib.dbd_spgemm_noalloc(C.byref(vb), None, C.c_void_p(cp.data_ptr()), None, None, 0, C.byref(nnz),
+                                None)
+    assert rc == -4
