@@ -88,8 +88,14 @@ struct NumArgs {
     double *Cv;
     int32_t *state;       // 2 * nnz(A) scratch for the dense windows (cursor, next column)
     int bSorted;          // B's rows have ascending columns
+    int rankWords;        // > 0: C's columns fit a shared bitmap of this many words (rank kernels)
     int *err;
 };
+
+// C's columns up to this count use the rank kernels (bitmap + rank prefix,
+// 64 KiB of shared memory at the limit).
+constexpr int64_t kRankColsMax = 1 << 18;
+inline int rank_words(int64_t ncols) { return ncols <= kRankColsMax ? (int)ceil_div(ncols > 0 ? ncols : 1, 32) : 0; }
 // Runs the numeric kernels of bin b over list[lo, hi).
 void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,
                         int *launches);

@@ -483,6 +483,7 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     na.Cv = Cv;
     na.state = c->cursor.as<int32_t>();
     na.bSorted = opB_sorted(c);
+    na.rankWords = rank_words(na.B.n);
     na.err = c->err.as<int>();
     const int64_t t0 = r0 / kTileRows;
     const int64_t t1 = (r1 >= c->m) ? c->ntiles : r1 / kTileRows;

@@ -159,30 +159,39 @@ __device__ __forceinline__ int block_sum_i(int v, int *sh) {
     return r;
 }
 
-// A batch of up to THREADS entries of one A row staged in shared memory:
-// pre[i] = exclusive prefix of |B_k| (pre[nb] = the batch's products),
-// bst[i] = first position of B_k, av[i] = A value.  Returns the products.
+// A batch of up to THREADS entries of one A row staged in shared memory,
+// keeping only entries whose B row is non-empty: pre[i] = exclusive prefix
+// of |B_k| (pre[*nb] = the batch's products), bst[i] = first position of B_k,
+// av[i] = A value.  Every staged entry has at least one product, so 32
+// consecutive products span at most 32 entries.  Returns the products.
 template <int THREADS, bool VALS>
-__device__ __forceinline__ int32_t stage_entries(const CsrDev &A, const CsrDev &B, int32_t eb, int nb,
-                                                 int32_t *pre, int32_t *bst, double *av, int32_t *sh) {
+__device__ __forceinline__ int32_t stage_entries(const CsrDev &A, const CsrDev &B, int32_t eb, int n_in,
+                                                 int32_t *pre, int32_t *bst, double *av, int *nb,
+                                                 int32_t *sh) {
     const int tid = threadIdx.x;
-    int32_t len = 0;
-    if (tid < nb) {
+    int32_t len = 0, s = 0;
+    double a = 0.0;
+    if (tid < n_in) {
         const int32_t k = A.idx[eb + tid];
-        const int32_t s = B.ptr[k];
+        s = B.ptr[k];
         len = B.ptr[k + 1] - s;
-        bst[tid] = s;
-        if constexpr (VALS) av[tid] = A.val[eb + tid];
+        if constexpr (VALS) a = A.val[eb + tid];
     }
-    int32_t total;
+    int32_t total, kept;
     const int32_t ex = block_excl_scan<THREADS>(len, &total, sh);
-    if (tid < nb) pre[tid] = ex;
-    if (tid == 0) pre[nb] = total;
+    const int32_t slot = block_excl_scan<THREADS>(len > 0 ? 1 : 0, &kept, sh);
+    if (len > 0) {
+        pre[slot] = ex;
+        bst[slot] = s;
+        if constexpr (VALS) av[slot] = a;
+    }
+    if (tid == 0) pre[kept] = total;
+    *nb = kept;
     __syncthreads();
     return total;
 }
 
-// Largest i in [0, nb) with pre[i] <= t (an entry with at least one product).
+// Largest i in [0, nb) with pre[i] <= t.
 __device__ __forceinline__ int find_entry(const int32_t *pre, int nb, int32_t t) {
     int lo = 0, hi = nb - 1;
     while (lo < hi) {
@@ -193,16 +202,61 @@ __device__ __forceinline__ int find_entry(const int32_t *pre, int nb, int32_t t)
     return lo;
 }
 
-// Sets bit `rel` of a shared bitmap for every lane in `active` with one
-// atomicOr per distinct word; returns the bits this call turned on (lane
-// leaders only, 0 elsewhere).
-__device__ __forceinline__ uint32_t set_bits_aggregated(uint32_t *bm, int64_t rel, unsigned active) {
-    const uint32_t w = (uint32_t)(rel >> 5);
-    const uint32_t bit = 1u << (rel & 31);
-    const unsigned grp = __match_any_sync(active, w);
-    const uint32_t all = __reduce_or_sync(grp, bit);
-    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) return all & ~atomicOr(&bm[w], all);
-    return 0u;
+// One warp walks products [tb, te) of a staged batch, 32 per step, calling
+// f(valid, pos, e) on every lane (pos = position in B, e = staged entry;
+// meaningful when valid).  Each lane finds its entry by a 5-step shuffle
+// search among the 32 entry starts after the step's first entry.
+template <class F>
+__device__ __forceinline__ void warp_range(const int32_t *pre, const int32_t *bst, int nb, int32_t tb,
+                                           int32_t te, F &&f) {
+    if (tb >= te) return;
+    const int lane = threadIdx.x & 31;
+    int e0 = find_entry(pre, nb, tb);
+    for (int32_t t0 = tb; t0 < te; t0 += 32) {
+        const int32_t t = t0 + lane;
+        const int ej = e0 + 1 + lane;
+        const int32_t bnd = ej <= nb ? pre[ej] : INT_MAX;
+        int o = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int32_t v = __shfl_sync(FULL, bnd, o + step - 1);
+            if (v <= t) o += step;
+        }
+        const int e = min(e0 + o, nb - 1);
+        const bool valid = t < te;
+        f(valid, bst[e] + (t - pre[e]), e);
+        e0 = __shfl_sync(FULL, e, 31);
+    }
+}
+
+// Sets one bit per lane in a shared bitmap with one atomicOr per run of
+// lanes that share a word.  Lanes whose products come from the same sorted B
+// row hold ascending columns, so equal words sit in adjacent lanes; a
+// segmented OR over such runs leaves each run's bits in its first lane.
+// Bits of equal words in non-adjacent lanes are ORed more than once, which
+// is harmless.  All lanes call; `v` marks lanes with a bit.
+__device__ __forceinline__ void or_bits_runs(uint32_t *bm, bool v, uint32_t rel) {
+    const int lane = threadIdx.x & 31;
+    const int32_t w = v ? (int32_t)(rel >> 5) : -1 - lane;
+    uint32_t acc = v ? 1u << (rel & 31) : 0u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int32_t ow = __shfl_down_sync(FULL, w, d);
+        const uint32_t ob = __shfl_down_sync(FULL, acc, d);
+        if (lane + d < 32 && ow == w) acc |= ob;
+    }
+    const int32_t pw = __shfl_up_sync(FULL, w, 1);
+    if (v && (lane == 0 || pw != w)) atomicOr(&bm[w], acc);
+}
+
+// Contiguous share of [0, total) for this warp, in multiples of 32 products.
+template <int THREADS>
+__device__ __forceinline__ void warp_share(int32_t total, int32_t *tb, int32_t *te) {
+    constexpr int NW = THREADS / 32;
+    const int64_t per = ((int64_t)total + NW * 32 - 1) / (NW * 32) * 32;
+    const int64_t b = (int64_t)(threadIdx.x >> 5) * per;
+    *tb = (int32_t)(b < total ? b : (int64_t)total);
+    *te = (int32_t)(b + per < total ? b + per : (int64_t)total);
 }
 
 template <int GROUP, int ROWS>
@@ -328,19 +382,22 @@ __global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t beg
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     int cnt = 0;
     for (int32_t eb = e0; eb < e1; eb += THREADS) {
-        const int nb = min(THREADS, e1 - eb);
-        const int32_t total = stage_entries<THREADS, false>(a.A, a.B, eb, nb, pre, bst, nullptr, sh);
-        for (int32_t t = tid; t < total; t += THREADS) {
-            const int e = find_entry(pre, nb, t);
-            cnt += hash_insert_key<TABLE>(keys, a.B.idx[bst[e] + (t - pre[e])], a.err);
-        }
+        int nb;
+        const int32_t total =
+            stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
+        int32_t tb, te;
+        warp_share<THREADS>(total, &tb, &te);
+        warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
+            if (v) cnt += hash_insert_key<TABLE>(keys, a.B.idx[pos], a.err);
+        });
         __syncthreads();
     }
     cnt = block_sum_i<THREADS>(cnt, sh);
     if (tid == 0) a.rowNnz[row] = cnt;
 }
 
-// Wide rows: one CTA per row, a shared bitmap over windows of winBits columns.
+// Wide rows: one CTA per row, a shared bitmap over windows of winBits
+// columns; the row's size is the bitmap's popcount.
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, int64_t ncols, int winBits) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -357,22 +414,20 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
     for (int64_t c_lo = 0; c_lo < ncols; c_lo += winBits) {
         for (int i = tid; i < words; i += THREADS) bm[i] = 0u;
         for (int32_t eb = e0; eb < e1; eb += THREADS) {
-            const int nb = min(THREADS, e1 - eb);
-            const int32_t total = stage_entries<THREADS, false>(a.A, a.B, eb, nb, pre, bst, nullptr, sh);
-            // Warp-uniform trip count: every lane reaches the aggregated update.
-            for (int32_t t0 = tid & ~31; t0 < total; t0 += THREADS) {
-                const int32_t t = t0 + (tid & 31);
-                int64_t rel = -1;
-                if (t < total) {
-                    const int e = find_entry(pre, nb, t);
-                    rel = (int64_t)a.B.idx[bst[e] + (t - pre[e])] - c_lo;
-                }
+            int nb;
+            const int32_t total =
+                stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
+            int32_t tb, te;
+            warp_share<THREADS>(total, &tb, &te);
+            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
+                const int64_t rel = v ? (int64_t)a.B.idx[pos] - c_lo : -1;
                 const bool in = rel >= 0 && rel < winBits;
-                const unsigned act = __ballot_sync(FULL, in);
-                if (in) cnt += __popc(set_bits_aggregated(bm, rel, act));
-            }
+                or_bits_runs(bm, in, in ? (uint32_t)rel : 0u);
+            });
             __syncthreads();
         }
+        for (int i = tid; i < words; i += THREADS) cnt += __popc(bm[i]);
+        __syncthreads();
     }
     cnt = block_sum_i<THREADS>(cnt, sh);
     if (tid == 0) a.rowNnz[row] = cnt;
@@ -542,17 +597,120 @@ __global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo)
     if (tid == 0) gcnt = 0;
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     for (int32_t eb = e0; eb < e1; eb += THREADS) {
-        const int nb = min(THREADS, e1 - eb);
-        const int32_t total = stage_entries<THREADS, true>(a.A, a.B, eb, nb, pre, bst, av, sh);
-        for (int32_t t = tid; t < total; t += THREADS) {
-            const int e = find_entry(pre, nb, t);
-            const int32_t pos = bst[e] + (t - pre[e]);
-            const int s = hash_insert_slot<TABLE>(keys, a.B.idx[pos], a.err);
-            if (s >= 0) atomicAdd(&vals[s], __dmul_rn(av[e], a.B.val[pos]));
-        }
+        int nb;
+        const int32_t total =
+            stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
+        int32_t tb, te;
+        warp_share<THREADS>(total, &tb, &te);
+        warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
+            if (v) {
+                const int s = hash_insert_slot<TABLE>(keys, a.B.idx[pos], a.err);
+                if (s >= 0) atomicAdd(&vals[s], __dmul_rn(av[e], a.B.val[pos]));
+            }
+        });
         __syncthreads();
     }
     table_write_sorted<THREADS, 1, TABLE>(a, row, keys, vals, &gcnt, tid);
+}
+
+// Rank rows (C has at most 2^18 columns): one CTA per row.  Pass 1 sets the
+// row's columns in a shared bitmap over all of C's columns; a scan of the
+// words' popcounts gives every column its rank among the row's columns, which
+// is its position in C's row.  Pass 2 accumulates every product into
+// vals[rank].  The output is in column order without hashing or sorting.
+// Rows with more than vcap entries accumulate vcap ranks per pass 2.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int nwords, int vcap) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    using L = StageLayout<THREADS>;
+    constexpr int NW = THREADS / 32;
+    __shared__ int32_t sh[NW];
+    int32_t *pre = reinterpret_cast<int32_t *>(smem + L::pre);
+    int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
+    double *av = reinterpret_cast<double *>(smem + L::av);
+    uint32_t *bits = reinterpret_cast<uint32_t *>(smem + L::bytes);
+    int32_t *wpre = reinterpret_cast<int32_t *>(bits + nwords);
+    double *vals = reinterpret_cast<double *>(wpre + nwords);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int32_t row = a.list[lo + blockIdx.x];
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+    const int64_t obase = a.Cp[row] - a.outBase;
+
+    for (int i = tid; i < nwords; i += THREADS) bits[i] = 0u;
+    for (int32_t eb = e0; eb < e1; eb += THREADS) {
+        int nb;
+        const int32_t total =
+            stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
+        int32_t tb, te;
+        warp_share<THREADS>(total, &tb, &te);
+        warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
+            or_bits_runs(bits, v, v ? (uint32_t)a.B.idx[pos] : 0u);
+        });
+        __syncthreads();
+    }
+
+    // Ranks: each warp takes a contiguous run of words, lanes read 32
+    // consecutive words per step.
+    const int per = ((nwords + NW - 1) / NW + 31) / 32 * 32;
+    const int wb = min(nwords, warp * per), we = min(nwords, wb + per);
+    int32_t wsum = 0;
+    for (int w = wb + lane; w < we; w += 32) wsum += __popc(bits[w]);
+#pragma unroll
+    for (int d = 16; d; d >>= 1) wsum += __shfl_xor_sync(FULL, wsum, d);
+    int32_t tot;
+    int32_t run = block_excl_scan<THREADS>(lane == 0 ? wsum : 0, &tot, sh);
+    run = __shfl_sync(FULL, run, 0);
+    for (int w0 = wb; w0 < we; w0 += 32) {
+        const int w = w0 + lane;
+        const int32_t pc = w < we ? __popc(bits[w]) : 0;
+        int32_t incl = pc;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int32_t y = __shfl_up_sync(FULL, incl, d);
+            if (lane >= d) incl += y;
+        }
+        if (w < we) wpre[w] = run + incl - pc;
+        run += __shfl_sync(FULL, incl, 31);
+    }
+    if (tid == 0 && tot != expect) raise(a.err, DEV_COUNT_MISMATCH);
+    __syncthreads();
+
+    // Columns of C's row.
+    for (int w = tid; w < nwords; w += THREADS) {
+        uint32_t word = bits[w];
+        int64_t p = wpre[w];
+        while (word) {
+            const int b = __ffs(word) - 1;
+            word &= word - 1u;
+            if (p < expect) a.Ci[obase + p] = (w << 5) + b;
+            ++p;
+        }
+    }
+
+    // Values, vcap ranks per pass.
+    for (int64_t s0 = 0; s0 < expect; s0 += vcap) {
+        const int ns = (int)min((int64_t)vcap, expect - s0);
+        for (int i = tid; i < ns; i += THREADS) vals[i] = 0.0;
+        for (int32_t eb = e0; eb < e1; eb += THREADS) {
+            int nb;
+            const int32_t total =
+                stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
+            int32_t tb, te;
+            warp_share<THREADS>(total, &tb, &te);
+            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
+                if (v) {
+                    const int32_t c = a.B.idx[pos];
+                    const int w = c >> 5;
+                    const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u)) - s0;
+                    if (r >= 0 && r < ns) atomicAdd(&vals[r], __dmul_rn(av[e], a.B.val[pos]));
+                }
+            });
+            __syncthreads();
+        }
+        for (int i = tid; i < ns; i += THREADS) a.Cv[obase + s0 + i] = vals[i];
+        __syncthreads();
+    }
 }
 
 // Dense rows: one CTA per row sweeps windows of W columns.  The per-entry
@@ -642,14 +800,12 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
                         const int32_t c = p < end ? a.B.idx[p] : INT_MAX;
                         const bool v = c < c_hi;
                         const unsigned m = __ballot_sync(FULL, v);
-                        if (v) {
-                            // cursors never point below the window (it starts at
-                            // the smallest next column); the guard keeps a
-                            // malformed row inside shared memory all the same
-                            const int rel = max(c - c_lo, 0);
-                            atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[p]));
-                            set_bits_aggregated(bits, rel, m);
-                        }
+                        // cursors never point below the window (it starts at the
+                        // smallest next column); the guard keeps a malformed row
+                        // inside shared memory all the same
+                        const int rel = v ? max(c - c_lo, 0) : 0;
+                        if (v) atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[p]));
+                        or_bits_runs(bits, v, (uint32_t)rel);
                         const int n = __popc(m);
                         cur += n;
                         if (n < 32) {
@@ -662,12 +818,10 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
                         const int32_t q = q0 + lane;
                         const int32_t c = q < end ? a.B.idx[q] : INT_MAX;
                         const bool v = c >= c_lo && c < c_hi;
-                        const unsigned m = __ballot_sync(FULL, v);
-                        if (v) {
-                            const int rel = c - c_lo;
-                            atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[q]));
-                            set_bits_aggregated(bits, rel, m);
-                        } else if (c >= c_hi) {
+                        const int rel = v ? c - c_lo : 0;
+                        if (v) atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[q]));
+                        or_bits_runs(bits, v, (uint32_t)rel);
+                        if (!v && c >= c_hi) {
                             nxt = min(nxt, c);
                         }
                     }
@@ -726,6 +880,10 @@ constexpr size_t kSmemNumCtaS = StageLayout<kNumCtaSThreads>::bytes + (size_t)kN
 constexpr size_t kSmemNumCtaL = StageLayout<kNumCtaLThreads>::bytes + (size_t)kNumCtaLTable * 12;
 constexpr size_t kSmemDense = (size_t)kDenseWindow * 8 + kDenseWindow / 8 + (size_t)kDenseStage * 20;
 constexpr size_t kSmemWideBase = StageLayout<kWideThreads>::bytes;
+constexpr int kRankSThreads = 256, kRankSVcap = kNumCtaLMax;
+constexpr int kRankLThreads = 1024;
+constexpr size_t kSmemRankSMax = StageLayout<kRankSThreads>::bytes + 8 * (kRankColsMax / 32) + 8 * (size_t)kRankSVcap;
+constexpr size_t kSmemRankLMax = 200 * 1024;
 
 }  // namespace
 
@@ -746,6 +904,10 @@ void init_kernel_attributes() {
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDense);
     cudaFuncSetAttribute(k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, false>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDense);
+    cudaFuncSetAttribute(k_num_rank<kRankSThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemRankSMax);
+    cudaFuncSetAttribute(k_num_rank<kRankLThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemRankLMax);
 }
 
 static int wide_window_bits(int64_t ncols) {
@@ -794,15 +956,25 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
                 <<<(unsigned)ceil_div(n, kNumWarpRows), 32 * kNumWarpRows, kSmemNumWarp, s>>>(a, lo, n);
             break;
         case NB_HCTA_S:
-            k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>
-                <<<(unsigned)n, kNumCtaSThreads, kSmemNumCtaS, s>>>(a, lo);
-            break;
         case NB_HCTA_L:
-            k_num_hash_cta<kNumCtaLThreads, kNumCtaLTable>
-                <<<(unsigned)n, kNumCtaLThreads, kSmemNumCtaL, s>>>(a, lo);
+            if (a.rankWords > 0) {
+                const size_t smem = StageLayout<kRankSThreads>::bytes + 8 * (size_t)a.rankWords +
+                                    8 * (size_t)kRankSVcap;
+                k_num_rank<kRankSThreads><<<(unsigned)n, kRankSThreads, smem, s>>>(a, lo, a.rankWords, kRankSVcap);
+            } else if (bin == NB_HCTA_S) {
+                k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>
+                    <<<(unsigned)n, kNumCtaSThreads, kSmemNumCtaS, s>>>(a, lo);
+            } else {
+                k_num_hash_cta<kNumCtaLThreads, kNumCtaLTable>
+                    <<<(unsigned)n, kNumCtaLThreads, kSmemNumCtaL, s>>>(a, lo);
+            }
             break;
         case NB_DENSE:
-            if (a.bSorted)
+            if (a.rankWords > 0) {
+                const size_t fixed = StageLayout<kRankLThreads>::bytes + 8 * (size_t)a.rankWords;
+                const int vcap = (int)((kSmemRankLMax - fixed) / 8);
+                k_num_rank<kRankLThreads><<<(unsigned)n, kRankLThreads, kSmemRankLMax, s>>>(a, lo, a.rankWords, vcap);
+            } else if (a.bSorted)
                 k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, true>
                     <<<(unsigned)n, kDenseThreads, kSmemDense, s>>>(a, lo);
             else

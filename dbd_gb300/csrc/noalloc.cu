@@ -234,6 +234,7 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     na.Cv = c_val;
     na.state = state;
     na.bSorted = hflags[3] ? 0 : 1;
+    na.rankWords = rank_words(B.n);
     na.err = flags;
     for (int bin = NB_TINY; bin < NB_COUNT; ++bin)
         launch_numeric_bin(na, bin, numStart_h[bin], numStart_h[bin + 1], s, &launches);
