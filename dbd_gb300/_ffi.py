@@ -89,6 +89,8 @@ SIGNATURES = {
     "dbd_csr_free": (None, [C.POINTER(CsrOut)]),
     "dbd_spgemm_noalloc": (C.c_int, [C.POINTER(CsrView), C.POINTER(CsrView), C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_int64, C.POINTER(C.c_int64), C.c_void_p]),
+    "dbd_spgemm_adjoint": (C.c_int, [C.c_void_p, C.POINTER(CsrView), C.POINTER(CsrView), C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_int, C.c_int]),
 }
 
 _lib = None

@@ -72,6 +72,12 @@ struct SymArgs {
     int32_t *rowNnz;
     uint32_t *ctr;
     int *err;
+    // Optional store of the wide rows' column bitmaps for the numeric rank
+    // kernel (null: not kept): wideWords words per wide row, at the row's
+    // position in the wide bin; wideSlot[row] receives that position.
+    uint32_t *wideBits = nullptr;
+    int32_t *wideSlot = nullptr;
+    int wideWords = 0;
 };
 // Launches the symbolic kernel of bin `bin` over list[begin, begin + n).
 void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cudaStream_t s, int *launches);
@@ -90,6 +96,12 @@ struct NumArgs {
     int bSorted;          // B's rows have ascending columns
     int rankWords;        // > 0: C's columns fit a shared bitmap of this many words (rank kernels)
     int *err;
+    // Column bitmaps of the wide rows kept by the symbolic pass (null: the
+    // rank kernel rebuilds them); a row is wide when rowP[row] > kSymCtaMax.
+    const int64_t *rowP = nullptr;
+    const uint32_t *wideBits = nullptr;
+    const int32_t *wideSlot = nullptr;
+    int wideWords = 0;
 };
 
 // C's columns up to this count use the rank kernels (bitmap + rank prefix,
@@ -99,6 +111,22 @@ inline int rank_words(int64_t ncols) { return ncols <= kRankColsMax ? (int)ceil_
 // Runs the numeric kernels of bin b over list[lo, hi).
 void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,
                         int *launches);
+
+// Adjoint of C = A*B over fixed patterns: given G = dL/dC on C's pattern
+// (Cp, Ci), dA[e] = sum_k G(i,k) B(j,k) for e = (i,j) in A and
+// dB[f] += A(i,j) G(i,k) for f = (j,k) in B.  dA and dB start at zero.
+struct AdjArgs {
+    CsrDev A, B;
+    const int64_t *Cp;
+    const int32_t *Ci;
+    const double *G;
+    double *dA;
+    double *dB;
+    const int32_t *order;  // rows of A in the forward's numeric bin order (null: 0..m-1)
+    int64_t nrows;
+    int *err;
+};
+void launch_adjoint(const AdjArgs &a, cudaStream_t s, int *launches);
 
 // One-time kernel attribute setup (dynamic shared memory limits).
 void init_kernel_attributes();

@@ -131,6 +131,12 @@ struct dbd_ctx {
     DevBuf rowP, symBin, numBin, rowNnz, symList, numList, hist, symTileOff, numTileOff, symStart,
         numStart, part, Cp, cursor, err, blockP, flags;
     DevBuf Ci, Cv;           // resident product or device output ring
+    DevBuf wideBits, wideSlot;  // column bitmaps of wide rows kept for the numeric pass
+    int wideWords = 0;          // words per kept bitmap (0: none kept this multiply)
+    // C's pattern left on the device by the last multiply (for the adjoint).
+    bool patternOk = false;
+    int64_t patA = -1, patB = -1;
+    DevBuf adjG, adjA, adjB;    // device copies for host-side adjoint arguments
     int64_t m = 0, ncols = 0, nnzC = 0, products = 0;
     int64_t nblocks = 0, ntiles = 0;
     bool divided = false;
@@ -435,6 +441,22 @@ int symbolic(dbd_ctx *c) {
     sa.rowNnz = c->rowNnz.as<int32_t>();
     sa.ctr = nullptr;
     sa.err = c->err.as<int>();
+    // Keep the wide rows' column bitmaps for the numeric rank kernel when C's
+    // columns fit one and the store stays within an eighth of the GPU budget.
+    c->wideWords = 0;
+    {
+        const int words = rank_words(c->ncols);
+        const int64_t nwide = c->symStart_h[SB_WIDE + 1] - c->symStart_h[SB_WIDE];
+        const double bytes = 4.0 * (double)words * (double)nwide;
+        if (words > 0 && nwide > 0 && bytes <= c->cfg.gpu_gib * kGiB / 8) {
+            CK(c, c->wideBits.ensure((size_t)bytes));
+            CK(c, c->wideSlot.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1)));
+            sa.wideBits = c->wideBits.as<uint32_t>();
+            sa.wideSlot = c->wideSlot.as<int32_t>();
+            sa.wideWords = words;
+            c->wideWords = words;
+        }
+    }
     // Bins run concurrently, one stream each (heaviest first).
     static const int sorder[] = {SB_WIDE, SB_HCTA, SB_HWARP, SB_TINY};
     Fork fk(c);
@@ -485,6 +507,12 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     na.bSorted = opB_sorted(c);
     na.rankWords = rank_words(na.B.n);
     na.err = c->err.as<int>();
+    na.rowP = c->rowP.as<int64_t>();
+    if (c->wideWords > 0) {
+        na.wideBits = c->wideBits.as<uint32_t>();
+        na.wideSlot = c->wideSlot.as<int32_t>();
+        na.wideWords = c->wideWords;
+    }
     const int64_t t0 = r0 / kTileRows;
     const int64_t t1 = (r1 >= c->m) ? c->ntiles : r1 / kTileRows;
     // Bins run concurrently, one stream each; heaviest first so that their
@@ -592,6 +620,7 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         if (rc) return rc;
     }
     c->divided = false;  // the bin lists are consumed by this multiply
+    c->patternOk = false;
     const auto t0 = Clock::now();
     int rc = symbolic(c);
     if (rc) return rc;
@@ -879,6 +908,9 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         else c->stats.t_scan_ms += x;
     }
     c->last_scope = scope;
+    c->patternOk = scope == DBD_SCOPE_KERNEL && resident;
+    c->patA = c->A.dev.nnz;
+    c->patB = opB(c).nnz;
     return DBD_OK;
 }
 
@@ -967,7 +999,8 @@ void dbd_destroy(dbd_ctx *c) {
     for (DevBuf *b : {&c->A.ptr, &c->A.idx, &c->A.val, &c->A.tmp, &c->B.ptr, &c->B.idx, &c->B.val, &c->B.tmp,
                       &c->rowP, &c->symBin, &c->numBin, &c->rowNnz, &c->symList, &c->numList, &c->hist,
                       &c->symTileOff, &c->numTileOff, &c->symStart, &c->numStart, &c->part, &c->Cp, &c->cursor,
-                      &c->err, &c->blockP, &c->flags, &c->Ci, &c->Cv})
+                      &c->err, &c->blockP, &c->flags, &c->Ci, &c->Cv, &c->wideBits, &c->wideSlot, &c->adjG,
+                      &c->adjA, &c->adjB})
         b->release();
     c->hCp.release();
     c->hCi.release();
@@ -1074,7 +1107,7 @@ int dbd_result_copy(dbd_ctx *c, int64_t *row_ptr, int32_t *col_idx, double *val)
     dbd_csr_out o;
     int rc = dbd_result(c, &o);
     if (rc) return rc;
-    const cudaMemcpyKind k = o.on_device ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+    const cudaMemcpyKind k = cudaMemcpyDefault;  // host or device destinations (unified addressing)
     if (row_ptr) CK(c, cudaMemcpy(row_ptr, o.row_ptr, sizeof(int64_t) * (size_t)(o.n_rows + 1), k));
     if (o.nnz > 0) {
         if (col_idx) CK(c, cudaMemcpy(col_idx, o.col_idx, sizeof(int32_t) * (size_t)o.nnz, k));
@@ -1118,6 +1151,69 @@ int dbd_spgemm(dbd_ctx *c, const dbd_csr_view *a, const dbd_csr_view *b, dbd_sco
         return dbd_result(c, out);
     }
     return DBD_OK;
+}
+
+int dbd_spgemm_adjoint(dbd_ctx *c, const dbd_csr_view *a, const dbd_csr_view *b, const double *g, double *da,
+                       double *db, int on_device, int recompute_pattern) {
+    if (!c || !a || !g || !da || !db) return DBD_ERR_INVALID;
+    cudaSetDevice(c->cfg.device);
+    const dbd_csr_view *bb = (b && b != a) ? b : a;
+    const bool have = c->patternOk && c->m == a->n_rows && c->ncols == bb->n_cols && c->patA == a->nnz &&
+                      c->patB == bb->nnz;
+    int rc;
+    if (recompute_pattern || !have) {
+        rc = dbd_spgemm(c, a, b, DBD_SCOPE_KERNEL, nullptr, nullptr, nullptr);
+        if (rc) return rc;
+        if (!c->patternOk) return set_err(c, DBD_ERR_BUDGET, "C's pattern does not fit the device budget");
+    } else {
+        // Same patterns as the last multiply: only the values may have changed.
+        rc = load_operand(c, c->A, a, "A");
+        if (rc) return rc;
+        c->b_is_a = bb == a;
+        if (!c->b_is_a) {
+            rc = load_operand(c, c->B, bb, "B");
+            if (rc) return rc;
+        }
+    }
+    const CsrDev &A = c->A.dev;
+    const CsrDev &B = opB(c);
+    const int64_t nnzC = c->nnzC;
+    const double *dG = g;
+    double *dA = da, *dB = db;
+    if (!on_device) {
+        CK(c, c->adjG.ensure(sizeof(double) * (size_t)std::max<int64_t>(nnzC, 1)));
+        CK(c, c->adjA.ensure(sizeof(double) * (size_t)std::max<int64_t>(A.nnz, 1)));
+        CK(c, c->adjB.ensure(sizeof(double) * (size_t)std::max<int64_t>(B.nnz, 1)));
+        if (nnzC > 0)
+            CK(c, cudaMemcpyAsync(c->adjG.p, g, sizeof(double) * (size_t)nnzC, cudaMemcpyHostToDevice, c->stream));
+        dG = c->adjG.as<double>();
+        dA = c->adjA.as<double>();
+        dB = c->adjB.as<double>();
+    }
+    if (A.nnz > 0) CK(c, cudaMemsetAsync(dA, 0, sizeof(double) * (size_t)A.nnz, c->stream));
+    if (B.nnz > 0) CK(c, cudaMemsetAsync(dB, 0, sizeof(double) * (size_t)B.nnz, c->stream));
+    CK(c, cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
+    AdjArgs aa;
+    aa.A = A;
+    aa.B = B;
+    aa.Cp = c->Cp.as<int64_t>();
+    aa.Ci = c->Ci.as<int32_t>();
+    aa.G = dG;
+    aa.dA = dA;
+    aa.dB = dB;
+    aa.order = c->numList.as<int32_t>();
+    aa.nrows = c->m;
+    aa.err = c->err.as<int>();
+    int launches = 0;
+    launch_adjoint(aa, c->stream, &launches);
+    CK(c, cudaGetLastError());
+    if (!on_device) {
+        if (A.nnz > 0)
+            CK(c, cudaMemcpyAsync(da, dA, sizeof(double) * (size_t)A.nnz, cudaMemcpyDeviceToHost, c->stream));
+        if (B.nnz > 0)
+            CK(c, cudaMemcpyAsync(db, dB, sizeof(double) * (size_t)B.nnz, cudaMemcpyDeviceToHost, c->stream));
+    }
+    return check_device_err(c, "adjoint");
 }
 
 int dbd_spgemm_files(dbd_ctx *c, const char *path_a, const char *path_b, dbd_scope scope, const char *out_dir,

@@ -426,6 +426,12 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
             });
             __syncthreads();
         }
+        if (a.wideBits) {
+            // One window covers all columns here; keep the row's bitmap.
+            uint32_t *dst = a.wideBits + (size_t)blockIdx.x * a.wideWords;
+            for (int i = tid; i < a.wideWords; i += THREADS) dst[i] = bm[i];
+            if (tid == 0) a.wideSlot[row] = (int32_t)blockIdx.x;
+        }
         for (int i = tid; i < words; i += THREADS) cnt += __popc(bm[i]);
         __syncthreads();
     }
@@ -618,8 +624,10 @@ __global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo)
 // words' popcounts gives every column its rank among the row's columns, which
 // is its position in C's row.  Pass 2 accumulates every product into
 // vals[rank].  The output is in column order without hashing or sorting.
-// Rows with more than vcap entries accumulate vcap ranks per pass 2.
-template <int THREADS>
+// Rows with more than vcap entries accumulate vcap ranks per pass 2.  With
+// GLOBAL_ACC the row's slice of C's values is zeroed and accumulated in place
+// by FP64 reductions at L2 (no shared value array, no slices).
+template <int THREADS, bool GLOBAL_ACC>
 __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int nwords, int vcap) {
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
@@ -637,17 +645,24 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
     const int64_t obase = a.Cp[row] - a.outBase;
 
-    for (int i = tid; i < nwords; i += THREADS) bits[i] = 0u;
-    for (int32_t eb = e0; eb < e1; eb += THREADS) {
-        int nb;
-        const int32_t total =
-            stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
-        int32_t tb, te;
-        warp_share<THREADS>(total, &tb, &te);
-        warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-            or_bits_runs(bits, v, v ? (uint32_t)a.B.idx[pos] : 0u);
-        });
+    if (a.wideBits && a.wideWords == nwords && a.rowP[row] > kSymCtaMax) {
+        // The symbolic pass kept this row's bitmap.
+        const uint32_t *src = a.wideBits + (size_t)a.wideSlot[row] * nwords;
+        for (int i = tid; i < nwords; i += THREADS) bits[i] = src[i];
         __syncthreads();
+    } else {
+        for (int i = tid; i < nwords; i += THREADS) bits[i] = 0u;
+        for (int32_t eb = e0; eb < e1; eb += THREADS) {
+            int nb;
+            const int32_t total =
+                stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
+            int32_t tb, te;
+            warp_share<THREADS>(total, &tb, &te);
+            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
+                or_bits_runs(bits, v, v ? (uint32_t)a.B.idx[pos] : 0u);
+            });
+            __syncthreads();
+        }
     }
 
     // Ranks: each warp takes a contiguous run of words, lanes read 32
@@ -688,10 +703,10 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
         }
     }
 
-    // Values, vcap ranks per pass.
-    for (int64_t s0 = 0; s0 < expect; s0 += vcap) {
-        const int ns = (int)min((int64_t)vcap, expect - s0);
-        for (int i = tid; i < ns; i += THREADS) vals[i] = 0.0;
+    if constexpr (GLOBAL_ACC) {
+        double *cv = a.Cv + obase;
+        for (int64_t i = tid; i < expect; i += THREADS) cv[i] = 0.0;
+        __syncthreads();
         for (int32_t eb = e0; eb < e1; eb += THREADS) {
             int nb;
             const int32_t total =
@@ -702,14 +717,36 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
                 if (v) {
                     const int32_t c = a.B.idx[pos];
                     const int w = c >> 5;
-                    const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u)) - s0;
-                    if (r >= 0 && r < ns) atomicAdd(&vals[r], __dmul_rn(av[e], a.B.val[pos]));
+                    const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
+                    if (r < expect) atomicAdd(&cv[r], __dmul_rn(av[e], a.B.val[pos]));
                 }
             });
             __syncthreads();
         }
-        for (int i = tid; i < ns; i += THREADS) a.Cv[obase + s0 + i] = vals[i];
-        __syncthreads();
+    } else {
+        // Values, vcap ranks per pass.
+        for (int64_t s0 = 0; s0 < expect; s0 += vcap) {
+            const int ns = (int)min((int64_t)vcap, expect - s0);
+            for (int i = tid; i < ns; i += THREADS) vals[i] = 0.0;
+            for (int32_t eb = e0; eb < e1; eb += THREADS) {
+                int nb;
+                const int32_t total =
+                    stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
+                int32_t tb, te;
+                warp_share<THREADS>(total, &tb, &te);
+                warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
+                    if (v) {
+                        const int32_t c = a.B.idx[pos];
+                        const int w = c >> 5;
+                        const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u)) - s0;
+                        if (r >= 0 && r < ns) atomicAdd(&vals[r], __dmul_rn(av[e], a.B.val[pos]));
+                    }
+                });
+                __syncthreads();
+            }
+            for (int i = tid; i < ns; i += THREADS) a.Cv[obase + s0 + i] = vals[i];
+            __syncthreads();
+        }
     }
 }
 
@@ -864,6 +901,70 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
     if (tid == 0 && run != expect) raise(a.err, DEV_COUNT_MISMATCH);
 }
 
+// ======================================================================
+// Adjoint (no reference counterpart): gradients with respect to A's and B's
+// values over their fixed patterns, given G = dL/dC on C's pattern.
+// ======================================================================
+
+// Position of column k within C's sorted row [lo, hi), or hi.
+__device__ __forceinline__ int64_t find_col(const int32_t *__restrict__ ci, int64_t lo, int64_t hi, int32_t k) {
+    const int64_t end = hi;
+    while (lo < hi) {
+        const int64_t mid = lo + ((hi - lo) >> 1);
+        if (ci[mid] < k) lo = mid + 1;
+        else hi = mid;
+    }
+    return (lo < end && ci[lo] == k) ? lo : end;
+}
+
+// One warp per row of A, rows in the forward's numeric order heaviest bins
+// first.  Every product (e = (i,j), f = (j,k)) looks up g = G(i,k) in C's
+// row i, adds A[e] * g to dB[f] (FP64 reduction at L2) and g * B[f] to dA[e]
+// (summed over the adjacent lanes that share e first).
+__global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int64_t item = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (item >= a.nrows) return;
+    const int32_t row = a.order ? a.order[a.nrows - 1 - item] : (int32_t)item;
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    const int64_t c0 = a.Cp[row], c1 = a.Cp[row + 1];
+    for (int32_t e = e0; e < e1; e += 32) {
+        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+            const int32_t t = t0 + lane;
+            const int o = chunk_owner(c, t);
+            const int32_t incl_o = __shfl_sync(FULL, c.incl, o);
+            const int32_t len_o = __shfl_sync(FULL, c.len, o);
+            const int32_t bs_o = __shfl_sync(FULL, c.bs, o);
+            const double av = __shfl_sync(FULL, c.a, o);
+            const bool valid = t < c.total;
+            double ga = 0.0;
+            if (valid) {
+                const int32_t pos = bs_o + (t - (incl_o - len_o));
+                const int32_t k = a.B.idx[pos];
+                const int64_t q = find_col(a.Ci, c0, c1, k);
+                if (q < c1) {
+                    const double g = a.G[q];
+                    ga = __dmul_rn(g, a.B.val[pos]);
+                    atomicAdd(&a.dB[pos], __dmul_rn(av, g));
+                } else {
+                    raise(a.err, DEV_COUNT_MISMATCH);
+                }
+            }
+            // Lanes of one entry are adjacent: sum ga over each run of equal o.
+            const int key = valid ? o : -1 - lane;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int ok = __shfl_down_sync(FULL, key, d);
+                const double og = __shfl_down_sync(FULL, ga, d);
+                if (lane + d < 32 && ok == key) ga += og;
+            }
+            const int pk = __shfl_up_sync(FULL, key, 1);
+            if (valid && (lane == 0 || pk != key)) atomicAdd(&a.dA[e + o], ga);
+        }
+    }
+}
+
 // Configurations and their dynamic shared memory.
 constexpr int kSymWarpRows = 8;
 constexpr int kNumWarpRows = 4;
@@ -881,9 +982,9 @@ constexpr size_t kSmemNumCtaL = StageLayout<kNumCtaLThreads>::bytes + (size_t)kN
 constexpr size_t kSmemDense = (size_t)kDenseWindow * 8 + kDenseWindow / 8 + (size_t)kDenseStage * 20;
 constexpr size_t kSmemWideBase = StageLayout<kWideThreads>::bytes;
 constexpr int kRankSThreads = 256, kRankSVcap = kNumCtaLMax;
-constexpr int kRankLThreads = 1024;
+constexpr int kRankLThreads = 512;  // global accumulation: staging + bitmap + ranks only
 constexpr size_t kSmemRankSMax = StageLayout<kRankSThreads>::bytes + 8 * (kRankColsMax / 32) + 8 * (size_t)kRankSVcap;
-constexpr size_t kSmemRankLMax = 200 * 1024;
+constexpr size_t kSmemRankLMax = StageLayout<kRankLThreads>::bytes + 8 * (kRankColsMax / 32);
 
 }  // namespace
 
@@ -904,9 +1005,9 @@ void init_kernel_attributes() {
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDense);
     cudaFuncSetAttribute(k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, false>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemDense);
-    cudaFuncSetAttribute(k_num_rank<kRankSThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_num_rank<kRankSThreads, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kSmemRankSMax);
-    cudaFuncSetAttribute(k_num_rank<kRankLThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_num_rank<kRankLThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kSmemRankLMax);
 }
 
@@ -943,6 +1044,12 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
     ++*launches;
 }
 
+void launch_adjoint(const AdjArgs &a, cudaStream_t s, int *launches) {
+    if (a.nrows <= 0) return;
+    k_adjoint<<<(unsigned)ceil_div(a.nrows, 8), 256, 0, s>>>(a);
+    ++*launches;
+}
+
 void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,
                         int *launches) {
     const int32_t n = hi - lo;
@@ -960,7 +1067,8 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
             if (a.rankWords > 0) {
                 const size_t smem = StageLayout<kRankSThreads>::bytes + 8 * (size_t)a.rankWords +
                                     8 * (size_t)kRankSVcap;
-                k_num_rank<kRankSThreads><<<(unsigned)n, kRankSThreads, smem, s>>>(a, lo, a.rankWords, kRankSVcap);
+                k_num_rank<kRankSThreads, false>
+                    <<<(unsigned)n, kRankSThreads, smem, s>>>(a, lo, a.rankWords, kRankSVcap);
             } else if (bin == NB_HCTA_S) {
                 k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>
                     <<<(unsigned)n, kNumCtaSThreads, kSmemNumCtaS, s>>>(a, lo);
@@ -971,9 +1079,8 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
             break;
         case NB_DENSE:
             if (a.rankWords > 0) {
-                const size_t fixed = StageLayout<kRankLThreads>::bytes + 8 * (size_t)a.rankWords;
-                const int vcap = (int)((kSmemRankLMax - fixed) / 8);
-                k_num_rank<kRankLThreads><<<(unsigned)n, kRankLThreads, kSmemRankLMax, s>>>(a, lo, a.rankWords, vcap);
+                const size_t smem = StageLayout<kRankLThreads>::bytes + 8 * (size_t)a.rankWords;
+                k_num_rank<kRankLThreads, true><<<(unsigned)n, kRankLThreads, smem, s>>>(a, lo, a.rankWords, 0);
             } else if (a.bSorted)
                 k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, true>
                     <<<(unsigned)n, kDenseThreads, kSmemDense, s>>>(a, lo);

@@ -210,9 +210,10 @@ int dbd_distribute_workload(dbd_ctx *ctx, dbd_scope scope, const char *out_dir);
 int dbd_result(dbd_ctx *ctx, dbd_csr_out *c);
 
 /* Copies the product of the last multiply (device- or host-resident) into
- * caller-provided host arrays sized from dbd_result: row_ptr n_rows+1,
- * col_idx and val nnz entries.  For FFI callers that cannot read device
- * memory; the reference hands results back only through Ptr/Idx/Val.output. */
+ * caller-provided arrays, host or device memory, sized from dbd_result:
+ * row_ptr n_rows+1, col_idx and val nnz entries; any of them may be NULL.
+ * For FFI callers that cannot read the context's memory; the reference hands
+ * results back only through Ptr/Idx/Val.output. */
 int dbd_result_copy(dbd_ctx *ctx, int64_t *row_ptr, int32_t *col_idx, double *val);
 
 int dbd_get_stats(const dbd_ctx *ctx, dbd_stats *st);
@@ -231,6 +232,23 @@ int dbd_spgemm_files(dbd_ctx *ctx, const char *path_a, const char *path_b,
                      dbd_scope scope, const char *out_dir, dbd_stats *st);
 
 void dbd_csr_free(dbd_csr_out *c);
+
+/* ---- adjoint (no reference counterpart) ----------------------------------- */
+
+/* Gradients of a scalar loss L(C), C = A*B, with respect to the values of A
+ * and B over their fixed patterns:  dA = mask_A(G * B^T),
+ * dB = mask_B(A^T * G), where g holds G = dL/dC on C's pattern in the order
+ * of the product's col_idx (nnz(C) values).  The reference has no
+ * differentiation; this is the benchmark spec's adjoint pair, done as one
+ * SDDMM-style kernel over A's rows in the forward's numeric row order.
+ *
+ * C's pattern is the one the last multiply on this context left on the
+ * device (DBD_SCOPE_KERNEL, resident).  recompute_pattern = 1 recomputes it
+ * from a and b instead, for callers that dropped it to save memory.
+ * on_device = 1: g, da, db are device pointers; 0: host arrays.  da has
+ * nnz(A) entries, db nnz(B); both are overwritten. */
+int dbd_spgemm_adjoint(dbd_ctx *ctx, const dbd_csr_view *a, const dbd_csr_view *b, const double *g,
+                       double *da, double *db, int on_device, int recompute_pattern);
 
 /* ---- allocation-free multiply --------------------------------------------- */
 

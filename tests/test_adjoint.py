@@ -1,0 +1,141 @@
+"""Adjoint of C = A*B over fixed patterns, through the torch.autograd harness.
+
+dA = mask_A(G B^T), dB = mask_B(A^T G) for G = dL/dC; with L = sum(W * C) the
+loss is bilinear, so central differences are exact up to rounding.  Checked
+against the sequential FP64 oracle (|d - oracle| <= 1e-12 * scale), a dense
+reference, and central differences (h = 1e-6) on sampled entries.
+"""
+import numpy as np
+import pytest
+
+from dbd_gb300 import generators as gen
+
+pytestmark = pytest.mark.gpu
+
+
+def to_dev(torch, M):
+    return (torch.from_numpy(np.ascontiguousarray(M.row_ptr, np.int32)).cuda(),
+            torch.from_numpy(np.ascontiguousarray(M.col_idx, np.int32)).cuda(),
+            torch.from_numpy(np.ascontiguousarray(M.val, np.float64)).cuda())
+
+
+def setup(torch, A, B):
+    from dbd_gb300.autograd import Pattern
+    ap, ai, av = to_dev(torch, A)
+    bp, bi, bv = to_dev(torch, B)
+    pat = Pattern(ap, ai, (A.n_rows, A.n_cols), bp, bi, (B.n_rows, B.n_cols))
+    return pat, av.requires_grad_(True), bv.requires_grad_(True)
+
+
+def dense(M):
+    D = np.zeros((M.n_rows, M.n_cols))
+    for r in range(M.n_rows):
+        s, e = M.row_ptr[r], M.row_ptr[r + 1]
+        np.add.at(D[r], M.col_idx[s:e], M.val[s:e])
+    return D
+
+
+@pytest.mark.parametrize("keep", [True, False])
+def test_adjoint_matches_oracle_and_dense(orc, keep):
+    torch = pytest.importorskip("torch")
+    from dbd_gb300.autograd import spgemm, engine
+    A = gen.uniform_rows(300, 7, seed=11, n_cols=200)
+    B = gen.uniform_rows(200, 9, seed=12, n_cols=250)
+    pat, av, bv = setup(torch, A, B)
+    with engine() as eng:
+        c = spgemm(av, bv, pat, eng, keep_pattern=keep)
+        rng = np.random.default_rng(5)
+        w = torch.from_numpy(rng.standard_normal(c.numel())).cuda()
+        (w * c).sum().backward()
+        Cp, Ci = pat.c_ptr.cpu().numpy(), pat.c_idx.cpu().numpy()
+        dA_o, dB_o = orc.adjoint(A, B, Cp, Ci, w.cpu().numpy())
+        dA, dB = av.grad.cpu().numpy(), bv.grad.cpu().numpy()
+        assert np.allclose(dA, dA_o, rtol=1e-12, atol=1e-12)
+        assert np.allclose(dB, dB_o, rtol=1e-12, atol=1e-12)
+        G = np.zeros((300, 250))
+        for r in range(300):
+            G[r, Ci[Cp[r]:Cp[r + 1]]] = w.cpu().numpy()[Cp[r]:Cp[r + 1]]
+        dAd, dBd = G @ dense(B).T, dense(A).T @ G
+        assert np.allclose(dA, dAd[np.repeat(np.arange(300), np.diff(A.row_ptr)), A.col_idx], rtol=1e-10, atol=1e-12)
+        assert np.allclose(dB, dBd[np.repeat(np.arange(200), np.diff(B.row_ptr)), B.col_idx], rtol=1e-10, atol=1e-12)
+
+
+def loss_at(torch, eng, pat, av, bv, w):
+    from dbd_gb300.autograd import spgemm
+    with torch.no_grad():
+        return float((w * spgemm(av, bv, pat, eng)).sum())
+
+
+def test_adjoint_2048_dense_reference_and_central_differences():
+    """The fwd+adjoint workload at its 2,048 x 2,048 sub-size: A, B with 16
+    entries per row, N(0,1) values, W ~ N(0,1) on C's pattern."""
+    torch = pytest.importorskip("torch")
+    from dbd_gb300.autograd import spgemm, engine
+    n = 2048
+    A = gen.uniform_rows(n, 16, seed=21)
+    B = gen.uniform_rows(n, 16, seed=22)
+    pat, av, bv = setup(torch, A, B)
+    with engine() as eng:
+        c = spgemm(av, bv, pat, eng)
+        rng = np.random.default_rng(7)
+        w = torch.from_numpy(rng.standard_normal(c.numel())).cuda()
+        (w * c).sum().backward()
+        Cp, Ci = pat.c_ptr.cpu().numpy(), pat.c_idx.cpu().numpy()
+        G = np.zeros((n, n))
+        wv = w.cpu().numpy()
+        for r in range(n):
+            G[r, Ci[Cp[r]:Cp[r + 1]]] = wv[Cp[r]:Cp[r + 1]]
+        Ad, Bd = dense(A), dense(B)
+        assert np.allclose(dense_vals(G @ Bd.T, A), av.grad.cpu().numpy(), rtol=1e-10, atol=1e-12)
+        assert np.allclose(dense_vals(Ad.T @ G, B), bv.grad.cpu().numpy(), rtol=1e-10, atol=1e-12)
+        h = 1e-6
+        for which, vals, grad in (("A", av, av.grad), ("B", bv, bv.grad)):
+            idx = rng.choice(vals.numel(), 25, replace=False)
+            for i in idx:
+                base = vals.detach().clone()
+                up, dn = base.clone(), base.clone()
+                up[i] += h
+                dn[i] -= h
+                if which == "A":
+                    fd = (loss_at(torch, eng, pat, up, bv.detach(), w) - loss_at(torch, eng, pat, dn, bv.detach(), w)) / (2 * h)
+                else:
+                    fd = (loss_at(torch, eng, pat, av.detach(), up, w) - loss_at(torch, eng, pat, av.detach(), dn, w)) / (2 * h)
+                g = float(grad[i])
+                assert abs(fd - g) <= 1e-6 * max(1.0, abs(g)), (which, i, fd, g)
+
+
+def dense_vals(D, M):
+    rows = np.repeat(np.arange(M.n_rows), np.diff(M.row_ptr))
+    return D[rows, M.col_idx]
+
+
+def test_adjoint_full_size_central_differences():
+    """The fwd+adjoint workload at full size (100,000 x 100,000, 16 per row):
+    central differences on 1,000 sampled entries (500 of A, 500 of B)."""
+    torch = pytest.importorskip("torch")
+    from dbd_gb300.autograd import spgemm, engine
+    n = 100_000
+    A = gen.uniform_rows(n, 16, seed=31)
+    B = gen.uniform_rows(n, 16, seed=32)
+    pat, av, bv = setup(torch, A, B)
+    with engine() as eng:
+        c = spgemm(av, bv, pat, eng)
+        assert c.numel() > 25_000_000
+        rng = np.random.default_rng(9)
+        w = torch.from_numpy(rng.standard_normal(c.numel())).cuda()
+        (w * c).sum().backward()
+        h = 1e-6
+        worst = 0.0
+        for which, vals, grad in (("A", av, av.grad), ("B", bv, bv.grad)):
+            for i in rng.choice(vals.numel(), 500, replace=False):
+                up, dn = vals.detach().clone(), vals.detach().clone()
+                up[i] += h
+                dn[i] -= h
+                if which == "A":
+                    fd = (loss_at(torch, eng, pat, up, bv.detach(), w) - loss_at(torch, eng, pat, dn, bv.detach(), w)) / (2 * h)
+                else:
+                    fd = (loss_at(torch, eng, pat, av.detach(), up, w) - loss_at(torch, eng, pat, av.detach(), dn, w)) / (2 * h)
+                g = float(grad[i])
+                worst = max(worst, abs(fd - g) / max(1.0, abs(g)))
+        # |loss| ~ sqrt(nnz(C)) ~ 5e3: rounding of the loss / (2h) is ~ 1e-9
+        assert worst <= 1e-5, worst
