@@ -64,23 +64,50 @@ def row_products(A):
 def thresholds():
     """Bin thresholds of the library (dbd_internal.h), for per-kernel byte counts."""
     text = open(os.path.join(ROOT, "dbd_gb300", "csrc", "dbd_internal.h")).read()
-    names = ["kTinyMax", "kSymWarpMax", "kSymCtaMax", "kNumWarpMax", "kNumCtaSMax", "kNumCtaLMax"]
+    names = ["kTinyMax", "kSymWarpMax", "kSymCtaMax", "kNumWarpMax", "kNumCtaSMax", "kNumCtaLMax",
+             "kWarpSpanWords", "kRankWordsMax", "kWideHashSpanWords"]
     return {n: int(re.search(rf"\b{n}\s*=\s*(\d+)", text).group(1)) for n in names}
 
 
-def bins(A, rowP, nnz_r):
+def span_words(A, B=None, col_off=0):
+    """Words of 32 columns spanned by each row of A*B (0 for empty rows); B's
+    rows have ascending columns, which sit at col_off in C."""
+    B = A if B is None else B
+    lens = np.diff(B.row_ptr)
+    imax = np.iinfo(np.int64).max
+    first = np.where(lens > 0, B.col_idx[np.minimum(B.row_ptr[:-1], max(B.nnz - 1, 0))].astype(np.int64), imax)
+    last = np.where(lens > 0, B.col_idx[np.maximum(B.row_ptr[1:] - 1, 0)].astype(np.int64), -1)
+    nA = np.diff(A.row_ptr)
+    lo = np.full(A.n_rows, imax, np.int64)
+    hi = np.full(A.n_rows, -1, np.int64)
+    nz = nA > 0
+    if A.nnz:
+        starts = A.row_ptr[:-1][nz]
+        lo[nz] = np.minimum.reduceat(first[A.col_idx], starts)
+        hi[nz] = np.maximum.reduceat(last[A.col_idx], starts)
+    ok = hi >= lo
+    return np.where(ok, ((hi + col_off) >> 5) - ((np.where(ok, lo, 0) + col_off) >> 5) + 1, 0)
+
+
+def bins(A, rowP, nnz_r, sw):
+    """Symbolic and numeric bin of every row (the rules of dbd_internal.h)."""
     t = thresholds()
     nA = np.diff(A.row_ptr)
     tiny = (rowP <= t["kTinyMax"]) & (nA <= 32)
-    sym = np.select([rowP == 0, tiny, rowP <= t["kSymWarpMax"], rowP <= t["kSymCtaMax"]], [0, 1, 2, 3], 4)
-    num = np.select([nnz_r == 0, tiny, nnz_r <= t["kNumWarpMax"], nnz_r <= t["kNumCtaSMax"],
-                     nnz_r <= t["kNumCtaLMax"]], [0, 1, 2, 3, 4], 5)
+    sym = np.select([rowP == 0, tiny, sw <= t["kWarpSpanWords"], rowP <= t["kSymWarpMax"],
+                     (rowP <= t["kSymCtaMax"]) & (sw > t["kWideHashSpanWords"])], [0, 1, 2, 3, 4], 5)
+    num = np.select([nnz_r == 0, tiny, (sw <= t["kWarpSpanWords"]) & (nnz_r <= t["kNumWarpMax"]),
+                     nnz_r <= t["kNumWarpMax"], (sw <= t["kRankWordsMax"]) & (nnz_r <= t["kNumCtaLMax"]),
+                     sw <= t["kRankWordsMax"], nnz_r <= t["kNumCtaSMax"], nnz_r <= t["kNumCtaLMax"]],
+                    [0, 1, 2, 3, 4, 5, 6, 7], 8)
     return sym, num
 
 
-SYM_NAMES = {1: "k_sym_tiny", 2: "k_sym_hash<32,8,1024>", 3: "k_sym_hash<256,1,8192>", 4: "k_sym_wide<512>"}
-NUM_NAMES = {1: "k_num_tiny", 2: "k_num_hash<32,4,512>", 3: "k_num_hash<256,1,2048>",
-             4: "k_num_hash<512,1,8192>", 5: "k_num_dense<512,8192>"}
+SYM_NAMES = {1: "k_sym_tiny", 2: "k_sym_bitw<8>", 3: "k_sym_hash_warp<8,1024>", 4: "k_sym_hash_cta<256,8192>",
+             5: "k_sym_wide<512>"}
+NUM_NAMES = {1: "k_num_tiny", 2: "k_num_rankw<8>", 3: "k_num_hash_warp<4,512>", 4: "k_num_rank<256,shared>",
+             5: "k_num_rank<512,in-place>", 6: "k_num_hash_cta<256,2048>", 7: "k_num_hash_cta<512,8192>",
+             8: "k_num_dense<512,8192>"}
 
 
 def kernel_bytes(A, rowP, nnz_r, sym, num):
@@ -226,6 +253,161 @@ def run_reference_arm(args, rank, world):
     return 0
 
 
+def pinned_copy(torch, M):
+    """M with its arrays in pinned host memory (numpy views of pinned tensors)."""
+    from dbd_gb300.csr import CSR
+    out = []
+    for x in (M.row_ptr, M.col_idx, M.val):
+        t = torch.empty(x.shape[0], dtype=getattr(torch, x.dtype.name), pin_memory=True)
+        t.numpy()[:] = x
+        out.append(t)
+    C_ = CSR(M.n_rows, M.n_cols, out[0].numpy(), out[1].numpy(), out[2].numpy())
+    C_._pinned = out
+    return C_
+
+
+def run_batched(args, local):
+    """512 independent A_q*B_q products: one dbd_spgemm_batched call per step
+    against 512 plain dbd_spgemm calls on the same device-resident pairs."""
+    import torch
+    import dbd_gb300 as dbd
+    from dbd_gb300 import generators as gen
+    from dbd_gb300.csr import CSR
+    count = 512
+    pairs = gen.batched_pairs(count, seed=0)
+    As = [a for a, _, _ in pairs]
+    Bs = [b for _, b, _ in pairs]
+    kinds = [k for _, _, k in pairs]
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(local)
+    keep = []
+
+    def on_dev(M):
+        t = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (M.row_ptr, M.col_idx, M.val)]
+        keep.append(t)
+        return CSR.from_device(M.n_rows, M.n_cols, M.nnz, t[0].data_ptr(), t[1].data_ptr(), t[2].data_ptr())
+
+    dA = [on_dev(A) for A in As]
+    dB = [on_dev(B) for B in Bs]
+    rowP, nA_all, sw_all = [], [], []
+    col_off = 0
+    for A, B in zip(As, Bs):
+        lens = np.diff(B.row_ptr).astype(np.int64)
+        cs = np.concatenate([[0], np.cumsum(lens[A.col_idx])])
+        rowP.append(cs[A.row_ptr[1:]] - cs[A.row_ptr[:-1]])
+        nA_all.append(np.diff(A.row_ptr))
+        sw_all.append(span_words(A, B, col_off))
+        col_off += B.n_cols
+    rowP = np.concatenate(rowP)
+    P = int(rowP.sum())
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    ctx = dbd.Context(cpu_gib=96, gpu_gib=200, rows_per_block=4096, device=local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    torch.cuda.synchronize()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+            flush.zero_()
+        torch.cuda.synchronize()
+        ms, out = [], None
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = fn()
+            e1.record(stream)
+            flush.zero_()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.mean(ms)) / 1e3, out
+
+    with Clocks(local) as clk:
+        t_batch, res = timed(lambda: ctx.spgemm_batched(dA, dB, scope="kernel", fetch=False), args.steps,
+                             args.warmup)
+    launches = int(res.stats["gpu_launches"])
+    nnzC = int(res.stats["nnz_c"])
+    # Roofline of the dominant kernel family of the batched multiply.
+    Cp = np.empty(int(res.row_off[-1]) + 1, np.int64)
+    ctx._lib.dbd_result_copy(ctx.handle, Cp.ctypes.data, None, None)
+    nnz_r = np.diff(Cp)
+    Acat = CSR(len(rowP), col_off, np.concatenate([[0], np.cumsum(np.concatenate(nA_all))]), None, None)
+    Acat.col_idx = np.zeros(0, np.int32)
+    sym, num = bins(Acat, rowP, nnz_r, np.concatenate(sw_all))
+    kb = kernel_bytes(Acat, rowP, nnz_r, sym, num)
+    # Per-kernel times: the same batched multiply on a context that times
+    # every kernel family, the bins one after another.
+    pctx = dbd.Context(cpu_gib=96, gpu_gib=200, rows_per_block=4096, device=local, time_kernels=True)
+    pctx.set_stream(stream.cuda_stream)
+    pctx.spgemm_batched(dA, dB, scope="kernel", fetch=False)
+    flush.zero_()
+    st = pctx.spgemm_batched(dA, dB, scope="kernel", fetch=False).stats
+    torch.cuda.synchronize()
+    pctx.close()
+    ktime = {("num", b): st["t_num_bin_ms"][b] for b in NUM_NAMES}
+    ktime.update({("sym", b): st["t_sym_bin_ms"][b] for b in SYM_NAMES})
+    dom = max(ktime, key=ktime.get)
+    dom_ms = ktime[dom]
+    dom_name, dom_bytes = kb[dom]
+    peak, peak_kind = peaks()
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+
+    def sequential():
+        for q in range(count):
+            ctx.spgemm(dA[q], dB[q], scope="kernel", fetch=False)
+    t_seq, _ = timed(sequential, max(1, min(args.steps, 3)), 1)
+
+    # e2e: host pairs in pinned memory, C back to (pinned) host memory.
+    hA = [pinned_copy(torch, A) for A in As]
+    hB = [pinned_copy(torch, B) for B in Bs]
+    ctx.set_stream(None)
+    ctx.spgemm_batched(hA, hB, scope="d2h", fetch=False)
+    te = []
+    for _ in range(max(1, args.e2e_steps)):
+        t0 = time.perf_counter()
+        ctx.spgemm_batched(hA, hB, scope="d2h", fetch=False)
+        te.append(time.perf_counter() - t0)
+    te = float(np.mean(te))
+    t0 = time.perf_counter()
+    for q in range(count):
+        ctx.spgemm(hA[q], hB[q], scope="d2h", fetch=False)
+    te_seq = time.perf_counter() - t0
+    nnz_in = sum(A.nnz + B.nnz for A, B in zip(As, Bs))
+    rows_in = sum(A.n_rows + B.n_rows + 2 for A, B in zip(As, Bs))
+    h2d = 12 * nnz_in + 4 * rows_in
+    d2h = 12 * nnzC + 8 * (len(rowP) + 1)
+    ctx.close()
+    g = lambda t: round(2.0 * P / t / 1e9, 4)
+    line = {"metric": METRIC, "value": g(t_batch), "unit": "GFLOPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t_batch * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded pairs, numpy PCG64)",
+            "config": {"workload": "batched: 512 independent A_q*B_q, n_q log-uniform in [1024, 65536], "
+                       "uniform Poisson(12) rows or band |i-j|<=32 (50/50 by seed), values U[-1,1], seed 0",
+                       "pairs": count, "banded_pairs": int(sum(k == "banded" for k in kinds)),
+                       "rows": int(len(rowP)), "nnz_a": int(sum(A.nnz for A in As)),
+                       "nnz_b": int(sum(B.nnz for B in Bs)), "products": P, "nnz_c": nnzC,
+                       "scope": "kernel (pairs resident in HBM, C left in HBM)",
+                       "l2": "flushed between steps (512 MiB device write outside the timed events)"},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 2), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                         "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_launch": dom_bytes,
+                         "launch_ms": round(dom_ms, 4),
+                         "kernel_ms_per_step": {kb[k][0]: round(v, 4) for k, v in
+                                                sorted(ktime.items(), key=lambda x: -x[1]) if v}},
+            "sequential": {"gflops": g(t_seq), "ms": round(t_seq * 1e3, 3),
+                           "what": "512 plain dbd_spgemm calls (kernel scope) on the same device-resident pairs"},
+            "batched_vs_sequential": round(t_seq / t_batch, 3),
+            "e2e": {"value": g(te), "unit": "GFLOPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": round(te * 1e3, 3),
+                    "scope": "+D2H through dbd_spgemm_batched with pinned host pairs and pinned host C",
+                    "sequential_gflops": g(te_seq), "sequential_ms": round(te_seq * 1e3, 3)},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -244,6 +426,10 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
+    if args.workload == "batched512":
+        if rank != 0:
+            return 0
+        return run_batched(args, local)
 
     import torch
     import dbd_gb300 as dbd
@@ -266,15 +452,15 @@ def main():
     D = CSR.from_device(A.n_rows, A.n_cols, A.nnz, tp.data_ptr(), ti.data_ptr(), tv.data_ptr())
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
-    ctx = dbd.Context(cpu_gib=96, gpu_gib=200, rows_per_block=rpb, device=local, time_kernels=True)
+    ctx = dbd.Context(cpu_gib=96, gpu_gib=200, rows_per_block=rpb, device=local)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
     ctx.initialize_A(D)
     ctx.initialize_B(D)
 
-    def step():
-        ctx.divide_Blocks()
-        return ctx.distribute_Workload("kernel")
+    def step(c=ctx):
+        c.divide_Blocks()
+        return c.distribute_Workload("kernel")
 
     for _ in range(args.warmup):
         step()
@@ -307,26 +493,40 @@ def main():
     nnzC = int(stats[-1]["nnz_c"])
     launches = int(sum(s["gpu_launches"] for s in stats))
 
-    # Roofline of the dominant kernel family (CUDA events inside the library).
+    # Roofline of the dominant kernel family: a second context runs the same
+    # multiply with CUDA events around every kernel family, the bins one
+    # after another on its stream (outside the timed steps above).
     Cp = np.empty(A.n_rows + 1, np.int64)
     ctx._lib.dbd_result_copy(ctx.handle, Cp.ctypes.data, None, None)
     nnz_r = np.diff(Cp)
-    sym, num = bins(A, rowP, nnz_r)
+    sym, num = bins(A, rowP, nnz_r, span_words(A))
     kb = kernel_bytes(A, rowP, nnz_r, sym, num)
+    pctx = dbd.Context(cpu_gib=96, gpu_gib=200, rows_per_block=rpb, device=local, time_kernels=True)
+    pctx.set_stream(stream.cuda_stream)
+    pctx.initialize_A(D)
+    pctx.initialize_B(D)
+    pstats = []
+    for i in range(args.warmup + 3):
+        st_i = step(pctx)
+        flush.zero_()
+        if i >= args.warmup:
+            pstats.append(st_i)
+    torch.cuda.synchronize()
+    pctx.close()
     ktime = {}
-    for s in stats:
-        for b in range(1, 6):
+    for s in pstats:
+        for b in NUM_NAMES:
             ktime[("num", b)] = ktime.get(("num", b), 0.0) + s["t_num_bin_ms"][b]
-        for b in range(1, 5):
+        for b in SYM_NAMES:
             ktime[("sym", b)] = ktime.get(("sym", b), 0.0) + s["t_sym_bin_ms"][b]
     dom = max(ktime, key=ktime.get)
-    dom_ms = ktime[dom] / len(stats)
+    dom_ms = ktime[dom] / len(pstats)
     dom_name, dom_bytes = kb[dom]
     peak, peak_kind = peaks()
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
     traffic = profiled_traffic().get((args.workload, dom_name))
     bytes_alg = 12 * P + 12 * A.nnz + 4 * (A.n_rows + 1) + 12 * nnzC + 8 * (A.n_rows + 1)
-    shares = {f"{kb[k][0]}": round(v / len(stats), 4) for k, v in sorted(ktime.items(), key=lambda x: -x[1]) if v}
+    shares = {f"{kb[k][0]}": round(v / len(pstats), 4) for k, v in sorted(ktime.items(), key=lambda x: -x[1]) if v}
 
     line = {"metric": METRIC, "value": round(value, 4), "unit": "GFLOPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 4), "higher_is_better": True,

@@ -91,6 +91,23 @@ class Result:
         return 2.0 * self.stats["products"] / t / 1e9 if t > 0 else float("nan")
 
 
+class BatchResult:
+    """Product of one batched multiply: per-pair offsets into the concatenated
+    C (row_off, nnz_off: count + 1 each), the stats and, when fetched, the
+    per-pair host products C[q]."""
+
+    def __init__(self, row_off, nnz_off, stats):
+        self.row_off = row_off
+        self.nnz_off = nnz_off
+        self.stats = stats
+        self.C = None
+
+    @property
+    def gflops(self):
+        t = self.stats["t_total"]
+        return 2.0 * self.stats["products"] / t / 1e9 if t > 0 else float("nan")
+
+
 class Context:
     """A libdbd context: device, budgets, streams, buffers (one per host thread)."""
 
@@ -197,6 +214,43 @@ class Context:
         if not fetch or _scope(scope) == SCOPES["io"]:
             return Result(None, stats)
         return Result(self.result(), stats)
+
+    def spgemm_batched(self, As, Bs=None, scope="kernel", fetch=True):
+        """C_q = A_q * B_q for every pair (Bs=None: A_q * A_q) in one multiply.
+
+        Returns a BatchResult: the pairs' row and entry offsets in the
+        concatenated product, the stats and, with fetch=True, the list of
+        per-pair host CSR products (local columns, row_ptr from 0)."""
+        count = len(As)
+        if Bs is not None and len(Bs) != count:
+            raise ValueError("As and Bs differ in length")
+        va = (_ffi.CsrView * count)()
+        keep = []
+        for q, A in enumerate(As):
+            v, k = A.view()
+            va[q] = v
+            keep.append(k)
+        pb = None
+        if Bs is not None:
+            vb = (_ffi.CsrView * count)()
+            for q, B in enumerate(Bs):
+                v, k = B.view()
+                vb[q] = v
+                keep.append(k)
+            pb = vb
+        row_off = np.zeros(count + 1, np.int64)
+        nnz_off = np.zeros(count + 1, np.int64)
+        st = _ffi.Stats()
+        _check(self._lib.dbd_spgemm_batched(self._h, count, va, pb, _scope(scope), row_off.ctypes.data,
+                                            nnz_off.ctypes.data, None, C.byref(st)), self._h)
+        del keep
+        res = BatchResult(row_off, nnz_off, st.as_dict())
+        if fetch:
+            whole = self.result()
+            ncols = [(Bs[q] if Bs is not None else As[q]).n_cols for q in range(count)]
+            res.C = [whole.slice_pair(row_off[q], row_off[q + 1], nnz_off[q], nnz_off[q + 1], ncols[q])
+                     for q in range(count)]
+        return res
 
     def spgemm_files(self, path_a, path_b=None, scope="io", out_dir="."):
         st = _ffi.Stats()

@@ -16,7 +16,7 @@ ERR_NAMES = {
     -9: "DBD_ERR_DEVICE_CHECK", -10: "DBD_ERR_NO_DEVICE",
 }
 SCOPES = {"kernel": 0, "d2h": 1, "io": 2}
-NUM_BINS = 8
+NUM_BINS = 12
 
 
 class CsrView(C.Structure):
@@ -91,6 +91,8 @@ SIGNATURES = {
                                      C.c_int64, C.POINTER(C.c_int64), C.c_void_p]),
     "dbd_spgemm_adjoint": (C.c_int, [C.c_void_p, C.POINTER(CsrView), C.POINTER(CsrView), C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_int, C.c_int]),
+    "dbd_spgemm_batched": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(CsrView), C.POINTER(CsrView), C.c_int,
+                                     C.c_void_p, C.c_void_p, C.POINTER(CsrOut), C.POINTER(Stats)]),
 }
 
 _lib = None

@@ -71,5 +71,10 @@ class CSR:
         v.on_device = 0
         return v, (ptr, idx, val)
 
+    def slice_pair(self, r0, r1, e0, e1, n_cols):
+        """Rows [r0, r1) with entries [e0, e1) as their own matrix (row_ptr rebased to 0)."""
+        r0, r1, e0, e1 = int(r0), int(r1), int(e0), int(e1)
+        return CSR(r1 - r0, n_cols, self.row_ptr[r0:r1 + 1] - e0, self.col_idx[e0:e1], self.val[e0:e1])
+
     def __repr__(self):
         return f"CSR({self.n_rows}x{self.n_cols}, nnz={self.nnz})"

@@ -15,14 +15,19 @@ struct CsrDev {
     const double *val = nullptr;
 };
 
-// Row categories.  The symbolic pass bins rows by their product count P_r
-// (an upper bound of the row's output size), the numeric pass by the exact
-// output size nnz_r that the symbolic pass found.  Lists of rows per bin keep
+// Row categories.  Each row of C spans the columns [lo, hi] (the smallest
+// and largest column its products reach, from the first and last column of
+// every B row it references); "span words" below is the number of 32-column
+// words that range covers.  The symbolic pass bins rows by their product
+// count P_r (an upper bound of the row's output size) and span, the numeric
+// pass by the exact output size nnz_r and span.  Lists of rows per bin keep
 // row order, so the rows of any run of row blocks form one contiguous range
 // of every bin.
-enum SymBin : uint8_t { SB_EMPTY = 0, SB_TINY, SB_HWARP, SB_HCTA, SB_WIDE, SB_COUNT };
-enum NumBin : uint8_t { NB_EMPTY = 0, NB_TINY, NB_HWARP, NB_HCTA_S, NB_HCTA_L, NB_DENSE, NB_COUNT };
-constexpr int kMaxBins = 8;
+enum SymBin : uint8_t { SB_EMPTY = 0, SB_TINY, SB_BITW, SB_HWARP, SB_HCTA, SB_WIDE, SB_COUNT };
+enum NumBin : uint8_t {
+    NB_EMPTY = 0, NB_TINY, NB_RANKW, NB_HWARP, NB_RANKS, NB_RANKL, NB_HCTA_S, NB_HCTA_L, NB_DENSE, NB_COUNT
+};
+constexpr int kMaxBins = 12;
 constexpr int kTileRows = 256;     // granularity of the per-bin offset tables
 constexpr int kScanTile = 4096;    // rows per CTA of the row_ptr scan
 
@@ -36,9 +41,43 @@ constexpr int kNumCtaSTable = 2048, kNumCtaSMax = 1024;
 constexpr int kNumCtaLTable = 8192, kNumCtaLMax = 4096;
 constexpr int kDenseWindow = 8192;           // FP64 columns per dense window (64 KiB)
 constexpr int kWideWindowBitsMax = 1 << 20;  // symbolic bitmap window (128 KiB)
+constexpr int kWarpSpanWords = 64;           // warp-level bitmap rows: span <= 2048 columns
+constexpr int kRankWordsMax = 8192;          // CTA rank rows: span <= 2^18 columns
+constexpr int kWideHashSpanWords = 2048;     // symbolic: P <= kSymCtaMax rows hash above this span
+
+__host__ __device__ __forceinline__ int span_words(int32_t lo, int32_t hi) {
+    return hi >= lo ? (hi >> 5) - (lo >> 5) + 1 : 0;
+}
+
+__host__ __device__ __forceinline__ uint8_t sym_bin_of(int64_t P, int32_t nA, int sw) {
+    if (P == 0) return SB_EMPTY;
+    if (P <= kTinyMax && nA <= 32) return SB_TINY;
+    if (sw <= kWarpSpanWords) return SB_BITW;
+    if (P <= kSymWarpMax) return SB_HWARP;
+    if (P <= kSymCtaMax && sw > kWideHashSpanWords) return SB_HCTA;
+    return SB_WIDE;
+}
+
+__host__ __device__ __forceinline__ uint8_t num_bin_of(int64_t P, int32_t nA, int32_t nnz, int sw) {
+    if (nnz == 0) return NB_EMPTY;
+    if (P <= kTinyMax && nA <= 32) return NB_TINY;
+    if (sw <= kWarpSpanWords && nnz <= kNumWarpMax) return NB_RANKW;
+    if (nnz <= kNumWarpMax) return NB_HWARP;
+    if (sw <= kRankWordsMax) return nnz <= kNumCtaLMax ? NB_RANKS : NB_RANKL;
+    if (nnz <= kNumCtaSMax) return NB_HCTA_S;
+    if (nnz <= kNumCtaLMax) return NB_HCTA_L;
+    return NB_DENSE;
+}
+
+// Per-row analysis of A*B: products and the column window of each row.
+struct RowInfo {
+    int64_t *rowP = nullptr;  // products
+    int32_t *lo = nullptr;    // smallest column reached (INT32_MAX if none)
+    int32_t *hi = nullptr;    // largest column reached (-1 if none)
+};
 
 // Device-side error word values (kernels never trap; the host reads this).
-enum DevErr : int { DEV_OK = 0, DEV_TABLE_FULL = 1, DEV_COUNT_MISMATCH = 2, DEV_ROW_TOO_LONG = 3 };
+enum DevErr : int { DEV_OK = 0, DEV_TABLE_FULL = 1, DEV_COUNT_MISMATCH = 2, DEV_ROW_TOO_LONG = 3, DEV_OUT_OF_WINDOW = 4 };
 
 // Counter slots for dynamically scheduled kernels (zeroed per multiply).
 enum CounterSlot : int { CTR_SYM_TINY = 0, CTR_SYM_HWARP, CTR_SYM_HCTA, CTR_SYM_WIDE, CTR_COUNT = 16 };
@@ -54,12 +93,15 @@ struct Binning {
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // ---- launchers (k_analysis.cu) ----
-void launch_row_products(const CsrDev &A, const int32_t *Bp, int64_t *rowP, uint8_t *symBin,
-                         int *err, cudaStream_t s, int num_sms);
+// First and last column of every row of B (bmin = INT32_MAX, bmax = -1 for
+// empty rows; any column order).
+void launch_row_minmax(const CsrDev &B, int32_t *bmin, int32_t *bmax, cudaStream_t s, int num_sms);
+void launch_row_products(const CsrDev &A, const int32_t *Bp, const int32_t *bmin, const int32_t *bmax,
+                         const RowInfo &ri, uint8_t *symBin, int *err, cudaStream_t s, int num_sms);
 void launch_block_products(int64_t m, const int64_t *rowP, int64_t rows_per_block,
                            int64_t *blockP, cudaStream_t s);
 void launch_bin_lists(int64_t m, const Binning &b, int nbins, cudaStream_t s);
-void launch_num_bins(int64_t m, const int32_t *Ap, const int64_t *rowP, const int32_t *rowNnz,
+void launch_num_bins(int64_t m, const int32_t *Ap, const RowInfo &ri, const int32_t *rowNnz,
                      uint8_t *numBin, cudaStream_t s, int num_sms);
 void launch_row_scan(int64_t m, const int32_t *rowNnz, int64_t *part, int64_t *Cp, cudaStream_t s);
 void launch_check_sorted(const CsrDev &B, int *unsorted, cudaStream_t s, int num_sms);
@@ -72,12 +114,14 @@ struct SymArgs {
     int32_t *rowNnz;
     uint32_t *ctr;
     int *err;
+    const int32_t *rowLo = nullptr;  // per-row column window (RowInfo)
+    const int32_t *rowHi = nullptr;
     // Optional store of the wide rows' column bitmaps for the numeric rank
-    // kernel (null: not kept): wideWords words per wide row, at the row's
-    // position in the wide bin; wideSlot[row] receives that position.
+    // kernel (null: not kept): kRankWordsMax words per wide row (the row's
+    // window from word lo/32 on), at the row's position in the wide bin;
+    // wideSlot[row] receives that position.
     uint32_t *wideBits = nullptr;
     int32_t *wideSlot = nullptr;
-    int wideWords = 0;
 };
 // Launches the symbolic kernel of bin `bin` over list[begin, begin + n).
 void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cudaStream_t s, int *launches);
@@ -94,20 +138,19 @@ struct NumArgs {
     double *Cv;
     int32_t *state;       // 2 * nnz(A) scratch for the dense windows (cursor, next column)
     int bSorted;          // B's rows have ascending columns
-    int rankWords;        // > 0: C's columns fit a shared bitmap of this many words (rank kernels)
     int *err;
+    const int64_t *rowP = nullptr;   // per-row products and column window (RowInfo)
+    const int32_t *rowLo = nullptr;
+    const int32_t *rowHi = nullptr;
+    // Optional per-row amount subtracted from the columns written to Ci
+    // (batched products: each pair's columns start at 0).
+    const int32_t *colShift = nullptr;
     // Column bitmaps of the wide rows kept by the symbolic pass (null: the
-    // rank kernel rebuilds them); a row is wide when rowP[row] > kSymCtaMax.
-    const int64_t *rowP = nullptr;
+    // rank kernels rebuild them); a row's is kept when its symbolic bin is
+    // SB_WIDE and its window has at most kRankWordsMax words.
     const uint32_t *wideBits = nullptr;
     const int32_t *wideSlot = nullptr;
-    int wideWords = 0;
 };
-
-// C's columns up to this count use the rank kernels (bitmap + rank prefix,
-// 64 KiB of shared memory at the limit).
-constexpr int64_t kRankColsMax = 1 << 18;
-inline int rank_words(int64_t ncols) { return ncols <= kRankColsMax ? (int)ceil_div(ncols > 0 ? ncols : 1, 32) : 0; }
 // Runs the numeric kernels of bin b over list[lo, hi).
 void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,
                         int *launches);
@@ -127,6 +170,28 @@ struct AdjArgs {
     int *err;
 };
 void launch_adjoint(const AdjArgs &a, cudaStream_t s, int *launches);
+
+// ---- batched products (k_batch.cu) ----
+// One operand of one pair and its place in the concatenated operand.
+struct BatchPair {
+    const int32_t *ptr;     // m + 1 row pointers (device-accessible)
+    const int32_t *idx;     // nnz columns in [0, ncols)
+    const double *val;      // nnz values (may alias the output at nnzOff)
+    int64_t m, nnz, ncols;
+    int64_t nnzOff;         // first entry in the concatenated operand
+    int64_t colOff;         // added to every column
+    int32_t shift;          // per-row column shift recorded for the product's rows
+};
+// Concatenates count pairs' operands: rows [rowOff[q], rowOff[q+1]) and
+// entries [nnzOff[q], nnzOff[q+1]) of the output come from pair q.  rowShift
+// (may be null) receives pairs[q].shift for every row of pair q.  *bad gets
+// bit 0 for a malformed row_ptr and bit 1 for a column out of range.
+void launch_batch_gather(const BatchPair *pairs, const int64_t *rowOff, const int64_t *nnzOff, int64_t count,
+                         int64_t totalRows, int64_t totalNnz, int32_t *outPtr, int32_t *outIdx, double *outVal,
+                         int32_t *rowShift, int *bad, cudaStream_t s);
+
+// dst[i] = src[idx[i]] for i < n.
+void launch_gather_i64(const int64_t *src, const int64_t *idx, int64_t n, int64_t *dst, cudaStream_t s);
 
 // One-time kernel attribute setup (dynamic shared memory limits).
 void init_kernel_attributes();

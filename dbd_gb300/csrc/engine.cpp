@@ -99,6 +99,7 @@ struct HostBuf {
 struct Operand {
     CsrDev dev;
     DevBuf ptr, idx, val, tmp;
+    DevBuf bmin, bmax;  // first and last column of every row (as the right operand)
     bool loaded = false;
     int sorted = 0;
 };
@@ -132,11 +133,19 @@ struct dbd_ctx {
         numStart, part, Cp, cursor, err, blockP, flags;
     DevBuf Ci, Cv;           // resident product or device output ring
     DevBuf wideBits, wideSlot;  // column bitmaps of wide rows kept for the numeric pass
-    int wideWords = 0;          // words per kept bitmap (0: none kept this multiply)
+    bool wideKept = false;      // the symbolic pass of this multiply kept them
+    DevBuf rowLo, rowHi;        // column window of every row of C
     // C's pattern left on the device by the last multiply (for the adjoint).
     bool patternOk = false;
     int64_t patA = -1, patB = -1;
     DevBuf adjG, adjA, adjB;    // device copies for host-side adjoint arguments
+    // Batched products: the pairs' placement (device copy of the pair
+    // descriptors and offsets, staged through pinned memory), the per-row
+    // column shift of the concatenated A, and the pair count of the last
+    // batched multiply (0: the last multiply was a single product).
+    DevBuf batchDev, rowShift;
+    HostBuf batchHost;
+    int64_t batchCount = 0;
     int64_t m = 0, ncols = 0, nnzC = 0, products = 0;
     int64_t nblocks = 0, ntiles = 0;
     bool divided = false;
@@ -203,6 +212,7 @@ struct Fork {
         cudaEventRecord(start, c->stream);
     }
     cudaStream_t stream(int b) {
+        if (c->cfg.time_kernels) return c->stream;  // serial: per-kernel events time that kernel alone
         if (!used[b]) cudaStreamWaitEvent(c->bin_streams[b], start, 0);
         used[b] = true;
         return c->bin_streams[b];
@@ -216,6 +226,14 @@ struct Fork {
         }
     }
 };
+
+RowInfo row_info(dbd_ctx *c) {
+    RowInfo ri;
+    ri.rowP = c->rowP.as<int64_t>();
+    ri.lo = c->rowLo.as<int32_t>();
+    ri.hi = c->rowHi.as<int32_t>();
+    return ri;
+}
 
 int set_err(dbd_ctx *c, int code, const std::string &msg) {
     if (c) c->last_error = msg;
@@ -241,6 +259,7 @@ int check_device_err(dbd_ctx *c, const char *stage) {
         const char *what = h == DEV_TABLE_FULL       ? "hash table full"
                            : h == DEV_COUNT_MISMATCH ? "numeric/symbolic count mismatch"
                            : h == DEV_ROW_TOO_LONG   ? "a row has more than 2^31 products"
+                           : h == DEV_OUT_OF_WINDOW  ? "a column lies outside its row's window (B changed after loading?)"
                                                      : "unknown";
         return set_err(c, DBD_ERR_DEVICE_CHECK, std::string(stage) + ": device check failed: " + what);
     }
@@ -266,10 +285,13 @@ int validate_host(dbd_ctx *c, const dbd_csr_view *v, const char *name) {
     return DBD_OK;
 }
 
+int finish_operand(dbd_ctx *c, Operand &op, const CsrDev &d);
+
 int load_operand(dbd_ctx *c, Operand &op, const dbd_csr_view *v, const char *name) {
     int rc = validate_host(c, v, name);
     if (rc) return rc;
     op.loaded = false;
+    c->batchCount = 0;
     CsrDev d;
     d.m = v->n_rows;
     d.n = v->n_cols;
@@ -316,11 +338,20 @@ int load_operand(dbd_ctx *c, Operand &op, const dbd_csr_view *v, const char *nam
         d.idx = op.idx.as<int32_t>();
         d.val = op.val.as<double>();
     }
+    return finish_operand(c, op, d);
+}
+
+// Sortedness and row column ranges of an operand now on the device.
+int finish_operand(dbd_ctx *c, Operand &op, const CsrDev &d) {
     op.dev = d;
     // B's rows ascending lets the dense windows use cursors.
     CK(c, c->flags.ensure(4 * sizeof(int)));
     CK(c, cudaMemsetAsync(c->flags.as<int>() + 2, 0, sizeof(int), c->stream));
     launch_check_sorted(d, c->flags.as<int>() + 2, c->stream, c->num_sms);
+    // Row column ranges, for the column windows of the products' rows.
+    CK(c, op.bmin.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(d.m, 1)));
+    CK(c, op.bmax.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(d.m, 1)));
+    launch_row_minmax(d, op.bmin.as<int32_t>(), op.bmax.as<int32_t>(), c->stream, c->num_sms);
     int unsorted = 0;
     CK(c, cudaMemcpyAsync(&unsorted, c->flags.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
@@ -354,6 +385,8 @@ int divide_blocks(dbd_ctx *c) {
     const size_t mm = (size_t)std::max<int64_t>(m, 1);
     const size_t nt = (size_t)c->ntiles;
     CK(c, c->rowP.ensure(sizeof(int64_t) * mm));
+    CK(c, c->rowLo.ensure(sizeof(int32_t) * mm));
+    CK(c, c->rowHi.ensure(sizeof(int32_t) * mm));
     CK(c, c->symBin.ensure(mm));
     CK(c, c->numBin.ensure(mm));
     CK(c, c->rowNnz.ensure(sizeof(int32_t) * mm));
@@ -372,8 +405,9 @@ int divide_blocks(dbd_ctx *c) {
 
     CK(c, cudaEventRecord(c->evStart, c->stream));
     CK(c, cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
-    launch_row_products(A, B.ptr, c->rowP.as<int64_t>(), c->symBin.as<uint8_t>(), c->err.as<int>(), c->stream,
-                        c->num_sms);
+    const Operand &opb = c->b_is_a ? c->A : c->B;
+    launch_row_products(A, B.ptr, opb.bmin.as<int32_t>(), opb.bmax.as<int32_t>(), row_info(c),
+                        c->symBin.as<uint8_t>(), c->err.as<int>(), c->stream, c->num_sms);
     launch_block_products(m, c->rowP.as<int64_t>(), rpb, c->blockP.as<int64_t>(), c->stream);
     Binning sb{c->symBin.as<uint8_t>(), c->symList.as<int32_t>(), c->hist.as<int32_t>(),
                c->symTileOff.as<int32_t>(), c->symStart.as<int32_t>()};
@@ -441,24 +475,25 @@ int symbolic(dbd_ctx *c) {
     sa.rowNnz = c->rowNnz.as<int32_t>();
     sa.ctr = nullptr;
     sa.err = c->err.as<int>();
-    // Keep the wide rows' column bitmaps for the numeric rank kernel when C's
-    // columns fit one and the store stays within an eighth of the GPU budget.
-    c->wideWords = 0;
+    sa.rowLo = c->rowLo.as<int32_t>();
+    sa.rowHi = c->rowHi.as<int32_t>();
+    // Keep the wide rows' column bitmaps (one slot of kRankWordsMax words per
+    // wide row) for the numeric rank kernels when the store stays within an
+    // eighth of the GPU budget.
+    c->wideKept = false;
     {
-        const int words = rank_words(c->ncols);
         const int64_t nwide = c->symStart_h[SB_WIDE + 1] - c->symStart_h[SB_WIDE];
-        const double bytes = 4.0 * (double)words * (double)nwide;
-        if (words > 0 && nwide > 0 && bytes <= c->cfg.gpu_gib * kGiB / 8) {
+        const double bytes = 4.0 * (double)kRankWordsMax * (double)nwide;
+        if (nwide > 0 && bytes <= c->cfg.gpu_gib * kGiB / 8) {
             CK(c, c->wideBits.ensure((size_t)bytes));
             CK(c, c->wideSlot.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1)));
             sa.wideBits = c->wideBits.as<uint32_t>();
             sa.wideSlot = c->wideSlot.as<int32_t>();
-            sa.wideWords = words;
-            c->wideWords = words;
+            c->wideKept = true;
         }
     }
     // Bins run concurrently, one stream each (heaviest first).
-    static const int sorder[] = {SB_WIDE, SB_HCTA, SB_HWARP, SB_TINY};
+    static const int sorder[] = {SB_WIDE, SB_HCTA, SB_HWARP, SB_BITW, SB_TINY};
     Fork fk(c);
     for (int b : sorder) {
         const int32_t n = c->symStart_h[b + 1] - c->symStart_h[b];
@@ -471,8 +506,8 @@ int symbolic(dbd_ctx *c) {
     fk.join();
     cudaEvent_t es = c->time_ev(c->stream);
     launch_row_scan(m, c->rowNnz.as<int32_t>(), c->part.as<int64_t>(), c->Cp.as<int64_t>(), c->stream);
-    launch_num_bins(m, c->A.dev.ptr, c->rowP.as<int64_t>(), c->rowNnz.as<int32_t>(), c->numBin.as<uint8_t>(),
-                    c->stream, c->num_sms);
+    launch_num_bins(m, c->A.dev.ptr, row_info(c), c->rowNnz.as<int32_t>(), c->numBin.as<uint8_t>(), c->stream,
+                    c->num_sms);
     Binning nb{c->numBin.as<uint8_t>(), c->numList.as<int32_t>(), c->hist.as<int32_t>(),
                c->numTileOff.as<int32_t>(), c->numStart.as<int32_t>()};
     launch_bin_lists(m, nb, NB_COUNT, c->stream);
@@ -505,19 +540,20 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     na.Cv = Cv;
     na.state = c->cursor.as<int32_t>();
     na.bSorted = opB_sorted(c);
-    na.rankWords = rank_words(na.B.n);
     na.err = c->err.as<int>();
     na.rowP = c->rowP.as<int64_t>();
-    if (c->wideWords > 0) {
+    na.rowLo = c->rowLo.as<int32_t>();
+    na.rowHi = c->rowHi.as<int32_t>();
+    if (c->wideKept) {
         na.wideBits = c->wideBits.as<uint32_t>();
         na.wideSlot = c->wideSlot.as<int32_t>();
-        na.wideWords = c->wideWords;
     }
+    if (c->batchCount > 0) na.colShift = c->rowShift.as<int32_t>();
     const int64_t t0 = r0 / kTileRows;
     const int64_t t1 = (r1 >= c->m) ? c->ntiles : r1 / kTileRows;
     // Bins run concurrently, one stream each; heaviest first so that their
     // long CTAs start early.
-    static const int order[] = {NB_DENSE, NB_HCTA_L, NB_HCTA_S, NB_HWARP, NB_TINY};
+    static const int order[] = {NB_DENSE, NB_RANKL, NB_HCTA_L, NB_RANKS, NB_HCTA_S, NB_HWARP, NB_RANKW, NB_TINY};
     Fork fk(c);
     for (int b : order) {
         const int32_t lo = c->numTileOff_h[(size_t)t0 * kMaxBins + b];
@@ -1000,7 +1036,7 @@ void dbd_destroy(dbd_ctx *c) {
                       &c->rowP, &c->symBin, &c->numBin, &c->rowNnz, &c->symList, &c->numList, &c->hist,
                       &c->symTileOff, &c->numTileOff, &c->symStart, &c->numStart, &c->part, &c->Cp, &c->cursor,
                       &c->err, &c->blockP, &c->flags, &c->Ci, &c->Cv, &c->wideBits, &c->wideSlot, &c->adjG,
-                      &c->adjA, &c->adjB})
+                      &c->adjA, &c->adjB, &c->rowLo, &c->rowHi, &c->A.bmin, &c->A.bmax, &c->B.bmin, &c->B.bmax})
         b->release();
     c->hCp.release();
     c->hCi.release();
@@ -1214,6 +1250,157 @@ int dbd_spgemm_adjoint(dbd_ctx *c, const dbd_csr_view *a, const dbd_csr_view *b,
             CK(c, cudaMemcpyAsync(db, dB, sizeof(double) * (size_t)B.nnz, cudaMemcpyDeviceToHost, c->stream));
     }
     return check_device_err(c, "adjoint");
+}
+
+int dbd_spgemm_batched(dbd_ctx *c, int64_t count, const dbd_csr_view *a, const dbd_csr_view *b, dbd_scope scope,
+                       int64_t *c_row_off, int64_t *c_nnz_off, dbd_csr_out *out, dbd_stats *st) {
+    if (!c || !a || count <= 0) return DBD_ERR_INVALID;
+    if (scope != DBD_SCOPE_KERNEL && scope != DBD_SCOPE_D2H)
+        return set_err(c, DBD_ERR_INVALID, "batched products keep C on the device or in host memory (no file scope)");
+    cudaSetDevice(c->cfg.device);
+    c->batchCount = 0;
+    c->A.loaded = c->B.loaded = false;
+    c->divided = false;
+    const bool square = b == nullptr;
+    const dbd_csr_view *bv = square ? a : b;
+    const size_t n1 = (size_t)count + 1;
+    // Pinned staging: pair descriptors of A and B, then rowOffA, nnzOffA,
+    // rowOffB (= the inner offsets, A's column offsets), nnzOffB, colOffC.
+    const size_t descBytes = sizeof(BatchPair) * 2 * (size_t)count;
+    const size_t hostBytes = descBytes + sizeof(int64_t) * 5 * n1;
+    CK(c, cudaStreamSynchronize(c->stream));  // the staging area may still feed an earlier copy
+    CK(c, c->batchHost.ensure(hostBytes));
+    BatchPair *pa = c->batchHost.as<BatchPair>();
+    BatchPair *pb = pa + count;
+    int64_t *rowA = reinterpret_cast<int64_t *>(c->batchHost.as<char>() + descBytes);
+    int64_t *nnzA = rowA + n1, *rowB = nnzA + n1, *nnzB = rowB + n1, *colC = nnzB + n1;
+    rowA[0] = nnzA[0] = rowB[0] = nnzB[0] = colC[0] = 0;
+    for (int64_t q = 0; q < count; ++q) {
+        const dbd_csr_view &x = a[q], &y = bv[q];
+        const std::string tag = "pair " + std::to_string(q);
+        for (const dbd_csr_view *v : {&x, &y}) {
+            if (v->n_rows < 0 || v->n_cols < 0 || v->nnz < 0 || v->val_fp32 || !v->row_ptr ||
+                (v->nnz > 0 && (!v->col_idx || !v->val)) || (v->n_rows == 0 && v->nnz > 0))
+                return set_err(c, DBD_ERR_INVALID, tag + ": malformed operand (FP64 values and row_ptr required)");
+        }
+        if (x.n_cols != y.n_rows) return set_err(c, DBD_ERR_INVALID, tag + ": inner dimensions differ");
+        rowA[q + 1] = rowA[q] + x.n_rows;
+        nnzA[q + 1] = nnzA[q] + x.nnz;
+        rowB[q + 1] = rowB[q] + y.n_rows;
+        nnzB[q + 1] = nnzB[q] + y.nnz;
+        colC[q + 1] = colC[q] + y.n_cols;
+    }
+    const int64_t lim = INT32_MAX - 1;
+    if (rowA[count] > lim || rowB[count] > lim || colC[count] > lim || nnzA[count] > lim || nnzB[count] > lim)
+        return set_err(c, DBD_ERR_INVALID, "the batch exceeds 2^31 rows, columns or entries; split it");
+
+    // Concatenated operands.  Host pairs are copied raw into place (row
+    // pointers into a staging area, since the gather rewrites them); device
+    // pairs are read where they are.
+    auto place = [&](Operand &op, const dbd_csr_view *views, const int64_t *rowOff, const int64_t *nnzOff,
+                     const int64_t *colOff, const int64_t *shiftOff, BatchPair *desc) -> int {
+        const int64_t rows = rowOff[count], ne = nnzOff[count];
+        CK(c, op.ptr.ensure(sizeof(int32_t) * (size_t)(rows + 1)));
+        CK(c, op.idx.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(ne, 1)));
+        CK(c, op.val.ensure(sizeof(double) * (size_t)std::max<int64_t>(ne, 1)));
+        bool anyHost = false;
+        for (int64_t q = 0; q < count; ++q) anyHost = anyHost || !views[q].on_device;
+        if (anyHost) CK(c, op.tmp.ensure(sizeof(int32_t) * (size_t)(rows + count)));
+        for (int64_t q = 0; q < count; ++q) {
+            const dbd_csr_view &v = views[q];
+            BatchPair &d = desc[q];
+            d.m = v.n_rows;
+            d.nnz = v.nnz;
+            d.ncols = v.n_cols;
+            d.nnzOff = nnzOff[q];
+            d.colOff = colOff[q];
+            d.shift = shiftOff ? (int32_t)shiftOff[q] : 0;
+            if (v.on_device) {
+                d.ptr = v.row_ptr;
+                d.idx = v.col_idx;
+                d.val = (const double *)v.val;
+                continue;
+            }
+            int32_t *sp = op.tmp.as<int32_t>() + rowOff[q] + q;
+            int32_t *di = op.idx.as<int32_t>() + nnzOff[q];
+            double *dv = op.val.as<double>() + nnzOff[q];
+            CK(c, cudaMemcpyAsync(sp, v.row_ptr, sizeof(int32_t) * (size_t)(v.n_rows + 1), cudaMemcpyHostToDevice,
+                                  c->stream));
+            if (v.nnz > 0) {
+                CK(c, cudaMemcpyAsync(di, v.col_idx, sizeof(int32_t) * (size_t)v.nnz, cudaMemcpyHostToDevice,
+                                      c->stream));
+                CK(c, cudaMemcpyAsync(dv, v.val, sizeof(double) * (size_t)v.nnz, cudaMemcpyHostToDevice, c->stream));
+            }
+            d.ptr = sp;
+            d.idx = di;
+            d.val = dv;
+        }
+        return DBD_OK;
+    };
+    int rc = place(c->A, a, rowA, nnzA, rowB, colC, pa);
+    if (rc) return rc;
+    if (!square) {
+        rc = place(c->B, bv, rowB, nnzB, colC, nullptr, pb);
+        if (rc) return rc;
+    }
+    CK(c, c->batchDev.ensure(hostBytes + sizeof(int64_t) * n1));
+    CK(c, cudaMemcpyAsync(c->batchDev.p, c->batchHost.p, hostBytes, cudaMemcpyHostToDevice, c->stream));
+    const BatchPair *dpa = c->batchDev.as<BatchPair>();
+    const int64_t *drow = reinterpret_cast<const int64_t *>(c->batchDev.as<char>() + descBytes);
+    const int64_t *dnnzA = drow + n1, *drowB = dnnzA + n1, *dnnzB = drowB + n1;
+    int64_t *dCoff = const_cast<int64_t *>(dnnzB + 2 * n1);
+    CK(c, c->rowShift.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(rowA[count], 1)));
+    CK(c, c->flags.ensure(4 * sizeof(int)));
+    CK(c, cudaMemsetAsync(c->flags.p, 0, sizeof(int), c->stream));
+    launch_batch_gather(dpa, drow, dnnzA, count, rowA[count], nnzA[count], c->A.ptr.as<int32_t>(),
+                        c->A.idx.as<int32_t>(), c->A.val.as<double>(), c->rowShift.as<int32_t>(), c->flags.as<int>(),
+                        c->stream);
+    if (!square)
+        launch_batch_gather(dpa + count, drowB, dnnzB, count, rowB[count], nnzB[count], c->B.ptr.as<int32_t>(),
+                            c->B.idx.as<int32_t>(), c->B.val.as<double>(), nullptr, c->flags.as<int>(), c->stream);
+    CK(c, cudaGetLastError());
+    int bad = 0;
+    CK(c, cudaMemcpyAsync(&bad, c->flags.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (bad) return set_err(c, DBD_ERR_INVALID, (bad & 1) ? "a pair's row_ptr does not span [0, nnz] monotonically"
+                                                          : "a pair's column index is out of range");
+    CsrDev da;
+    da.m = rowA[count];
+    da.n = rowB[count];
+    da.nnz = nnzA[count];
+    da.ptr = c->A.ptr.as<int32_t>();
+    da.idx = c->A.idx.as<int32_t>();
+    da.val = c->A.val.as<double>();
+    rc = finish_operand(c, c->A, da);
+    if (rc) return rc;
+    c->b_is_a = square;
+    if (!square) {
+        CsrDev db;
+        db.m = rowB[count];
+        db.n = colC[count];
+        db.nnz = nnzB[count];
+        db.ptr = c->B.ptr.as<int32_t>();
+        db.idx = c->B.idx.as<int32_t>();
+        db.val = c->B.val.as<double>();
+        rc = finish_operand(c, c->B, db);
+        if (rc) return rc;
+    }
+    c->batchCount = count;
+    rc = divide_blocks(c);
+    if (rc) return rc;
+    rc = distribute(c, scope, nullptr);
+    c->patternOk = false;  // C's columns are pair-local: no adjoint on this pattern
+    if (rc) return rc;
+    // Entry offsets of every pair's rows in C.
+    launch_gather_i64(c->Cp.as<int64_t>(), drow, (int64_t)n1, dCoff, c->stream);
+    int64_t *hCoff = colC;  // the host copy of the column offsets is no longer needed
+    CK(c, cudaMemcpyAsync(hCoff, dCoff, sizeof(int64_t) * n1, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    if (c_row_off) memcpy(c_row_off, rowA, sizeof(int64_t) * n1);
+    if (c_nnz_off) memcpy(c_nnz_off, hCoff, sizeof(int64_t) * n1);
+    if (st) *st = c->stats;
+    if (out) return dbd_result(c, out);
+    return DBD_OK;
 }
 
 int dbd_spgemm_files(dbd_ctx *c, const char *path_a, const char *path_b, dbd_scope scope, const char *out_dir,

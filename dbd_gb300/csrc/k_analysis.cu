@@ -18,26 +18,35 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-__device__ __forceinline__ uint8_t sym_bin_of(int64_t P, int32_t nA) {
-    if (P == 0) return SB_EMPTY;
-    if (P <= kTinyMax && nA <= 32) return SB_TINY;
-    if (P <= kSymWarpMax) return SB_HWARP;
-    if (P <= kSymCtaMax) return SB_HCTA;
-    return SB_WIDE;
+// First and last column of every B row (one warp per row, any column order).
+__global__ void k_row_minmax(CsrDev B, int32_t *__restrict__ bmin, int32_t *__restrict__ bmax) {
+    const int lane = threadIdx.x & 31;
+    int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t stride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (; row < B.m; row += stride) {
+        int32_t lo = INT32_MAX, hi = -1;
+        for (int32_t i = B.ptr[row] + lane; i < B.ptr[row + 1]; i += 32) {
+            const int32_t c = B.idx[i];
+            lo = min(lo, c);
+            hi = max(hi, c);
+        }
+#pragma unroll
+        for (int d = 16; d; d >>= 1) {
+            lo = min(lo, __shfl_xor_sync(FULL, lo, d));
+            hi = max(hi, __shfl_xor_sync(FULL, hi, d));
+        }
+        if (lane == 0) {
+            bmin[row] = lo;
+            bmax[row] = hi;
+        }
+    }
 }
 
-__device__ __forceinline__ uint8_t num_bin_of(int64_t P, int32_t nA, int32_t nnz) {
-    if (nnz == 0) return NB_EMPTY;
-    if (P <= kTinyMax && nA <= 32) return NB_TINY;
-    if (nnz <= kNumWarpMax) return NB_HWARP;
-    if (nnz <= kNumCtaSMax) return NB_HCTA_S;
-    if (nnz <= kNumCtaLMax) return NB_HCTA_L;
-    return NB_DENSE;
-}
-
-// Products per row: P_r = sum over k in A_r of |B_k|.  Eight lanes per row.
-__global__ void k_row_products(CsrDev A, const int32_t *__restrict__ Bp,
-                               int64_t *__restrict__ rowP, uint8_t *__restrict__ symBin,
+// Products per row, P_r = sum over k in A_r of |B_k|, and the row's column
+// window [lo, hi] from the B rows' first and last columns.  Eight lanes per
+// row.
+__global__ void k_row_products(CsrDev A, const int32_t *__restrict__ Bp, const int32_t *__restrict__ bmin,
+                               const int32_t *__restrict__ bmax, RowInfo ri, uint8_t *__restrict__ symBin,
                                int *err) {
     const int lane = threadIdx.x & 31;
     const int sub = lane & 7;
@@ -47,16 +56,24 @@ __global__ void k_row_products(CsrDev A, const int32_t *__restrict__ Bp,
     for (; row < A.m; row += stride) {
         const int32_t s = A.ptr[row], e = A.ptr[row + 1];
         int64_t sum = 0;
+        int32_t lo = INT32_MAX, hi = -1;
         for (int32_t i = s + sub; i < e; i += 8) {
             const int32_t k = A.idx[i];
             sum += (int64_t)(Bp[k + 1] - Bp[k]);
+            lo = min(lo, bmin[k]);
+            hi = max(hi, bmax[k]);
         }
-        sum += __shfl_xor_sync(gmask, sum, 4, 8);
-        sum += __shfl_xor_sync(gmask, sum, 2, 8);
-        sum += __shfl_xor_sync(gmask, sum, 1, 8);
+#pragma unroll
+        for (int d = 4; d; d >>= 1) {
+            sum += __shfl_xor_sync(gmask, sum, d, 8);
+            lo = min(lo, __shfl_xor_sync(gmask, lo, d, 8));
+            hi = max(hi, __shfl_xor_sync(gmask, hi, d, 8));
+        }
         if (sub == 0) {
-            rowP[row] = sum;
-            symBin[row] = sym_bin_of(sum, e - s);
+            ri.rowP[row] = sum;
+            ri.lo[row] = lo;
+            ri.hi[row] = hi;
+            symBin[row] = sym_bin_of(sum, e - s, span_words(lo, hi));
             if (sum > 0x7fffffffLL) atomicCAS(err, 0, (int)DEV_ROW_TOO_LONG);
         }
     }
@@ -81,11 +98,11 @@ __global__ void k_block_products(int64_t m, const int64_t *__restrict__ rowP,
     }
 }
 
-__global__ void k_num_bins(int64_t m, const int32_t *__restrict__ Ap, const int64_t *__restrict__ rowP,
+__global__ void k_num_bins(int64_t m, const int32_t *__restrict__ Ap, RowInfo ri,
                            const int32_t *__restrict__ rowNnz, uint8_t *__restrict__ numBin) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m;
          r += (int64_t)gridDim.x * blockDim.x)
-        numBin[r] = num_bin_of(rowP[r], Ap[r + 1] - Ap[r], rowNnz[r]);
+        numBin[r] = num_bin_of(ri.rowP[r], Ap[r + 1] - Ap[r], rowNnz[r], span_words(ri.lo[r], ri.hi[r]));
 }
 
 // Per-tile (kTileRows rows) counts of each bin.
@@ -303,13 +320,19 @@ __global__ void k_validate_idx(const int32_t *__restrict__ idx, int64_t nnz, int
 
 }  // namespace
 
-void launch_row_products(const CsrDev &A, const int32_t *Bp, int64_t *rowP, uint8_t *symBin,
-                         int *err, cudaStream_t s, int num_sms) {
+void launch_row_minmax(const CsrDev &B, int32_t *bmin, int32_t *bmax, cudaStream_t s, int num_sms) {
+    if (B.m == 0) return;
+    const int grid = (int)std::min<int64_t>(ceil_div(B.m * 32, 256), (int64_t)num_sms * 8);
+    k_row_minmax<<<grid, 256, 0, s>>>(B, bmin, bmax);
+}
+
+void launch_row_products(const CsrDev &A, const int32_t *Bp, const int32_t *bmin, const int32_t *bmax,
+                         const RowInfo &ri, uint8_t *symBin, int *err, cudaStream_t s, int num_sms) {
     if (A.m == 0) return;
     const int threads = 256;
     const int64_t need = ceil_div(A.m * 8, threads);
     const int grid = (int)std::min<int64_t>(need, (int64_t)num_sms * 8);
-    k_row_products<<<grid, threads, 0, s>>>(A, Bp, rowP, symBin, err);
+    k_row_products<<<grid, threads, 0, s>>>(A, Bp, bmin, bmax, ri, symBin, err);
 }
 
 void launch_block_products(int64_t m, const int64_t *rowP, int64_t rows_per_block, int64_t *blockP,
@@ -326,11 +349,11 @@ void launch_bin_lists(int64_t m, const Binning &b, int nbins, cudaStream_t s) {
     if (ntiles > 0) k_bin_scatter<<<(unsigned)ntiles, kTileRows, 0, s>>>(m, b.bin, nbins, b.tileOff, b.list);
 }
 
-void launch_num_bins(int64_t m, const int32_t *Ap, const int64_t *rowP, const int32_t *rowNnz,
+void launch_num_bins(int64_t m, const int32_t *Ap, const RowInfo &ri, const int32_t *rowNnz,
                      uint8_t *numBin, cudaStream_t s, int num_sms) {
     if (m == 0) return;
     const int grid = (int)std::min<int64_t>(ceil_div(m, 256), (int64_t)num_sms * 8);
-    k_num_bins<<<grid, 256, 0, s>>>(m, Ap, rowP, rowNnz, numBin);
+    k_num_bins<<<grid, 256, 0, s>>>(m, Ap, ri, rowNnz, numBin);
 }
 
 void launch_row_scan(int64_t m, const int32_t *rowNnz, int64_t *part, int64_t *Cp, cudaStream_t s) {

@@ -50,6 +50,15 @@ __device__ __forceinline__ uint32_t hslot(int32_t c, int shift) {
 
 __device__ __forceinline__ void raise(int *err, int code) { atomicCAS(err, 0, code); }
 
+// A column's offset in its row's window: true when inside [0, limit), else
+// records DEV_OUT_OF_WINDOW (the window came from B's row ranges, so this
+// only fires when B changed after it was loaded) and the product is skipped.
+__device__ __forceinline__ bool in_window(uint32_t rel, uint32_t limit, int *err) {
+    if (rel < limit) return true;
+    raise(err, DEV_OUT_OF_WINDOW);
+    return false;
+}
+
 // ---------------------------------------------------------------------------
 // Warp-level enumeration of the products of up to 32 consecutive A entries:
 // product t (0 <= t < total) comes from the lane whose inclusive length
@@ -399,7 +408,7 @@ __global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t beg
 // Wide rows: one CTA per row, a shared bitmap over windows of winBits
 // columns; the row's size is the bitmap's popcount.
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, int64_t ncols, int winBits) {
+__global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, int winBits) {
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
     __shared__ int32_t sh[THREADS / 32];
@@ -409,9 +418,14 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
     const int tid = threadIdx.x;
     const int32_t row = a.list[begin + blockIdx.x];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
-    const int words = winBits >> 5;
+    // The row's window [lo, hi], in windows of winBits columns from lo's word.
+    const int32_t rlo = a.rowLo[row], rhi = a.rowHi[row];
+    const int sw = span_words(rlo, rhi);
+    const int64_t base = (int64_t)(rlo >> 5) << 5;
+    const int64_t end = (int64_t)rhi + 1;
     int cnt = 0;
-    for (int64_t c_lo = 0; c_lo < ncols; c_lo += winBits) {
+    for (int64_t c_lo = base; c_lo < end; c_lo += winBits) {
+        const int words = (int)min((int64_t)winBits, end - c_lo + 31) >> 5;
         for (int i = tid; i < words; i += THREADS) bm[i] = 0u;
         for (int32_t eb = e0; eb < e1; eb += THREADS) {
             int nb;
@@ -426,10 +440,10 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
             });
             __syncthreads();
         }
-        if (a.wideBits) {
-            // One window covers all columns here; keep the row's bitmap.
-            uint32_t *dst = a.wideBits + (size_t)blockIdx.x * a.wideWords;
-            for (int i = tid; i < a.wideWords; i += THREADS) dst[i] = bm[i];
+        if (a.wideBits && sw <= kRankWordsMax) {
+            // One window covers the row here; keep its bitmap for the numeric pass.
+            uint32_t *dst = a.wideBits + (size_t)blockIdx.x * kRankWordsMax;
+            for (int i = tid; i < sw; i += THREADS) dst[i] = bm[i];
             if (tid == 0) a.wideSlot[row] = (int32_t)blockIdx.x;
         }
         for (int i = tid; i < words; i += THREADS) cnt += __popc(bm[i]);
@@ -439,9 +453,45 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
     if (tid == 0) a.rowNnz[row] = cnt;
 }
 
+// Narrow rows (window of at most kWarpSpanWords words): one warp per row,
+// a bitmap of the window in shared memory.
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_sym_bitw(SymArgs a, int32_t begin, int32_t count) {
+    __shared__ uint32_t bms[ROWS][kWarpSpanWords];
+    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    if (item >= count) return;
+    uint32_t *bm = bms[g];
+    const int32_t row = a.list[begin + item];
+    const int32_t base = (a.rowLo[row] >> 5) << 5;
+    for (int i = lane; i < kWarpSpanWords; i += 32) bm[i] = 0u;
+    __syncwarp();
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    for (int32_t e = e0; e < e1; e += 32) {
+        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+            const int32_t t = t0 + lane;
+            const int32_t j = chunk_pos(c, t, nullptr);
+            const uint32_t rel = t < c.total ? (uint32_t)(a.B.idx[j] - base) : 0u;
+            const bool v = t < c.total && in_window(rel, kWarpSpanWords * 32, a.err);
+            or_bits_runs(bm, v, rel);
+        }
+    }
+    __syncwarp();
+    int cnt = 0;
+    for (int i = lane; i < kWarpSpanWords; i += 32) cnt += __popc(bm[i]);
+    cnt = warp_sum_i(cnt);
+    if (lane == 0) a.rowNnz[row] = cnt;
+}
+
 // ======================================================================
 // Numeric kernels: columns ascending, values in FP64.
 // ======================================================================
+
+// Amount subtracted from the columns a row writes (0 unless batched).
+__device__ __forceinline__ int32_t col_shift(const NumArgs &a, int32_t row) {
+    return a.colShift ? a.colShift[row] : 0;
+}
 
 __global__ void __launch_bounds__(256) k_num_tiny(NumArgs a, int32_t lo, int32_t count) {
     const int lane = threadIdx.x & 31;
@@ -475,7 +525,7 @@ __global__ void __launch_bounds__(256) k_num_tiny(NumArgs a, int32_t lo, int32_t
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
     const int64_t base = a.Cp[row] - a.outBase;
     if (leader && rank < expect) {
-        a.Ci[base + rank] = col;
+        a.Ci[base + rank] = col - col_shift(a, row);
         a.Cv[base + rank] = acc;
     }
     if (lane == 0 && __popc(lm) != expect) raise(a.err, DEV_COUNT_MISMATCH);
@@ -539,10 +589,11 @@ __device__ __forceinline__ void table_write_sorted(NumArgs &a, int32_t row, int3
     group_sync<GROUP, ROWS>();
     group_bitonic<GROUP, ROWS>(sbuf, N, gt);
     const int64_t obase = a.Cp[row] - a.outBase;
+    const int32_t shift = col_shift(a, row);
     const int wn = (int)min((int64_t)nn, expect);
     for (int i = gt; i < wn; i += GROUP) {
         const uint64_t v = sbuf[i];
-        a.Ci[obase + i] = (int32_t)(v >> 32);
+        a.Ci[obase + i] = (int32_t)(v >> 32) - shift;
         a.Cv[obase + i] = vals[(uint32_t)v];
     }
 }
@@ -628,7 +679,7 @@ __global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo)
 // GLOBAL_ACC the row's slice of C's values is zeroed and accumulated in place
 // by FP64 reductions at L2 (no shared value array, no slices).
 template <int THREADS, bool GLOBAL_ACC>
-__global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int nwords, int vcap) {
+__global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int maxWords, int vcap) {
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
     constexpr int NW = THREADS / 32;
@@ -637,17 +688,23 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
     int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
     double *av = reinterpret_cast<double *>(smem + L::av);
     uint32_t *bits = reinterpret_cast<uint32_t *>(smem + L::bytes);
-    int32_t *wpre = reinterpret_cast<int32_t *>(bits + nwords);
-    double *vals = reinterpret_cast<double *>(wpre + nwords);
+    int32_t *wpre = reinterpret_cast<int32_t *>(bits + maxWords);
+    double *vals = reinterpret_cast<double *>(wpre + maxWords);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int32_t row = a.list[lo + blockIdx.x];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
     const int64_t obase = a.Cp[row] - a.outBase;
+    // The row's window: words [rw0, rw0 + nwords) of C's columns.
+    const int32_t rlo = a.rowLo[row];
+    const int32_t rw0 = rlo >> 5;
+    const int nwords = min(span_words(rlo, a.rowHi[row]), maxWords);
+    const int32_t cbase = rw0 << 5;
+    const int32_t obc = cbase - col_shift(a, row);  // column written for bit 0
 
-    if (a.wideBits && a.wideWords == nwords && a.rowP[row] > kSymCtaMax) {
+    if (a.wideBits && sym_bin_of(a.rowP[row], e1 - e0, nwords) == SB_WIDE) {
         // The symbolic pass kept this row's bitmap.
-        const uint32_t *src = a.wideBits + (size_t)a.wideSlot[row] * nwords;
+        const uint32_t *src = a.wideBits + (size_t)a.wideSlot[row] * kRankWordsMax;
         for (int i = tid; i < nwords; i += THREADS) bits[i] = src[i];
         __syncthreads();
     } else {
@@ -659,7 +716,8 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
             int32_t tb, te;
             warp_share<THREADS>(total, &tb, &te);
             warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-                or_bits_runs(bits, v, v ? (uint32_t)a.B.idx[pos] : 0u);
+                const uint32_t rel = v ? (uint32_t)(a.B.idx[pos] - cbase) : 0u;
+                or_bits_runs(bits, v && in_window(rel, (uint32_t)nwords * 32u, a.err), rel);
             });
             __syncthreads();
         }
@@ -698,7 +756,7 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
         while (word) {
             const int b = __ffs(word) - 1;
             word &= word - 1u;
-            if (p < expect) a.Ci[obase + p] = (w << 5) + b;
+            if (p < expect) a.Ci[obase + p] = obc + (w << 5) + b;
             ++p;
         }
     }
@@ -714,8 +772,8 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
             int32_t tb, te;
             warp_share<THREADS>(total, &tb, &te);
             warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
-                if (v) {
-                    const int32_t c = a.B.idx[pos];
+                const int32_t c = v ? a.B.idx[pos] - cbase : 0;
+                if (v && (uint32_t)c < (uint32_t)nwords * 32u) {
                     const int w = c >> 5;
                     const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
                     if (r < expect) atomicAdd(&cv[r], __dmul_rn(av[e], a.B.val[pos]));
@@ -735,8 +793,8 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
                 warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
-                    if (v) {
-                        const int32_t c = a.B.idx[pos];
+                    const int32_t c = v ? a.B.idx[pos] - cbase : 0;
+                    if (v && (uint32_t)c < (uint32_t)nwords * 32u) {
                         const int w = c >> 5;
                         const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u)) - s0;
                         if (r >= 0 && r < ns) atomicAdd(&vals[r], __dmul_rn(av[e], a.B.val[pos]));
@@ -748,6 +806,86 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
             __syncthreads();
         }
     }
+}
+
+// Narrow rows (window of at most kWarpSpanWords words, at most kNumWarpMax
+// entries): one warp per row with the window's bitmap, word ranks and the
+// row's values in shared memory; the rank kernel's method at warp scale.
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_num_rankw(NumArgs a, int32_t lo, int32_t count) {
+    static_assert(kWarpSpanWords == 64, "two bitmap words per lane");
+    __shared__ uint32_t bms[ROWS][kWarpSpanWords];
+    __shared__ int32_t wps[ROWS][kWarpSpanWords];
+    __shared__ double vs[ROWS][kNumWarpMax];
+    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    if (item >= count) return;
+    uint32_t *bm = bms[g];
+    int32_t *wp = wps[g];
+    double *vals = vs[g];
+    const int32_t row = a.list[lo + item];
+    const int32_t cbase = (a.rowLo[row] >> 5) << 5;
+    const int32_t obc = cbase - col_shift(a, row);  // column written for bit 0
+    const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+    const int64_t obase = a.Cp[row] - a.outBase;
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    for (int i = lane; i < kWarpSpanWords; i += 32) bm[i] = 0u;
+    for (int i = lane; i < kNumWarpMax; i += 32) vals[i] = 0.0;
+    __syncwarp();
+    for (int32_t e = e0; e < e1; e += 32) {
+        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+            const int32_t t = t0 + lane;
+            const int32_t j = chunk_pos(c, t, nullptr);
+            const uint32_t rel = t < c.total ? (uint32_t)(a.B.idx[j] - cbase) : 0u;
+            const bool v = t < c.total && in_window(rel, kWarpSpanWords * 32, a.err);
+            or_bits_runs(bm, v, rel);
+        }
+    }
+    __syncwarp();
+    const int32_t p0 = __popc(bm[lane]), p1 = __popc(bm[lane + 32]);
+    int32_t i0 = p0, i1 = p1;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int32_t y0 = __shfl_up_sync(FULL, i0, d), y1 = __shfl_up_sync(FULL, i1, d);
+        if (lane >= d) {
+            i0 += y0;
+            i1 += y1;
+        }
+    }
+    const int32_t half = __shfl_sync(FULL, i0, 31);
+    const int32_t total = half + __shfl_sync(FULL, i1, 31);
+    wp[lane] = i0 - p0;
+    wp[lane + 32] = half + i1 - p1;
+    if (lane == 0 && total != expect) raise(a.err, DEV_COUNT_MISMATCH);
+    __syncwarp();
+    for (int w = lane; w < kWarpSpanWords; w += 32) {
+        uint32_t word = bm[w];
+        int64_t p = wp[w];
+        while (word) {
+            const int b = __ffs(word) - 1;
+            word &= word - 1u;
+            if (p < expect) a.Ci[obase + p] = obc + (w << 5) + b;
+            ++p;
+        }
+    }
+    for (int32_t e = e0; e < e1; e += 32) {
+        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+            const int32_t t = t0 + lane;
+            double av;
+            const int32_t j = chunk_pos(c, t, &av);
+            const int32_t col = t < c.total ? a.B.idx[j] - cbase : 0;
+            if (t < c.total && (uint32_t)col < (uint32_t)(kWarpSpanWords * 32)) {
+                const int w = col >> 5;
+                const int r = wp[w] + __popc(bm[w] & ((1u << (col & 31)) - 1u));
+                if (r < kNumWarpMax) atomicAdd(&vals[r], __dmul_rn(av, a.B.val[j]));
+            }
+        }
+    }
+    __syncwarp();
+    const int64_t nout = min(expect, (int64_t)kNumWarpMax);
+    for (int64_t i = lane; i < nout; i += 32) a.Cv[obase + i] = vals[i];
 }
 
 // Dense rows: one CTA per row sweeps windows of W columns.  The per-entry
@@ -778,6 +916,7 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
     int32_t *gnext = a.state + a.A.nnz;  // next column per A entry
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
     const int64_t obase = a.Cp[row] - a.outBase;
+    const int32_t shift = col_shift(a, row);
 
     // Initial state of every entry.
     int32_t mymin = INT_MAX;
@@ -890,7 +1029,7 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
             word &= word - 1u;
             const int rel = tid * 32 + b;
             if (pos < expect) {
-                a.Ci[obase + pos] = c_lo + rel;
+                a.Ci[obase + pos] = c_lo - shift + rel;
                 a.Cv[obase + pos] = dense[rel];
             }
             ++pos;
@@ -983,8 +1122,10 @@ constexpr size_t kSmemDense = (size_t)kDenseWindow * 8 + kDenseWindow / 8 + (siz
 constexpr size_t kSmemWideBase = StageLayout<kWideThreads>::bytes;
 constexpr int kRankSThreads = 256, kRankSVcap = kNumCtaLMax;
 constexpr int kRankLThreads = 512;  // global accumulation: staging + bitmap + ranks only
-constexpr size_t kSmemRankSMax = StageLayout<kRankSThreads>::bytes + 8 * (kRankColsMax / 32) + 8 * (size_t)kRankSVcap;
-constexpr size_t kSmemRankLMax = StageLayout<kRankLThreads>::bytes + 8 * (kRankColsMax / 32);
+constexpr size_t kSmemRankSMax = StageLayout<kRankSThreads>::bytes + 8 * (size_t)kRankWordsMax + 8 * (size_t)kRankSVcap;
+constexpr size_t kSmemRankLMax = StageLayout<kRankLThreads>::bytes + 8 * (size_t)kRankWordsMax;
+constexpr int kBitwRows = 8;
+constexpr int kRankwRows = 8;
 
 }  // namespace
 
@@ -1025,6 +1166,9 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
         case SB_TINY:
             k_sym_tiny<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(a, begin, n);
             break;
+        case SB_BITW:
+            k_sym_bitw<kBitwRows><<<(unsigned)ceil_div(n, kBitwRows), 32 * kBitwRows, 0, s>>>(a, begin, n);
+            break;
         case SB_HWARP:
             k_sym_hash_warp<kSymWarpRows, kSymWarpTable>
                 <<<(unsigned)ceil_div(n, kSymWarpRows), 32 * kSymWarpRows, kSmemSymWarp, s>>>(a, begin, n);
@@ -1034,8 +1178,7 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
             break;
         case SB_WIDE: {
             const int wb = wide_window_bits(a.B.n);
-            k_sym_wide<kWideThreads><<<(unsigned)n, kWideThreads, kSmemWideBase + (size_t)wb / 8, s>>>(
-                a, begin, a.B.n, wb);
+            k_sym_wide<kWideThreads><<<(unsigned)n, kWideThreads, kSmemWideBase + (size_t)wb / 8, s>>>(a, begin, wb);
             break;
         }
         default:
@@ -1062,26 +1205,24 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
             k_num_hash_warp<kNumWarpRows, kNumWarpTable>
                 <<<(unsigned)ceil_div(n, kNumWarpRows), 32 * kNumWarpRows, kSmemNumWarp, s>>>(a, lo, n);
             break;
+        case NB_RANKW:
+            k_num_rankw<kRankwRows><<<(unsigned)ceil_div(n, kRankwRows), 32 * kRankwRows, 0, s>>>(a, lo, n);
+            break;
+        case NB_RANKS:
+            k_num_rank<kRankSThreads, false>
+                <<<(unsigned)n, kRankSThreads, kSmemRankSMax, s>>>(a, lo, kRankWordsMax, kRankSVcap);
+            break;
+        case NB_RANKL:
+            k_num_rank<kRankLThreads, true><<<(unsigned)n, kRankLThreads, kSmemRankLMax, s>>>(a, lo, kRankWordsMax, 0);
+            break;
         case NB_HCTA_S:
+            k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable><<<(unsigned)n, kNumCtaSThreads, kSmemNumCtaS, s>>>(a, lo);
+            break;
         case NB_HCTA_L:
-            if (a.rankWords > 0) {
-                const size_t smem = StageLayout<kRankSThreads>::bytes + 8 * (size_t)a.rankWords +
-                                    8 * (size_t)kRankSVcap;
-                k_num_rank<kRankSThreads, false>
-                    <<<(unsigned)n, kRankSThreads, smem, s>>>(a, lo, a.rankWords, kRankSVcap);
-            } else if (bin == NB_HCTA_S) {
-                k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>
-                    <<<(unsigned)n, kNumCtaSThreads, kSmemNumCtaS, s>>>(a, lo);
-            } else {
-                k_num_hash_cta<kNumCtaLThreads, kNumCtaLTable>
-                    <<<(unsigned)n, kNumCtaLThreads, kSmemNumCtaL, s>>>(a, lo);
-            }
+            k_num_hash_cta<kNumCtaLThreads, kNumCtaLTable><<<(unsigned)n, kNumCtaLThreads, kSmemNumCtaL, s>>>(a, lo);
             break;
         case NB_DENSE:
-            if (a.rankWords > 0) {
-                const size_t smem = StageLayout<kRankLThreads>::bytes + 8 * (size_t)a.rankWords;
-                k_num_rank<kRankLThreads, true><<<(unsigned)n, kRankLThreads, smem, s>>>(a, lo, a.rankWords, 0);
-            } else if (a.bSorted)
+            if (a.bSorted)
                 k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, true>
                     <<<(unsigned)n, kDenseThreads, kSmemDense, s>>>(a, lo);
             else

@@ -75,11 +75,16 @@ struct Carver {
     }
 };
 
-// Bytes of scratch the pipeline needs for m rows and nnzA entries of A; the
-// carving below in dbd_spgemm_noalloc takes the same regions in this order.
-size_t scratch_bytes(int64_t m, int64_t nnzA) {
+// Bytes of scratch the pipeline needs for m rows and nnzA entries of A and
+// mB rows of B; the carving below in dbd_spgemm_noalloc takes the same
+// regions in this order.
+size_t scratch_bytes(int64_t m, int64_t nnzA, int64_t mB) {
     Carver c{nullptr};
     const size_t nt = (size_t)ceil_div(m, kTileRows) + 1;
+    c.take<int32_t>((size_t)mB);                   // bmin
+    c.take<int32_t>((size_t)mB);                   // bmax
+    c.take<int32_t>((size_t)m);                    // rowLo
+    c.take<int32_t>((size_t)m);                    // rowHi
     c.take<int64_t>((size_t)m);                    // rowP
     c.take<uint8_t>((size_t)m);                    // symBin
     c.take<uint8_t>((size_t)m);                    // numBin
@@ -129,7 +134,7 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
         !b->row_ptr)
         return fail(DBD_ERR_INVALID, "null operand array");
     const int64_t m = a->n_rows;
-    const size_t need = scratch_bytes(m, a->nnz);
+    const size_t need = scratch_bytes(m, a->nnz, b->n_rows);
     if (need > kDbdNoallocScratchBytes) {
         snprintf(g_msg, sizeof(g_msg),
                  "needs %zu bytes of scratch for %lld rows and %lld entries of A; the limit is %zu bytes",
@@ -144,7 +149,13 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     cudaStream_t s = (cudaStream_t)stream_handle;
     Carver c{base};  // the layout of scratch_bytes()
     const size_t nt = (size_t)ceil_div(m, kTileRows) + 1;
+    int32_t *bmin = c.take<int32_t>((size_t)b->n_rows);
+    int32_t *bmax = c.take<int32_t>((size_t)b->n_rows);
+    RowInfo ri;
+    ri.lo = c.take<int32_t>((size_t)m);
+    ri.hi = c.take<int32_t>((size_t)m);
     int64_t *rowP = c.take<int64_t>((size_t)m);
+    ri.rowP = rowP;
     uint8_t *symBin = c.take<uint8_t>((size_t)m);
     uint8_t *numBin = c.take<uint8_t>((size_t)m);
     int32_t *rowNnz = c.take<int32_t>((size_t)m);
@@ -183,8 +194,9 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     int sms = 0;
     NA_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     launch_check_sorted(B, flags + 3, s, sms);
+    launch_row_minmax(B, bmin, bmax, s, sms);
     // Analysis: products per row, symbolic bins, row lists.
-    launch_row_products(A, B.ptr, rowP, symBin, flags, s, sms);
+    launch_row_products(A, B.ptr, bmin, bmax, ri, symBin, flags, s, sms);
     Binning sb{symBin, symList, hist, symTileOff, symStart};
     launch_bin_lists(m, sb, SB_COUNT, s);
     int32_t symStart_h[kMaxBins + 1];
@@ -202,11 +214,13 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     sa.rowNnz = rowNnz;
     sa.ctr = nullptr;
     sa.err = flags;
+    sa.rowLo = ri.lo;
+    sa.rowHi = ri.hi;
     int launches = 0;
     for (int bin = SB_TINY; bin < SB_COUNT; ++bin)
         launch_symbolic_bin(sa, bin, symStart_h[bin], symStart_h[bin + 1] - symStart_h[bin], s, &launches);
     launch_row_scan(m, rowNnz, part, c_row_ptr, s);
-    launch_num_bins(m, A.ptr, rowP, rowNnz, numBin, s, sms);
+    launch_num_bins(m, A.ptr, ri, rowNnz, numBin, s, sms);
     Binning nb{numBin, numList, hist, numTileOff, numStart};
     launch_bin_lists(m, nb, NB_COUNT, s);
     int64_t nnz = 0;
@@ -234,8 +248,10 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     na.Cv = c_val;
     na.state = state;
     na.bSorted = hflags[3] ? 0 : 1;
-    na.rankWords = rank_words(B.n);
     na.err = flags;
+    na.rowP = rowP;
+    na.rowLo = ri.lo;
+    na.rowHi = ri.hi;
     for (int bin = NB_TINY; bin < NB_COUNT; ++bin)
         launch_numeric_bin(na, bin, numStart_h[bin], numStart_h[bin + 1], s, &launches);
     NA_CK(cudaMemcpyAsync(hflags, flags, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -111,21 +111,40 @@ def uniform_rows(n, k, seed=0, n_cols=None, dist="normal"):
 
 
 def poisson_rows(n, lam, seed=0):
-    """n x n, Poisson(lam) distinct uniform columns per row, values U[-1, 1]."""
+    """n x n, Poisson(lam) distinct uniform columns per row, values U[-1, 1].
+
+    Columns are drawn per row, sorted by (row, column) key, and duplicates
+    redrawn until every row's columns are distinct; the values are drawn in
+    CSR order."""
     rng = _rng(seed)
     counts = np.minimum(rng.poisson(lam, n), n).astype(np.int64)
-    rows, cols = _distinct_cols(rng, counts, n)
-    return _from_coo(n, n, rows, cols, rng.uniform(-1.0, 1.0, rows.size))
+    ptr = np.zeros(n + 1, np.int64)
+    np.cumsum(counts, out=ptr[1:])
+    rows = np.repeat(np.arange(n, dtype=np.int64), counts)
+    key = np.sort(rows * n + rng.integers(0, n, rows.size))
+    while True:
+        dup = np.flatnonzero(key[1:] == key[:-1]) + 1
+        if dup.size == 0:
+            break
+        key[dup] = (key[dup] // n) * n + rng.integers(0, n, dup.size)
+        key.sort()
+    cols = key - rows * n
+    return CSR(n, n, ptr.astype(np.int32), cols.astype(np.int32), rng.uniform(-1.0, 1.0, key.size))
 
 
 def banded(n, half_bandwidth=32, seed=0):
-    """n x n with a_ij != 0 iff |i - j| <= half_bandwidth, values U[-1, 1]."""
+    """n x n with a_ij != 0 iff |i - j| <= half_bandwidth, values U[-1, 1].
+
+    Built row by row in CSR order directly (the entries are generated sorted)."""
     rng = _rng(seed)
-    i = np.repeat(np.arange(n, dtype=np.int64), 2 * half_bandwidth + 1)
-    j = i + np.tile(np.arange(-half_bandwidth, half_bandwidth + 1), n)
-    ok = (j >= 0) & (j < n)
-    i, j = i[ok], j[ok]
-    return _from_coo(n, n, i, j, rng.uniform(-1.0, 1.0, i.size))
+    r = np.arange(n, dtype=np.int64)
+    first = np.maximum(r - half_bandwidth, 0)
+    counts = np.minimum(r + half_bandwidth, n - 1) - first + 1
+    ptr = np.zeros(n + 1, np.int64)
+    np.cumsum(counts, out=ptr[1:])
+    nnz = int(ptr[-1])
+    cols = np.arange(nnz, dtype=np.int64) - np.repeat(ptr[:-1] - first, counts)
+    return CSR(n, n, ptr.astype(np.int32), cols.astype(np.int32), rng.uniform(-1.0, 1.0, nnz))
 
 
 def batched_pairs(count=512, seed=0, n_min=1024, n_max=65536):

@@ -96,13 +96,15 @@ typedef struct {
     int32_t out_val_fp32;     /* Val.output as float32 (reference layout) instead of FP64 */
     int32_t out_ptr32;        /* Ptr.output as int32 (reference layout; fails if nnz(C) >= 2^31) */
     int32_t verbose;          /* print the reference's progress lines */
-    int32_t time_kernels;     /* record CUDA events around every kernel family (dbd_stats.t_*_bin_ms) */
+    int32_t time_kernels;     /* record CUDA events around every kernel family (dbd_stats.t_*_bin_ms);
+                                 the bins then run one after another on the context's stream, so
+                                 each time is that kernel's own duration (for profiling runs) */
     double io_rotate_gib;     /* > 0: +I/O output files wrap after this many GiB (disk smaller than C) */
 } dbd_config;
 
 /* Number of row bins the categoriser produces for the symbolic and numeric
  * kernels (see dbd_stats.rows_per_bin). */
-#define DBD_NUM_BINS 8
+#define DBD_NUM_BINS 12
 
 /* Counters and times of the last multiply.  Times are seconds. */
 typedef struct {
@@ -122,8 +124,9 @@ typedef struct {
     int32_t criteria;         /* categoriser threshold (distributeWorkload.cpp:249-264) */
     int32_t n_chunks;         /* device output chunks streamed */
     int64_t blocks_per_category[3]; /* 0 dense, 1 light, 2 either (distributeWorkload.cpp:266-270) */
-    int64_t rows_per_bin[DBD_NUM_BINS];   /* numeric bins: empty, tiny, warp-hash, cta-hash S, cta-hash L, dense */
-    int64_t sym_rows_per_bin[DBD_NUM_BINS];
+    int64_t rows_per_bin[DBD_NUM_BINS];   /* numeric bins: empty, tiny, warp rank, warp hash, CTA rank (shared),
+                                             CTA rank (in place), CTA hash S, CTA hash L, dense windows */
+    int64_t sym_rows_per_bin[DBD_NUM_BINS]; /* symbolic bins: empty, tiny, warp bitmap, warp hash, CTA hash, CTA bitmap */
     int64_t bytes_d2h;
     int64_t bytes_written;
     int64_t gpu_launches;     /* kernels this library launched for the multiply */
@@ -250,6 +253,31 @@ void dbd_csr_free(dbd_csr_out *c);
 int dbd_spgemm_adjoint(dbd_ctx *ctx, const dbd_csr_view *a, const dbd_csr_view *b, const double *g,
                        double *da, double *db, int on_device, int recompute_pattern);
 
+/* ---- batched products (no reference counterpart) -------------------------- */
+
+/* C_q = A_q * B_q for q in [0, count) -- hundreds of independent, uneven
+ * products in one multiply.  The reference runs one product per process
+ * (main.cpp:152-176); this is the benchmark spec's batched form.  The pairs are
+ * placed block-diagonally, diag(A_q) * diag(B_q) = diag(C_q), so that one set
+ * of binned kernel launches covers the rows of every pair.
+ *
+ * a[q], b[q]: host or device views (each its own residency) with FP64 values;
+ * b == NULL multiplies every A_q by itself.  Sums over the batch (rows, inner
+ * and output columns, entries of A and of B) must stay below 2^31.
+ * scope: DBD_SCOPE_KERNEL (C stays on the device) or DBD_SCOPE_D2H.
+ *
+ * C is returned as one CSR (the same forms as dbd_spgemm's c): pair q owns
+ * rows [c_row_off[q], c_row_off[q+1]) and entries [c_nnz_off[q],
+ * c_nnz_off[q+1]); its row pointers are global (subtract c_nnz_off[q]) and
+ * its column indices are local to C_q (0 .. b[q].n_cols - 1).  c_row_off and
+ * c_nnz_off are host arrays of count + 1 entries (either may be NULL).
+ * Invalid pairs (row_ptr not spanning [0, nnz] monotonically, a column out of
+ * range, mismatched inner dimensions) return DBD_ERR_INVALID before any
+ * multiply.  dbd_spgemm_adjoint does not apply to a batched product. */
+int dbd_spgemm_batched(dbd_ctx *ctx, int64_t count, const dbd_csr_view *a, const dbd_csr_view *b,
+                       dbd_scope scope, int64_t *c_row_off, int64_t *c_nnz_off, dbd_csr_out *c,
+                       dbd_stats *st);
+
 /* ---- allocation-free multiply --------------------------------------------- */
 
 /* Bytes of device scratch that dbd_spgemm_noalloc owns per GPU. */
@@ -273,8 +301,9 @@ int dbd_spgemm_adjoint(dbd_ctx *ctx, const dbd_csr_view *a, const dbd_csr_view *
  * Every temporary array lives in one file-scope device array of
  * DBD_NOALLOC_SCRATCH_BYTES (32 MiB), which each GPU that loads the library
  * holds until the process exits.  Inputs whose scratch would exceed it --
- * about 22 bytes per row of A plus 8 per entry of A, e.g. ~1.2M rows at 2
- * entries per row -- are rejected with DBD_ERR_BUDGET.  The first call on a
+ * about 31 bytes per row of A, 8 per row of B and 8 per entry of A, e.g.
+ * ~700k rows at 2 entries per row of a square A -- are rejected with
+ * DBD_ERR_BUDGET.  The first call on a
  * device sets that device up (its kernel attributes and the array's device
  * address), so make the first call on each device before any stream capture.
  * All calls share the array: calls that overlap on the GPU (other threads or

@@ -102,14 +102,11 @@ def test_rmat_small(ctx, orc, scale, ef, seed):
     check(res.C, A, A, orc)
 
 
-def test_every_numeric_bin_exercised(ctx, orc):
-    """A matrix whose rows fall in every bin (tiny, warp hash, both CTA hash
-    sizes, dense windows), rectangular with n > one dense window."""
-    rng = np.random.default_rng(11)
-    m, k, n = 600, 3000, 20000
+def mixed_rows(rng, m, k, n):
+    """m x k A with row lengths from 1 to 2500, k x n B with Poisson(6) rows."""
     rows, cols = [], []
     lens = np.concatenate([rng.integers(1, 3, 200), rng.integers(5, 20, 150), rng.integers(40, 80, 100),
-                           rng.integers(150, 300, 100), rng.integers(1500, 2500, 50)])
+                           rng.integers(150, 300, 100), rng.integers(1500, 2500, 50)])[:m]
     rng.shuffle(lens)
     for r in range(m):
         c = rng.choice(k, size=int(lens[r]), replace=False)
@@ -119,17 +116,32 @@ def test_every_numeric_bin_exercised(ctx, orc):
     A = gen._from_coo(m, k, rows, cols, rng.uniform(-1, 1, rows.size))
     br, bc = gen._distinct_cols(rng, rng.poisson(6, k).astype(np.int64), n)
     B = gen._from_coo(k, n, br, bc, rng.uniform(-1, 1, br.size))
-    res = ctx.spgemm(A, B, scope="kernel")
-    check(res.C, A, B, orc)
-    used = bins_used(res.stats)
-    assert set(used) >= {1, 2, 3, 4, 5}, res.stats["rows_per_bin"]
+    return A, B
+
+
+def test_every_numeric_bin_exercised(ctx, orc):
+    """Rows in every numeric bin: narrow rows (banded, warp rank), rows within
+    2^18 columns (CTA rank, shared and in place), and rows spanning more than
+    2^18 columns (CTA hash of both sizes, dense windows)."""
+    rng = np.random.default_rng(11)
+    used = set()
+    sym_used = set()
+    cases = [mixed_rows(rng, 600, 3000, 20000), mixed_rows(rng, 600, 3000, 600000),
+             (gen.banded(3000, 8, seed=3), gen.banded(3000, 8, seed=4))]
+    for A, B in cases:
+        res = ctx.spgemm(A, B, scope="kernel")
+        check(res.C, A, B, orc)
+        used |= set(bins_used(res.stats))
+        sym_used |= {i for i, v in enumerate(res.stats["sym_rows_per_bin"]) if v}
+    assert used >= set(range(1, 9)), used
+    assert sym_used >= set(range(1, 6)), sym_used
 
 
 def test_dense_rows_unsorted_b(ctx, orc):
     """Dense-window rows with B rows out of column order take the rescanning path."""
     rng = np.random.default_rng(5)
     A = gen.uniform_rows(64, 1500, seed=1, n_cols=4000, dist="uniform")
-    B = gen.uniform_rows(4000, 12, seed=2, n_cols=30000, dist="uniform")
+    B = gen.uniform_rows(4000, 12, seed=2, n_cols=600000, dist="uniform")
     perm_idx = B.col_idx.copy()
     for r in range(B.n_rows):
         s, e = B.row_ptr[r], B.row_ptr[r + 1]
@@ -139,7 +151,7 @@ def test_dense_rows_unsorted_b(ctx, orc):
     B = CSR(B.n_rows, B.n_cols, B.row_ptr, perm_idx, B.val)
     res = ctx.spgemm(A, B, scope="kernel")
     check(res.C, A, B, orc)
-    assert res.stats["rows_per_bin"][5] > 0
+    assert res.stats["rows_per_bin"][8] > 0  # dense windows
 
 
 def test_edge_cases(ctx, orc):
