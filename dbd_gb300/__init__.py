@@ -252,6 +252,56 @@ class Context:
                      for q in range(count)]
         return res
 
+    # ---- tuning ----
+    @property
+    def tuning(self):
+        """The bin thresholds in use (dict of dbd_tuning's fields)."""
+        t = _ffi.Tuning()
+        _check(self._lib.dbd_get_tuning(self._h, C.byref(t)), self._h)
+        return t.as_dict()
+
+    def set_tuning(self, **kw):
+        """Changes some bin thresholds (names as in dbd_tuning)."""
+        t = _ffi.Tuning()
+        _check(self._lib.dbd_get_tuning(self._h, C.byref(t)), self._h)
+        for k, v in kw.items():
+            if not hasattr(t, k):
+                raise KeyError(k)
+            setattr(t, k, int(v))
+        _check(self._lib.dbd_set_tuning(self._h, C.byref(t)), self._h)
+
+    def autotune(self, repeats=2):
+        """Tunes the bin thresholds on the operands loaded now; returns (tuning, ms)."""
+        t = _ffi.Tuning()
+        ms = C.c_double()
+        _check(self._lib.dbd_autotune(self._h, int(repeats), C.byref(t), C.byref(ms)), self._h)
+        return t.as_dict(), ms.value
+
+    def update_values(self, a_vals, b_vals=None):
+        """New values of A (and B) on the last kernel-scope multiply's patterns:
+        only the numeric kernels run, replayed from a captured CUDA graph.
+
+        a_vals / b_vals: one array per pair (a single array after spgemm),
+        all numpy float64 (host) or all CUDA tensors (device)."""
+        if not isinstance(a_vals, (list, tuple)):
+            a_vals = [a_vals]
+            b_vals = None if b_vals is None else [b_vals]
+
+        def table(vals):
+            on_dev = hasattr(vals[0], "data_ptr")
+            keep = [v if on_dev else np.ascontiguousarray(v, np.float64) for v in vals]
+            t = (C.c_void_p * len(keep))(*[(v.data_ptr() if on_dev else v.ctypes.data) for v in keep])
+            return t, keep, on_dev
+
+        ta, ka, on_dev = table(a_vals)
+        tb, kb = None, None
+        if b_vals is not None:
+            tb, kb, on_dev_b = table(b_vals)
+            if on_dev_b != on_dev:
+                raise ValueError("A and B values must both be host or both be device arrays")
+        _check(self._lib.dbd_update_values(self._h, len(a_vals), ta, tb, 1 if on_dev else 0), self._h)
+        del ka, kb
+
     def spgemm_files(self, path_a, path_b=None, scope="io", out_dir="."):
         st = _ffi.Stats()
         _check(self._lib.dbd_spgemm_files(self._h, os.fsencode(path_a),

@@ -43,6 +43,15 @@ class Config(C.Structure):
                 ("verbose", C.c_int32), ("time_kernels", C.c_int32), ("io_rotate_gib", C.c_double)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("warp_span_words", C.c_int32), ("warp_max_nnz", C.c_int32), ("sym_warp_max_products", C.c_int32),
+                ("rank_words_max", C.c_int32), ("rank_shared_max_nnz", C.c_int32),
+                ("sym_hash_span_words", C.c_int32)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class Stats(C.Structure):
     _fields_ = [("t_preprocess", C.c_double), ("t_compute_gpu", C.c_double), ("t_write_file", C.c_double),
                 ("t_kernel_exec", C.c_double), ("t_total", C.c_double), ("t_d2h", C.c_double),
@@ -93,6 +102,10 @@ SIGNATURES = {
                                      C.c_void_p, C.c_int, C.c_int]),
     "dbd_spgemm_batched": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(CsrView), C.POINTER(CsrView), C.c_int,
                                      C.c_void_p, C.c_void_p, C.POINTER(CsrOut), C.POINTER(Stats)]),
+    "dbd_update_values": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int]),
+    "dbd_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "dbd_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "dbd_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_double)]),
 }
 
 _lib = None

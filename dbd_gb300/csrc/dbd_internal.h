@@ -49,24 +49,51 @@ __host__ __device__ __forceinline__ int span_words(int32_t lo, int32_t hi) {
     return hi >= lo ? (hi >> 5) - (lo >> 5) + 1 : 0;
 }
 
-__host__ __device__ __forceinline__ uint8_t sym_bin_of(int64_t P, int32_t nA, int sw) {
+// Runtime bin thresholds (the autotuner's knobs).  Each is capped by the
+// compile-time size it selects against, so every choice keeps every row
+// inside its kernel's tables: warpSpanWords <= kWarpSpanWords, numWarpMax <=
+// kNumWarpMax, symWarpMax <= kSymWarpMax, rankWordsMax <= kRankWordsMax,
+// rankSharedMax <= kNumCtaLMax (the shared value array of the rank kernel).
+struct Tuning {
+    int32_t warpSpanWords = kWarpSpanWords;   // narrow rows: warp bitmap / warp rank kernels
+    int32_t numWarpMax = kNumWarpMax;         // numeric rows on one warp (rank or hash)
+    int32_t symWarpMax = kSymWarpMax;         // symbolic rows on a warp hash table
+    int32_t rankWordsMax = kRankWordsMax;     // CTA rank kernels for windows up to this many words
+    int32_t rankSharedMax = kNumCtaLMax;      // rank rows accumulating in shared memory
+    int32_t symHashSpanWords = kWideHashSpanWords;  // symbolic CTA rows hash above this span
+};
+
+__host__ __device__ __forceinline__ uint8_t sym_bin_of(int64_t P, int32_t nA, int sw, const Tuning &t) {
     if (P == 0) return SB_EMPTY;
     if (P <= kTinyMax && nA <= 32) return SB_TINY;
-    if (sw <= kWarpSpanWords) return SB_BITW;
-    if (P <= kSymWarpMax) return SB_HWARP;
-    if (P <= kSymCtaMax && sw > kWideHashSpanWords) return SB_HCTA;
+    if (sw <= t.warpSpanWords) return SB_BITW;
+    if (P <= t.symWarpMax) return SB_HWARP;
+    if (P <= kSymCtaMax && sw > t.symHashSpanWords) return SB_HCTA;
     return SB_WIDE;
 }
 
-__host__ __device__ __forceinline__ uint8_t num_bin_of(int64_t P, int32_t nA, int32_t nnz, int sw) {
+__host__ __device__ __forceinline__ uint8_t num_bin_of(int64_t P, int32_t nA, int32_t nnz, int sw,
+                                                       const Tuning &t) {
     if (nnz == 0) return NB_EMPTY;
     if (P <= kTinyMax && nA <= 32) return NB_TINY;
-    if (sw <= kWarpSpanWords && nnz <= kNumWarpMax) return NB_RANKW;
-    if (nnz <= kNumWarpMax) return NB_HWARP;
-    if (sw <= kRankWordsMax) return nnz <= kNumCtaLMax ? NB_RANKS : NB_RANKL;
+    if (sw <= t.warpSpanWords && nnz <= t.numWarpMax) return NB_RANKW;
+    if (nnz <= t.numWarpMax) return NB_HWARP;
+    if (sw <= t.rankWordsMax) return nnz <= t.rankSharedMax ? NB_RANKS : NB_RANKL;
     if (nnz <= kNumCtaSMax) return NB_HCTA_S;
     if (nnz <= kNumCtaLMax) return NB_HCTA_L;
     return NB_DENSE;
+}
+
+// Clamps t into its caps (minimums keep each bin meaningful).
+inline Tuning clamp_tuning(Tuning t) {
+    auto cl = [](int32_t v, int32_t lo, int32_t hi) { return v < lo ? lo : (v > hi ? hi : v); };
+    t.warpSpanWords = cl(t.warpSpanWords, 1, kWarpSpanWords);
+    t.numWarpMax = cl(t.numWarpMax, 1, kNumWarpMax);
+    t.symWarpMax = cl(t.symWarpMax, kTinyMax, kSymWarpMax);
+    t.rankWordsMax = cl(t.rankWordsMax, 1, kRankWordsMax);
+    t.rankSharedMax = cl(t.rankSharedMax, 1, kNumCtaLMax);
+    t.symHashSpanWords = cl(t.symHashSpanWords, 0, 1 << 26);
+    return t;
 }
 
 // Per-row analysis of A*B: products and the column window of each row.
@@ -97,12 +124,13 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // empty rows; any column order).
 void launch_row_minmax(const CsrDev &B, int32_t *bmin, int32_t *bmax, cudaStream_t s, int num_sms);
 void launch_row_products(const CsrDev &A, const int32_t *Bp, const int32_t *bmin, const int32_t *bmax,
-                         const RowInfo &ri, uint8_t *symBin, int *err, cudaStream_t s, int num_sms);
+                         const RowInfo &ri, uint8_t *symBin, int *err, const Tuning &t, cudaStream_t s,
+                         int num_sms);
 void launch_block_products(int64_t m, const int64_t *rowP, int64_t rows_per_block,
                            int64_t *blockP, cudaStream_t s);
 void launch_bin_lists(int64_t m, const Binning &b, int nbins, cudaStream_t s);
 void launch_num_bins(int64_t m, const int32_t *Ap, const RowInfo &ri, const int32_t *rowNnz,
-                     uint8_t *numBin, cudaStream_t s, int num_sms);
+                     uint8_t *numBin, const Tuning &t, cudaStream_t s, int num_sms);
 void launch_row_scan(int64_t m, const int32_t *rowNnz, int64_t *part, int64_t *Cp, cudaStream_t s);
 void launch_check_sorted(const CsrDev &B, int *unsorted, cudaStream_t s, int num_sms);
 
@@ -122,6 +150,7 @@ struct SymArgs {
     // wideSlot[row] receives that position.
     uint32_t *wideBits = nullptr;
     int32_t *wideSlot = nullptr;
+    Tuning tune;
 };
 // Launches the symbolic kernel of bin `bin` over list[begin, begin + n).
 void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cudaStream_t s, int *launches);
@@ -150,6 +179,7 @@ struct NumArgs {
     // SB_WIDE and its window has at most kRankWordsMax words.
     const uint32_t *wideBits = nullptr;
     const int32_t *wideSlot = nullptr;
+    Tuning tune;
 };
 // Runs the numeric kernels of bin b over list[lo, hi).
 void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,

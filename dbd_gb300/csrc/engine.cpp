@@ -146,6 +146,14 @@ struct dbd_ctx {
     DevBuf batchDev, rowShift;
     HostBuf batchHost;
     int64_t batchCount = 0;
+    std::vector<int64_t> batchNnzA, batchNnzB;  // per-pair entry offsets of the last batch (count + 1)
+    // The numeric launches of the last multiply captured as a CUDA graph,
+    // replayed by dbd_update_values (dropped by the next multiply).
+    cudaGraph_t numGraph = nullptr;
+    cudaGraphExec_t numExec = nullptr;
+    bool capturing = false;
+    bool replayOk = false;  // the last multiply left its plan and C on the device (kernel scope)
+    Tuning tune;            // bin thresholds (dbd_set_tuning / dbd_autotune)
     int64_t m = 0, ncols = 0, nnzC = 0, products = 0;
     int64_t nblocks = 0, ntiles = 0;
     bool divided = false;
@@ -180,7 +188,7 @@ struct dbd_ctx {
     std::vector<Timed> timed;
 
     cudaEvent_t time_ev(cudaStream_t s) {
-        if (!cfg.time_kernels) return nullptr;
+        if (!cfg.time_kernels || capturing) return nullptr;
         if (tused == tpool.size()) {
             cudaEvent_t e;
             if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
@@ -233,6 +241,13 @@ RowInfo row_info(dbd_ctx *c) {
     ri.lo = c->rowLo.as<int32_t>();
     ri.hi = c->rowHi.as<int32_t>();
     return ri;
+}
+
+void drop_graph(dbd_ctx *c) {
+    if (c->numExec) cudaGraphExecDestroy(c->numExec);
+    if (c->numGraph) cudaGraphDestroy(c->numGraph);
+    c->numExec = nullptr;
+    c->numGraph = nullptr;
 }
 
 int set_err(dbd_ctx *c, int code, const std::string &msg) {
@@ -292,6 +307,8 @@ int load_operand(dbd_ctx *c, Operand &op, const dbd_csr_view *v, const char *nam
     if (rc) return rc;
     op.loaded = false;
     c->batchCount = 0;
+    c->replayOk = false;  // operand buffers may move: the captured numeric graph is stale
+    drop_graph(c);
     CsrDev d;
     d.m = v->n_rows;
     d.n = v->n_cols;
@@ -373,6 +390,7 @@ int divide_blocks(dbd_ctx *c) {
     const CsrDev &B = opB(c);
     if (A.n != B.m) return set_err(c, DBD_ERR_INVALID, "inner dimensions differ (A.n_cols != B.n_rows)");
     const auto t0 = Clock::now();
+    drop_graph(c);  // the plan it replays is replaced
     c->launches = 0;
     c->tused = c->sused = 0;
     c->timed.clear();
@@ -407,7 +425,7 @@ int divide_blocks(dbd_ctx *c) {
     CK(c, cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream));
     const Operand &opb = c->b_is_a ? c->A : c->B;
     launch_row_products(A, B.ptr, opb.bmin.as<int32_t>(), opb.bmax.as<int32_t>(), row_info(c),
-                        c->symBin.as<uint8_t>(), c->err.as<int>(), c->stream, c->num_sms);
+                        c->symBin.as<uint8_t>(), c->err.as<int>(), c->tune, c->stream, c->num_sms);
     launch_block_products(m, c->rowP.as<int64_t>(), rpb, c->blockP.as<int64_t>(), c->stream);
     Binning sb{c->symBin.as<uint8_t>(), c->symList.as<int32_t>(), c->hist.as<int32_t>(),
                c->symTileOff.as<int32_t>(), c->symStart.as<int32_t>()};
@@ -477,6 +495,7 @@ int symbolic(dbd_ctx *c) {
     sa.err = c->err.as<int>();
     sa.rowLo = c->rowLo.as<int32_t>();
     sa.rowHi = c->rowHi.as<int32_t>();
+    sa.tune = c->tune;
     // Keep the wide rows' column bitmaps (one slot of kRankWordsMax words per
     // wide row) for the numeric rank kernels when the store stays within an
     // eighth of the GPU budget.
@@ -506,7 +525,7 @@ int symbolic(dbd_ctx *c) {
     fk.join();
     cudaEvent_t es = c->time_ev(c->stream);
     launch_row_scan(m, c->rowNnz.as<int32_t>(), c->part.as<int64_t>(), c->Cp.as<int64_t>(), c->stream);
-    launch_num_bins(m, c->A.dev.ptr, row_info(c), c->rowNnz.as<int32_t>(), c->numBin.as<uint8_t>(), c->stream,
+    launch_num_bins(m, c->A.dev.ptr, row_info(c), c->rowNnz.as<int32_t>(), c->numBin.as<uint8_t>(), c->tune, c->stream,
                     c->num_sms);
     Binning nb{c->numBin.as<uint8_t>(), c->numList.as<int32_t>(), c->hist.as<int32_t>(),
                c->numTileOff.as<int32_t>(), c->numStart.as<int32_t>()};
@@ -544,6 +563,7 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     na.rowP = c->rowP.as<int64_t>();
     na.rowLo = c->rowLo.as<int32_t>();
     na.rowHi = c->rowHi.as<int32_t>();
+    na.tune = c->tune;
     if (c->wideKept) {
         na.wideBits = c->wideBits.as<uint32_t>();
         na.wideSlot = c->wideSlot.as<int32_t>();
@@ -657,6 +677,7 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     }
     c->divided = false;  // the bin lists are consumed by this multiply
     c->patternOk = false;
+    c->replayOk = false;
     const auto t0 = Clock::now();
     int rc = symbolic(c);
     if (rc) return rc;
@@ -944,7 +965,8 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         else c->stats.t_scan_ms += x;
     }
     c->last_scope = scope;
-    c->patternOk = scope == DBD_SCOPE_KERNEL && resident;
+    c->replayOk = scope == DBD_SCOPE_KERNEL && resident;
+    c->patternOk = c->replayOk && c->batchCount == 0;  // batched C has pair-local columns
     c->patA = c->A.dev.nnz;
     c->patB = opB(c).nnz;
     return DBD_OK;
@@ -1043,6 +1065,10 @@ void dbd_destroy(dbd_ctx *c) {
     c->hCv.release();
     for (cudaEvent_t e : {c->evStart, c->evPre, c->evSym, c->evEnd, c->evNumA, c->evNumB})
         if (e) cudaEventDestroy(e);
+    drop_graph(c);
+    c->batchDev.release();
+    c->rowShift.release();
+    c->batchHost.release();
     for (cudaEvent_t e : c->tpool) cudaEventDestroy(e);
     for (cudaEvent_t e : c->spool) cudaEventDestroy(e);
     for (int b = 0; b < kMaxBins; ++b) {
@@ -1259,6 +1285,8 @@ int dbd_spgemm_batched(dbd_ctx *c, int64_t count, const dbd_csr_view *a, const d
         return set_err(c, DBD_ERR_INVALID, "batched products keep C on the device or in host memory (no file scope)");
     cudaSetDevice(c->cfg.device);
     c->batchCount = 0;
+    c->replayOk = false;
+    drop_graph(c);
     c->A.loaded = c->B.loaded = false;
     c->divided = false;
     const bool square = b == nullptr;
@@ -1386,6 +1414,8 @@ int dbd_spgemm_batched(dbd_ctx *c, int64_t count, const dbd_csr_view *a, const d
         if (rc) return rc;
     }
     c->batchCount = count;
+    c->batchNnzA.assign(nnzA, nnzA + n1);
+    c->batchNnzB.assign(nnzB, nnzB + n1);
     rc = divide_blocks(c);
     if (rc) return rc;
     rc = distribute(c, scope, nullptr);
@@ -1401,6 +1431,156 @@ int dbd_spgemm_batched(dbd_ctx *c, int64_t count, const dbd_csr_view *a, const d
     if (st) *st = c->stats;
     if (out) return dbd_result(c, out);
     return DBD_OK;
+}
+
+int dbd_get_tuning(const dbd_ctx *c, dbd_tuning *t) {
+    if (!c || !t) return DBD_ERR_INVALID;
+    t->warp_span_words = c->tune.warpSpanWords;
+    t->warp_max_nnz = c->tune.numWarpMax;
+    t->sym_warp_max_products = c->tune.symWarpMax;
+    t->rank_words_max = c->tune.rankWordsMax;
+    t->rank_shared_max_nnz = c->tune.rankSharedMax;
+    t->sym_hash_span_words = c->tune.symHashSpanWords;
+    return DBD_OK;
+}
+
+int dbd_set_tuning(dbd_ctx *c, const dbd_tuning *t) {
+    if (!c || !t) return DBD_ERR_INVALID;
+    Tuning u;
+    u.warpSpanWords = t->warp_span_words;
+    u.numWarpMax = t->warp_max_nnz;
+    u.symWarpMax = t->sym_warp_max_products;
+    u.rankWordsMax = t->rank_words_max;
+    u.rankSharedMax = t->rank_shared_max_nnz;
+    u.symHashSpanWords = t->sym_hash_span_words;
+    const Tuning v = clamp_tuning(u);
+    if (memcmp(&u, &v, sizeof(u)) != 0) return set_err(c, DBD_ERR_INVALID, "a tuning value is out of its range");
+    c->tune = u;
+    c->divided = false;  // bins depend on the thresholds
+    return DBD_OK;
+}
+
+int dbd_autotune(dbd_ctx *c, int repeats, dbd_tuning *best, double *best_ms) {
+    if (!c || repeats < 1) return DBD_ERR_INVALID;
+    if (!c->A.loaded || (!c->b_is_a && !c->B.loaded))
+        return set_err(c, DBD_ERR_INVALID, "load operands (or run a multiply) before autotuning");
+    cudaSetDevice(c->cfg.device);
+    auto run = [&](const Tuning &t, double *ms) -> int {
+        c->tune = t;
+        double bestt = 1e300;
+        for (int r = 0; r < repeats; ++r) {
+            const auto t0 = Clock::now();
+            int rc = divide_blocks(c);
+            if (!rc) rc = distribute(c, DBD_SCOPE_KERNEL, nullptr);
+            if (rc) return rc;
+            bestt = std::min(bestt, seconds_since(t0) * 1e3);
+        }
+        *ms = bestt;
+        return DBD_OK;
+    };
+    // Candidates per knob; the current setting is always one of them.
+    struct Knob {
+        int32_t Tuning::*field;
+        std::vector<int32_t> values;
+    };
+    const std::vector<Knob> knobs = {
+        {&Tuning::warpSpanWords, {8, 16, 32, 64}},
+        {&Tuning::numWarpMax, {64, 128, 256}},
+        {&Tuning::rankWordsMax, {1024, 2048, 4096, 8192}},
+        {&Tuning::rankSharedMax, {512, 1024, 2048, 4096}},
+        {&Tuning::symWarpMax, {128, 256, 512}},
+        {&Tuning::symHashSpanWords, {512, 2048, 8192}},
+    };
+    const Tuning start = c->tune;
+    Tuning cur = start;
+    double cur_ms = 0.0;
+    int rc = run(cur, &cur_ms);  // warms the context up; timed again below
+    if (!rc) rc = run(cur, &cur_ms);
+    for (int sweep = 0; sweep < 2 && !rc; ++sweep) {
+        bool improved = false;
+        for (const Knob &k : knobs) {
+            for (int32_t v : k.values) {
+                if (cur.*k.field == v) continue;
+                Tuning t = cur;
+                t.*k.field = v;
+                t = clamp_tuning(t);
+                double ms = 0.0;
+                rc = run(t, &ms);
+                if (rc) break;
+                if (ms < cur_ms * 0.98) {  // keep a change only for a clear gain
+                    cur = t;
+                    cur_ms = ms;
+                    improved = true;
+                }
+            }
+            if (rc) break;
+        }
+        if (!improved) break;
+    }
+    c->tune = rc ? start : cur;
+    c->divided = false;
+    if (rc) return rc;
+    if (best) dbd_get_tuning(c, best);
+    if (best_ms) *best_ms = cur_ms;
+    return DBD_OK;
+}
+
+int dbd_update_values(dbd_ctx *c, int64_t count, const double *const *a_val, const double *const *b_val,
+                      int on_device) {
+    if (!c || count <= 0 || !a_val) return DBD_ERR_INVALID;
+    cudaSetDevice(c->cfg.device);
+    if (!c->replayOk)
+        return set_err(c, DBD_ERR_INVALID, "values can be updated after a kernel-scope multiply with C resident");
+    const bool batch = c->batchCount > 0;
+    if (batch ? count != c->batchCount : count != 1)
+        return set_err(c, DBD_ERR_INVALID, "count differs from the last multiply's pair count");
+    if (!c->b_is_a && !b_val) return set_err(c, DBD_ERR_INVALID, "b_val is required (the last multiply had a B)");
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    // Values go to context-owned arrays, whose addresses the graph holds.
+    auto put = [&](Operand &op, const double *const *src, const std::vector<int64_t> &off) -> int {
+        const int64_t ne = op.dev.nnz;
+        if (op.dev.val != op.val.as<double>()) {
+            CK(c, op.val.ensure(sizeof(double) * (size_t)std::max<int64_t>(ne, 1)));
+            op.dev.val = op.val.as<double>();
+            drop_graph(c);
+        }
+        for (int64_t q = 0; q < count; ++q) {
+            const int64_t o = batch ? off[(size_t)q] : 0;
+            const int64_t n = batch ? off[(size_t)q + 1] - o : ne;
+            if (n > 0) {
+                if (!src[q]) return set_err(c, DBD_ERR_INVALID, "null value array");
+                CK(c, cudaMemcpyAsync(op.val.as<double>() + o, src[q], sizeof(double) * (size_t)n, kind, c->stream));
+            }
+        }
+        return DBD_OK;
+    };
+    int rc = put(c->A, a_val, c->batchNnzA);
+    if (rc) return rc;
+    if (!c->b_is_a) {
+        rc = put(c->B, b_val, c->batchNnzB);
+        if (rc) return rc;
+    }
+    if (!c->numExec) {
+        // Capture the numeric kernels of every bin (their fork/join across the
+        // bin streams included) once; replays launch them with one call.
+        c->tused = c->sused = 0;
+        CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        c->capturing = true;
+        cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream);
+        numeric_rows(c, 0, c->m, 0, c->Ci.as<int32_t>(), c->Cv.as<double>());
+        c->capturing = false;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+        c->numGraph = g;
+        e = cudaGraphInstantiate(&c->numExec, g, 0);
+        if (e != cudaSuccess) {
+            drop_graph(c);
+            return cuda_fail(c, e, "cudaGraphInstantiate");
+        }
+    }
+    CK(c, cudaGraphLaunch(c->numExec, c->stream));
+    return check_device_err(c, "update values");
 }
 
 int dbd_spgemm_files(dbd_ctx *c, const char *path_a, const char *path_b, dbd_scope scope, const char *out_dir,

@@ -47,7 +47,7 @@ __global__ void k_row_minmax(CsrDev B, int32_t *__restrict__ bmin, int32_t *__re
 // row.
 __global__ void k_row_products(CsrDev A, const int32_t *__restrict__ Bp, const int32_t *__restrict__ bmin,
                                const int32_t *__restrict__ bmax, RowInfo ri, uint8_t *__restrict__ symBin,
-                               int *err) {
+                               int *err, Tuning tune) {
     const int lane = threadIdx.x & 31;
     const int sub = lane & 7;
     const unsigned gmask = 0xffu << (lane & 24);
@@ -73,7 +73,7 @@ __global__ void k_row_products(CsrDev A, const int32_t *__restrict__ Bp, const i
             ri.rowP[row] = sum;
             ri.lo[row] = lo;
             ri.hi[row] = hi;
-            symBin[row] = sym_bin_of(sum, e - s, span_words(lo, hi));
+            symBin[row] = sym_bin_of(sum, e - s, span_words(lo, hi), tune);
             if (sum > 0x7fffffffLL) atomicCAS(err, 0, (int)DEV_ROW_TOO_LONG);
         }
     }
@@ -99,10 +99,10 @@ __global__ void k_block_products(int64_t m, const int64_t *__restrict__ rowP,
 }
 
 __global__ void k_num_bins(int64_t m, const int32_t *__restrict__ Ap, RowInfo ri,
-                           const int32_t *__restrict__ rowNnz, uint8_t *__restrict__ numBin) {
+                           const int32_t *__restrict__ rowNnz, uint8_t *__restrict__ numBin, Tuning tune) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m;
          r += (int64_t)gridDim.x * blockDim.x)
-        numBin[r] = num_bin_of(ri.rowP[r], Ap[r + 1] - Ap[r], rowNnz[r], span_words(ri.lo[r], ri.hi[r]));
+        numBin[r] = num_bin_of(ri.rowP[r], Ap[r + 1] - Ap[r], rowNnz[r], span_words(ri.lo[r], ri.hi[r]), tune);
 }
 
 // Per-tile (kTileRows rows) counts of each bin.
@@ -327,12 +327,13 @@ void launch_row_minmax(const CsrDev &B, int32_t *bmin, int32_t *bmax, cudaStream
 }
 
 void launch_row_products(const CsrDev &A, const int32_t *Bp, const int32_t *bmin, const int32_t *bmax,
-                         const RowInfo &ri, uint8_t *symBin, int *err, cudaStream_t s, int num_sms) {
+                         const RowInfo &ri, uint8_t *symBin, int *err, const Tuning &t, cudaStream_t s,
+                         int num_sms) {
     if (A.m == 0) return;
     const int threads = 256;
     const int64_t need = ceil_div(A.m * 8, threads);
     const int grid = (int)std::min<int64_t>(need, (int64_t)num_sms * 8);
-    k_row_products<<<grid, threads, 0, s>>>(A, Bp, bmin, bmax, ri, symBin, err);
+    k_row_products<<<grid, threads, 0, s>>>(A, Bp, bmin, bmax, ri, symBin, err, t);
 }
 
 void launch_block_products(int64_t m, const int64_t *rowP, int64_t rows_per_block, int64_t *blockP,
@@ -350,10 +351,10 @@ void launch_bin_lists(int64_t m, const Binning &b, int nbins, cudaStream_t s) {
 }
 
 void launch_num_bins(int64_t m, const int32_t *Ap, const RowInfo &ri, const int32_t *rowNnz,
-                     uint8_t *numBin, cudaStream_t s, int num_sms) {
+                     uint8_t *numBin, const Tuning &t, cudaStream_t s, int num_sms) {
     if (m == 0) return;
     const int grid = (int)std::min<int64_t>(ceil_div(m, 256), (int64_t)num_sms * 8);
-    k_num_bins<<<grid, 256, 0, s>>>(m, Ap, ri, rowNnz, numBin);
+    k_num_bins<<<grid, 256, 0, s>>>(m, Ap, ri, rowNnz, numBin, t);
 }
 
 void launch_row_scan(int64_t m, const int32_t *rowNnz, int64_t *part, int64_t *Cp, cudaStream_t s) {

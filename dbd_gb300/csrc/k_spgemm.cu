@@ -702,7 +702,7 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
     const int32_t cbase = rw0 << 5;
     const int32_t obc = cbase - col_shift(a, row);  // column written for bit 0
 
-    if (a.wideBits && sym_bin_of(a.rowP[row], e1 - e0, nwords) == SB_WIDE) {
+    if (a.wideBits && sym_bin_of(a.rowP[row], e1 - e0, nwords, a.tune) == SB_WIDE) {
         // The symbolic pass kept this row's bitmap.
         const uint32_t *src = a.wideBits + (size_t)a.wideSlot[row] * kRankWordsMax;
         for (int i = tid; i < nwords; i += THREADS) bits[i] = src[i];
@@ -1152,6 +1152,13 @@ void init_kernel_attributes() {
                          (int)kSmemRankLMax);
 }
 
+// Dynamic shared memory of the rank kernel: staging, bitmap and word ranks of
+// maxWords words, vcap shared values.
+static size_t smem_rank(int threads, int maxWords, int vcap) {
+    const size_t stage = threads == kRankSThreads ? StageLayout<kRankSThreads>::bytes : StageLayout<kRankLThreads>::bytes;
+    return stage + 8 * (size_t)maxWords + 8 * (size_t)vcap;
+}
+
 static int wide_window_bits(int64_t ncols) {
     int64_t w = 32;
     while (w < ncols && w < kWideWindowBitsMax) w <<= 1;
@@ -1210,10 +1217,12 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
             break;
         case NB_RANKS:
             k_num_rank<kRankSThreads, false>
-                <<<(unsigned)n, kRankSThreads, kSmemRankSMax, s>>>(a, lo, kRankWordsMax, kRankSVcap);
+                <<<(unsigned)n, kRankSThreads, smem_rank(kRankSThreads, a.tune.rankWordsMax, a.tune.rankSharedMax), s>>>(
+                    a, lo, a.tune.rankWordsMax, a.tune.rankSharedMax);
             break;
         case NB_RANKL:
-            k_num_rank<kRankLThreads, true><<<(unsigned)n, kRankLThreads, kSmemRankLMax, s>>>(a, lo, kRankWordsMax, 0);
+            k_num_rank<kRankLThreads, true><<<(unsigned)n, kRankLThreads, smem_rank(kRankLThreads, a.tune.rankWordsMax, 0),
+                                             s>>>(a, lo, a.tune.rankWordsMax, 0);
             break;
         case NB_HCTA_S:
             k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable><<<(unsigned)n, kNumCtaSThreads, kSmemNumCtaS, s>>>(a, lo);

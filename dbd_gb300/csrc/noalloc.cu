@@ -196,7 +196,7 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     launch_check_sorted(B, flags + 3, s, sms);
     launch_row_minmax(B, bmin, bmax, s, sms);
     // Analysis: products per row, symbolic bins, row lists.
-    launch_row_products(A, B.ptr, bmin, bmax, ri, symBin, flags, s, sms);
+    launch_row_products(A, B.ptr, bmin, bmax, ri, symBin, flags, Tuning{}, s, sms);
     Binning sb{symBin, symList, hist, symTileOff, symStart};
     launch_bin_lists(m, sb, SB_COUNT, s);
     int32_t symStart_h[kMaxBins + 1];
@@ -220,7 +220,7 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     for (int bin = SB_TINY; bin < SB_COUNT; ++bin)
         launch_symbolic_bin(sa, bin, symStart_h[bin], symStart_h[bin + 1] - symStart_h[bin], s, &launches);
     launch_row_scan(m, rowNnz, part, c_row_ptr, s);
-    launch_num_bins(m, A.ptr, ri, rowNnz, numBin, s, sms);
+    launch_num_bins(m, A.ptr, ri, rowNnz, numBin, Tuning{}, s, sms);
     Binning nb{numBin, numList, hist, numTileOff, numStart};
     launch_bin_lists(m, nb, NB_COUNT, s);
     int64_t nnz = 0;

@@ -278,6 +278,65 @@ int dbd_spgemm_batched(dbd_ctx *ctx, int64_t count, const dbd_csr_view *a, const
                        dbd_scope scope, int64_t *c_row_off, int64_t *c_nnz_off, dbd_csr_out *c,
                        dbd_stats *st);
 
+/* ---- tuning (no reference counterpart) ------------------------------------ */
+
+/* Row-bin thresholds of the categoriser: which kernel (and so which table
+ * size and how many threads) each row of C gets.  The reference fixes its
+ * block categories at compile time (distributeWorkload.cpp:249-270); these
+ * are runtime knobs, each capped by the size of the tables it selects:
+ *   warp_span_words        rows whose column window spans at most this many
+ *                          32-column words use the one-warp bitmap kernels (1..64)
+ *   warp_max_nnz           numeric rows with at most this many entries stay
+ *                          on one warp (1..256)
+ *   sym_warp_max_products  symbolic rows with at most this many products use a
+ *                          one-warp hash table (32..512)
+ *   rank_words_max         CTA rank kernels take windows up to this many words;
+ *                          wider rows use CTA hash tables or dense windows (1..8192)
+ *   rank_shared_max_nnz    rank rows up to this size accumulate in shared
+ *                          memory, larger ones in place in C (1..4096)
+ *   sym_hash_span_words    symbolic rows with at most 4096 products hash
+ *                          (instead of a bitmap) above this span (>= 0) */
+typedef struct {
+    int32_t warp_span_words;
+    int32_t warp_max_nnz;
+    int32_t sym_warp_max_products;
+    int32_t rank_words_max;
+    int32_t rank_shared_max_nnz;
+    int32_t sym_hash_span_words;
+} dbd_tuning;
+
+int dbd_get_tuning(const dbd_ctx *ctx, dbd_tuning *t);
+/* Values outside the ranges above return DBD_ERR_INVALID. */
+int dbd_set_tuning(dbd_ctx *ctx, const dbd_tuning *t);
+
+/* Autotuner: times the multiply of the operands currently loaded on the
+ * context (after dbd_load_a/b, dbd_spgemm or dbd_spgemm_batched) in the
+ * kernel scope under candidate thresholds, one knob at a time (coordinate
+ * descent, best of `repeats` runs per candidate), and keeps the fastest
+ * setting on the context.  *best and *best_ms (either may be NULL) receive it
+ * and its time.  The context's product afterwards is that of the last trial
+ * (the same C as any other setting gives). */
+int dbd_autotune(dbd_ctx *ctx, int repeats, dbd_tuning *best, double *best_ms);
+
+/* ---- new values on the same patterns (no reference counterpart) ----------- */
+
+/* Recomputes C's values for new values of A and B on the patterns of the last
+ * multiply on this context, which must have run in DBD_SCOPE_KERNEL with C
+ * resident (dbd_spgemm or dbd_spgemm_batched).  Only the numeric kernels run:
+ * the first call captures them (every bin, across the bin streams) into a
+ * CUDA graph, later calls copy the values and replay it with one launch.  C's
+ * structure and the plan stay as they were; C's values are overwritten in
+ * place (dbd_result gives them).
+ *
+ * count: 1 after dbd_spgemm, the pair count after dbd_spgemm_batched.
+ * a_val[q]: nnz(A_q) values in A_q's entry order; b_val[q] likewise for B_q
+ * (b_val is ignored when the last multiply squared A).  on_device: the value
+ * arrays are device (1) or host (0) memory.  Device operands of the last
+ * multiply must still hold their row pointers and column indices.  A new
+ * multiply, dbd_load_a/b or dbd_spgemm_adjoint's reload drops the graph. */
+int dbd_update_values(dbd_ctx *ctx, int64_t count, const double *const *a_val, const double *const *b_val,
+                      int on_device);
+
 /* ---- allocation-free multiply --------------------------------------------- */
 
 /* Bytes of device scratch that dbd_spgemm_noalloc owns per GPU. */
