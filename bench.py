@@ -40,6 +40,8 @@ WORKLOADS = {
                "FP64 values 1-U[0,1), blocksize 4096", 4096),
     "laplacian256": ("A*A, A = 5-point Laplacian on a 256x256 grid (n=65,536), FP64 values 4/-1, blocksize 4096",
                      4096),
+    "rmat21": ("out-of-core A*A, A = R-MAT scale 21 (n=2,097,152), edge factor 16, (a,b,c,d)=(.57,.19,.19,.05), "
+               "seed 0, FP64 values 1-U[0,1), blocksize 512, GPU budget 24 GiB, host budget 64 GiB", 512),
 }
 
 
@@ -61,12 +63,20 @@ def row_products(A):
     return cs[A.row_ptr[1:]] - cs[A.row_ptr[:-1]]
 
 
-def thresholds():
-    """Bin thresholds of the library (dbd_internal.h), for per-kernel byte counts."""
+def thresholds(tuning=None):
+    """Bin thresholds of the library: the fixed table sizes of dbd_internal.h
+    and the runtime knobs of a context (dbd_tuning; defaults when None)."""
     text = open(os.path.join(ROOT, "dbd_gb300", "csrc", "dbd_internal.h")).read()
     names = ["kTinyMax", "kSymWarpMax", "kSymCtaMax", "kNumWarpMax", "kNumCtaSMax", "kNumCtaLMax",
-             "kWarpSpanWords", "kRankWordsMax", "kWideHashSpanWords"]
-    return {n: int(re.search(rf"\b{n}\s*=\s*(\d+)", text).group(1)) for n in names}
+             "kWarpSpanWords", "kRankWordsMax", "kWideHashSpanWords", "kDenseWarpWords"]
+    t = {n: int(re.search(rf"\b{n}\s*=\s*(\d+)", text).group(1)) for n in names}
+    if tuning:
+        t.update(kWarpSpanWords=tuning["warp_span_words"], kNumWarpMax=tuning["warp_max_nnz"],
+                 kSymWarpMax=tuning["sym_warp_max_products"], kRankWordsMax=tuning["rank_words_max"],
+                 kRankSharedMax=tuning["rank_shared_max_nnz"], kWideHashSpanWords=tuning["sym_hash_span_words"],
+                 kDenseWarpWords=tuning["dense_warp_span_words"])
+    t.setdefault("kRankSharedMax", t["kNumCtaLMax"])
+    return t
 
 
 def span_words(A, B=None, col_off=0):
@@ -89,25 +99,26 @@ def span_words(A, B=None, col_off=0):
     return np.where(ok, ((hi + col_off) >> 5) - ((np.where(ok, lo, 0) + col_off) >> 5) + 1, 0)
 
 
-def bins(A, rowP, nnz_r, sw):
+def bins(A, rowP, nnz_r, sw, tuning=None):
     """Symbolic and numeric bin of every row (the rules of dbd_internal.h)."""
-    t = thresholds()
+    t = thresholds(tuning)
     nA = np.diff(A.row_ptr)
     tiny = (rowP <= t["kTinyMax"]) & (nA <= 32)
     sym = np.select([rowP == 0, tiny, sw <= t["kWarpSpanWords"], rowP <= t["kSymWarpMax"],
                      (rowP <= t["kSymCtaMax"]) & (sw > t["kWideHashSpanWords"])], [0, 1, 2, 3, 4], 5)
-    num = np.select([nnz_r == 0, tiny, (sw <= t["kWarpSpanWords"]) & (nnz_r <= t["kNumWarpMax"]),
-                     nnz_r <= t["kNumWarpMax"], (sw <= t["kRankWordsMax"]) & (nnz_r <= t["kNumCtaLMax"]),
+    num = np.select([nnz_r == 0, tiny, sw <= t["kDenseWarpWords"],
+                     (sw <= t["kWarpSpanWords"]) & (nnz_r <= t["kNumWarpMax"]),
+                     nnz_r <= t["kNumWarpMax"], (sw <= t["kRankWordsMax"]) & (nnz_r <= t["kRankSharedMax"]),
                      sw <= t["kRankWordsMax"], nnz_r <= t["kNumCtaSMax"], nnz_r <= t["kNumCtaLMax"]],
-                    [0, 1, 2, 3, 4, 5, 6, 7], 8)
+                    [0, 1, 9, 2, 3, 4, 5, 6, 7], 8)
     return sym, num
 
 
-SYM_NAMES = {1: "k_sym_tiny", 2: "k_sym_bitw<8>", 3: "k_sym_hash_warp<8,1024>", 4: "k_sym_hash_cta<256,8192>",
+SYM_NAMES = {1: "k_sym_tiny", 2: "k_sym_flagw<8>", 3: "k_sym_hash_warp<8,1024>", 4: "k_sym_hash_cta<256,8192>",
              5: "k_sym_wide<512>"}
 NUM_NAMES = {1: "k_num_tiny", 2: "k_num_rankw<8>", 3: "k_num_hash_warp<4,512>", 4: "k_num_rank<256,shared>",
              5: "k_num_rank<512,in-place>", 6: "k_num_hash_cta<256,2048>", 7: "k_num_hash_cta<512,8192>",
-             8: "k_num_dense<512,8192>"}
+             8: "k_num_dense<512,8192>", 9: "k_num_densew<8>"}
 
 
 def kernel_bytes(A, rowP, nnz_r, sym, num):
@@ -122,6 +133,65 @@ def kernel_bytes(A, rowP, nnz_r, sym, num):
     for b, name in NUM_NAMES.items():
         m = num == b
         out[("num", b)] = (name, int(12 * nA[m].sum() + 12 * rowP[m].sum() + 12 * nnz_r[m].sum() + 8 * m.sum()))
+    return out
+
+
+def fp64_flops(rowP, num):
+    """FP64 flops per launch of each numeric kernel family: one fused
+    multiply-add (2 flops) per intermediate product of its rows."""
+    return {("num", b): int(2 * rowP[num == b].sum()) for b in NUM_NAMES}
+
+
+_FP64_PEAK = None
+
+
+def fp64_peak(torch, dev):
+    """Measured FP64 throughput of this GPU (TFLOP/s): cuBLAS DGEMM of 4096^2
+    operands through torch.mm, best of 3 after a warm-up."""
+    global _FP64_PEAK
+    if _FP64_PEAK is None:
+        n = 4096
+        a = torch.randn(n, n, dtype=torch.float64, device=dev)
+        b = torch.randn(n, n, dtype=torch.float64, device=dev)
+        torch.mm(a, b)
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.mm(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 1e3
+            best = t if best is None else min(best, t)
+        _FP64_PEAK = 2.0 * n ** 3 / best / 1e12
+        del a, b
+    return _FP64_PEAK
+
+
+def roofline(ktime, kb, flops, torch, dev):
+    """Roofline of the dominant kernel family (largest time per step): its
+    algorithmic bytes against the measured HBM copy bandwidth and its FP64
+    flops against the measured FP64 rate; the larger fraction names the
+    bound."""
+    dom = max(ktime, key=ktime.get)
+    ms = ktime[dom]
+    name, nbytes = kb[dom]
+    nflops = flops.get(dom, 0)
+    peak, peak_kind = peaks()
+    fpk = fp64_peak(torch, dev)
+    gbs = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+    tfs = nflops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
+    hbm = {"achieved": round(gbs, 2), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
+           "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_launch": nbytes}
+    fp = {"achieved": round(tfs, 4), "peak": round(fpk, 4), "unit": "TFLOP/s", "frac": round(tfs / fpk, 4),
+          "peak_kind": "of measured (cuBLAS DGEMM 4096^3 via torch.mm)", "fp64_flops_per_launch": nflops}
+    main = fp if fp["frac"] > hbm["frac"] else hbm
+    out = {"bound": "fp64" if main is fp else "hbm", "kernel": name, "launch_ms": round(ms, 4)}
+    out.update({k: main[k] for k in ("achieved", "peak", "unit", "frac", "peak_kind")})
+    out["hbm"] = hbm
+    out["fp64"] = fp
+    out["kernel_ms_per_step"] = {kb[k][0]: round(v, 4) for k, v in sorted(ktime.items(), key=lambda x: -x[1]) if v}
     return out
 
 
@@ -322,9 +392,13 @@ def run_batched(args, local):
             ms.append(e0.elapsed_time(e1))
         return float(np.mean(ms)) / 1e3, out
 
+    batched = lambda: ctx.spgemm_batched(dA, dB, scope="kernel", fetch=False)
+    t_default, _ = timed(batched, max(1, min(args.steps, 3)), 1)
+    tuned = None
+    if not args.no_autotune:
+        tuned, _ = ctx.autotune(repeats=1)
     with Clocks(local) as clk:
-        t_batch, res = timed(lambda: ctx.spgemm_batched(dA, dB, scope="kernel", fetch=False), args.steps,
-                             args.warmup)
+        t_batch, res = timed(batched, args.steps, args.warmup)
     launches = int(res.stats["gpu_launches"])
     nnzC = int(res.stats["nnz_c"])
     # Roofline of the dominant kernel family of the batched multiply.
@@ -333,12 +407,15 @@ def run_batched(args, local):
     nnz_r = np.diff(Cp)
     Acat = CSR(len(rowP), col_off, np.concatenate([[0], np.cumsum(np.concatenate(nA_all))]), None, None)
     Acat.col_idx = np.zeros(0, np.int32)
-    sym, num = bins(Acat, rowP, nnz_r, np.concatenate(sw_all))
+    sym, num = bins(Acat, rowP, nnz_r, np.concatenate(sw_all), ctx.tuning)
+    bins_match = bool(np.array_equal(np.bincount(num, minlength=12)[:12], np.array(res.stats["rows_per_bin"])))
     kb = kernel_bytes(Acat, rowP, nnz_r, sym, num)
     # Per-kernel times: the same batched multiply on a context that times
     # every kernel family, the bins one after another.
     pctx = dbd.Context(cpu_gib=96, gpu_gib=200, rows_per_block=4096, device=local, time_kernels=True)
     pctx.set_stream(stream.cuda_stream)
+    if tuned:
+        pctx.set_tuning(**tuned)
     pctx.spgemm_batched(dA, dB, scope="kernel", fetch=False)
     flush.zero_()
     st = pctx.spgemm_batched(dA, dB, scope="kernel", fetch=False).stats
@@ -346,11 +423,16 @@ def run_batched(args, local):
     pctx.close()
     ktime = {("num", b): st["t_num_bin_ms"][b] for b in NUM_NAMES}
     ktime.update({("sym", b): st["t_sym_bin_ms"][b] for b in SYM_NAMES})
-    dom = max(ktime, key=ktime.get)
-    dom_ms = ktime[dom]
-    dom_name, dom_bytes = kb[dom]
-    peak, peak_kind = peaks()
-    achieved = dom_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    roof = roofline(ktime, kb, fp64_flops(rowP, num), torch, dev)
+    roof["traffic"] = None
+    roof["bins_match_library"] = bins_match
+
+    # New values on the same patterns: the captured numeric graph replayed.
+    batched()
+    rng = np.random.default_rng(1)
+    newA = [torch.from_numpy(rng.uniform(-1.0, 1.0, A.nnz)).to(dev) for A in As]
+    newB = [torch.from_numpy(rng.uniform(-1.0, 1.0, B.nnz)).to(dev) for B in Bs]
+    t_update, _ = timed(lambda: ctx.update_values(newA, newB), args.steps, args.warmup)
 
     def sequential():
         for q in range(count):
@@ -376,6 +458,7 @@ def run_batched(args, local):
     rows_in = sum(A.n_rows + B.n_rows + 2 for A, B in zip(As, Bs))
     h2d = 12 * nnz_in + 4 * rows_in
     d2h = 12 * nnzC + 8 * (len(rowP) + 1)
+    ctx_tuning = ctx.tuning
     ctx.close()
     g = lambda t: round(2.0 * P / t / 1e9, 4)
     line = {"metric": METRIC, "value": g(t_batch), "unit": "GFLOPS", "n_gpus": 1, "steps": args.steps,
@@ -388,14 +471,14 @@ def run_batched(args, local):
                        "rows": int(len(rowP)), "nnz_a": int(sum(A.nnz for A in As)),
                        "nnz_b": int(sum(B.nnz for B in Bs)), "products": P, "nnz_c": nnzC,
                        "scope": "kernel (pairs resident in HBM, C left in HBM)",
-                       "l2": "flushed between steps (512 MiB device write outside the timed events)"},
+                       "l2": "flushed between steps (512 MiB device write outside the timed events)",
+                       "tuning": ctx_tuning, "autotuned": tuned is not None,
+                       "default_tuning_ms": round(t_default * 1e3, 3)},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 2), "peak": peak,
-                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
-                         "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_launch": dom_bytes,
-                         "launch_ms": round(dom_ms, 4),
-                         "kernel_ms_per_step": {kb[k][0]: round(v, 4) for k, v in
-                                                sorted(ktime.items(), key=lambda x: -x[1]) if v}},
+            "roofline": roof,
+            "update_values": {"gflops": g(t_update), "ms": round(t_update * 1e3, 3),
+                              "what": "dbd_update_values: new device values for every pair, the captured "
+                                      "CUDA graph of the numeric kernels replayed (C's values recomputed)"},
             "sequential": {"gflops": g(t_seq), "ms": round(t_seq * 1e3, 3),
                            "what": "512 plain dbd_spgemm calls (kernel scope) on the same device-resident pairs"},
             "batched_vs_sequential": round(t_seq / t_batch, 3),
@@ -403,6 +486,210 @@ def run_batched(args, local):
                     "ms_per_step": round(te * 1e3, 3),
                     "scope": "+D2H through dbd_spgemm_batched with pinned host pairs and pinned host C",
                     "sequential_gflops": g(te_seq), "sequential_ms": round(te_seq * 1e3, 3)},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_adjoint(args, local):
+    """Forward + adjoint of C = A*B, A and B 100,000 x 100,000 with 16
+    uniform columns per row and N(0,1) values, loss = sum(W * C) with W ~
+    N(0,1) on C's pattern: dbd_spgemm (kernel scope) and dbd_spgemm_adjoint
+    (dA = mask_A(W B^T), dB = mask_B(A^T W)) on device-resident operands."""
+    import ctypes as C_
+    import torch
+    import dbd_gb300 as dbd
+    from dbd_gb300 import generators as gen
+    from dbd_gb300.csr import CSR
+    n = 100_000
+    A = gen.uniform_rows(n, 16, seed=31)
+    B = gen.uniform_rows(n, 16, seed=32)
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(local)
+    tA = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (A.row_ptr, A.col_idx, A.val)]
+    tB = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (B.row_ptr, B.col_idx, B.val)]
+    dA = CSR.from_device(n, n, A.nnz, *[t.data_ptr() for t in tA])
+    dB = CSR.from_device(n, n, B.nnz, *[t.data_ptr() for t in tB])
+    lens = np.diff(B.row_ptr).astype(np.int64)
+    P = int(lens[A.col_idx].sum())
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    ctx = dbd.Context(cpu_gib=32, gpu_gib=64, device=local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+            flush.zero_()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            flush.zero_()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.mean(ms)) / 1e3
+
+    tuned = None
+    ctx.spgemm(dA, dB, scope="kernel", fetch=False)
+    if not args.no_autotune:
+        tuned, _ = ctx.autotune(repeats=2)
+    with Clocks(local) as clk:
+        t_fwd = timed(lambda: ctx.spgemm(dA, dB, scope="kernel", fetch=False), args.steps, args.warmup)
+    nnzC = int(ctx.stats()["nnz_c"])
+    launches = int(ctx.stats()["gpu_launches"])
+    rng = np.random.default_rng(3)
+    W = torch.from_numpy(rng.standard_normal(nnzC)).to(dev)
+    gA = torch.empty(A.nnz, dtype=torch.float64, device=dev)
+    gB = torch.empty(B.nnz, dtype=torch.float64, device=dev)
+    va, _ = dA.view()
+    vb, _ = dB.view()
+
+    def adjoint():
+        dbd._check(ctx._lib.dbd_spgemm_adjoint(ctx.handle, C_.byref(va), C_.byref(vb), C_.c_void_p(W.data_ptr()),
+                                               C_.c_void_p(gA.data_ptr()), C_.c_void_p(gB.data_ptr()), 1, 0),
+                   ctx.handle)
+    t_adj = timed(adjoint, args.steps, args.warmup)
+    # New values on the same patterns: the numeric graph replayed.
+    ctx.spgemm(dA, dB, scope="kernel", fetch=False)
+    nA = torch.from_numpy(rng.standard_normal(A.nnz)).to(dev)
+    nB = torch.from_numpy(rng.standard_normal(B.nnz)).to(dev)
+    t_replay = timed(lambda: ctx.update_values(nA, nB), args.steps, args.warmup)
+    # e2e: host operands, C back to the host (+D2H), then the adjoint with
+    # host W and host gradients.
+    ctx.set_stream(None)
+    Wh = W.cpu().numpy()
+    gAh = np.empty(A.nnz)
+    gBh = np.empty(B.nnz)
+    ha, ka = A.view()
+    hb, kb = B.view()
+    hCp = torch.empty(n + 1, dtype=torch.int64, pin_memory=True)
+    hCi = torch.empty(nnzC, dtype=torch.int32, pin_memory=True)
+    hCv = torch.empty(nnzC, dtype=torch.float64, pin_memory=True)
+    te = []
+    for i in range(max(1, args.e2e_steps) + 1):
+        t0 = time.perf_counter()
+        ctx.spgemm(A, B, scope="kernel", fetch=False)
+        dbd._check(ctx._lib.dbd_result_copy(ctx.handle, hCp.data_ptr(), hCi.data_ptr(), hCv.data_ptr()),
+                   ctx.handle)
+        dbd._check(ctx._lib.dbd_spgemm_adjoint(ctx.handle, C_.byref(ha), C_.byref(hb), Wh.ctypes.data,
+                                               gAh.ctypes.data, gBh.ctypes.data, 0, 0), ctx.handle)
+        if i:
+            te.append(time.perf_counter() - t0)
+    te = float(np.mean(te))
+    ctx_tuning = ctx.tuning
+    ctx.close()
+    g = lambda work, t: round(work / t / 1e9, 4)
+    peak, peak_kind = peaks()
+    fpk = fp64_peak(torch, dev)
+    adj_bytes = 12 * P + 12 * nnzC + 20 * A.nnz + 20 * B.nnz
+    line = {"metric": METRIC, "value": g(2 * P, t_fwd), "unit": "GFLOPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t_fwd * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded uniform rows, numpy PCG64)",
+            "config": {"workload": "forward + adjoint: C = A*B, A and B 100,000 x 100,000 with 16 uniform "
+                       "columns per row, N(0,1) values; loss = sum(W * C), W ~ N(0,1) on C's pattern",
+                       "products": P, "nnz_c": nnzC, "scope": "kernel (operands resident in HBM)",
+                       "l2": "flushed between steps (512 MiB device write outside the timed events)",
+                       "tuning": ctx_tuning, "autotuned": tuned is not None},
+            "gpu_launches": launches,
+            "adjoint": {"gflops": g(4 * P, t_adj), "ms": round(t_adj * 1e3, 3),
+                        "what": "dbd_spgemm_adjoint on the kept pattern: dA and dB, 2 multiply-adds per product",
+                        "roofline": {"algorithmic_bytes": adj_bytes,
+                                     "achieved": round(adj_bytes / t_adj / 1e9, 2), "peak": peak,
+                                     "frac": round(adj_bytes / t_adj / 1e9 / peak, 4),
+                                     "peak_kind": f"of {peak_kind}",
+                                     "fp64_tflops": round(4 * P / t_adj / 1e12, 4), "fp64_peak": round(fpk, 4),
+                                     "fp64_frac": round(4 * P / t_adj / 1e12 / fpk, 4)}},
+            "forward_plus_adjoint": {"ms": round((t_fwd + t_adj) * 1e3, 3),
+                                     "gflops": g(6 * P, t_fwd + t_adj),
+                                     "adjoint_over_forward_time": round(t_adj / t_fwd, 3)},
+            "forward_replay": {"gflops": g(2 * P, t_replay), "ms": round(t_replay * 1e3, 3),
+                               "what": "dbd_update_values (numeric graph replay, same patterns)"},
+            "e2e": {"value": g(2 * P, te), "unit": "GFLOPS", "h2d_bytes_per_step": 12 * (A.nnz + B.nnz) +
+                    4 * (2 * n + 2) + 8 * nnzC, "d2h_bytes_per_step": 12 * nnzC + 8 * (n + 1) + 8 * (A.nnz + B.nnz),
+                    "ms_per_step": round(te * 1e3, 3),
+                    "scope": "dbd_spgemm with host operands, C copied to pinned host memory, then "
+                             "dbd_spgemm_adjoint with host W and host gradients on the kept pattern; "
+                             "value = 2P / that time"},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_outofcore(args, local):
+    """Out-of-core A*A, A = R-MAT scale 21, edge factor 16, blocks of 512 rows,
+    GPU budget 24 GiB and host budget 64 GiB: C (billions of entries) streams
+    through the device output ring (kernel scope), pinned D2H (+D2H scope)
+    and the writer thread (+I/O scope, files wrapping when the disk is
+    smaller than C)."""
+    import torch
+    import dbd_gb300 as dbd
+    from dbd_gb300 import generators as gen
+    from dbd_gb300.csr import CSR
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    A = gen.rmat(21, 16, seed=0)
+    t_gen = time.perf_counter() - t0
+    rowP = row_products(A)
+    P = int(rowP.sum())
+    t = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (A.row_ptr, A.col_idx, A.val)]
+    D = CSR.from_device(A.n_rows, A.n_cols, A.nnz, *[x.data_ptr() for x in t])
+    free = shutil.disk_usage(ROOT).free
+    rotate = max(1.0, min(16.0, free / 4 / 2**30))
+    ctx = dbd.Context(cpu_gib=64, gpu_gib=24, rows_per_block=512, device=local, io_rotate_gib=rotate)
+    out = {}
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    with Clocks(local) as clk:
+        for _ in range(args.warmup):
+            ctx.spgemm(D, scope="kernel", fetch=False)
+            flush.zero_()
+        ts = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            r = ctx.spgemm(D, scope="kernel", fetch=False)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - a)
+            flush.zero_()
+        out["kernel"] = (float(np.mean(ts)), r.stats)
+        ctx.spgemm(A, scope="d2h", fetch=False)
+        a = time.perf_counter()
+        r = ctx.spgemm(A, scope="d2h", fetch=False)
+        out["d2h"] = (time.perf_counter() - a, r.stats)
+    tmp = tempfile.mkdtemp(prefix="dbd_io_", dir=ROOT)
+    try:
+        a = time.perf_counter()
+        r = ctx.spgemm(A, scope="io", out_dir=tmp, fetch=False)
+        out["io"] = (time.perf_counter() - a, r.stats)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    ctx.close()
+    st = out["kernel"][1]
+    nnzC = int(st["nnz_c"])
+    g = lambda x: round(2.0 * P / x / 1e9, 4)
+    line = {"metric": METRIC, "value": g(out["kernel"][0]), "unit": "GFLOPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(out["kernel"][0] * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded R-MAT, numpy PCG64)",
+            "config": {"workload": WORKLOADS["rmat21"][0], "n": A.n_rows, "nnz": A.nnz, "products": P,
+                       "nnz_c": nnzC, "c_bytes": 12 * nnzC + 8 * (A.n_rows + 1), "gpu_gib": 24, "host_gib": 64,
+                       "rows_per_block": 512, "n_chunks": int(st["n_chunks"]), "io_rotate_gib": round(rotate, 2),
+                       "generate_s": round(t_gen, 1),
+                       "scope": "kernel: C streamed through the device ring (no D2H), inputs resident in HBM"},
+            "gpu_launches": int(st["gpu_launches"]),
+            "scopes": {"kernel_gflops": g(out["kernel"][0]), "kernel_s": round(out["kernel"][0], 3),
+                       "d2h_gflops": g(out["d2h"][0]), "d2h_s": round(out["d2h"][0], 3),
+                       "d2h_bytes": int(out["d2h"][1]["bytes_d2h"]),
+                       "io_gflops": g(out["io"][0]), "io_s": round(out["io"][0], 3),
+                       "io_bytes": int(out["io"][1]["bytes_written"]),
+                       "io_fsync_s": round(out["io"][1]["t_fsync"], 3)},
+            "e2e": {"value": g(out["d2h"][0]), "unit": "GFLOPS", "h2d_bytes_per_step": 12 * A.nnz + 4 * (A.n_rows + 1),
+                    "d2h_bytes_per_step": int(out["d2h"][1]["bytes_d2h"]),
+                    "scope": "+D2H through dbd_spgemm with host A; C through the 64 GiB pinned host ring"},
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0
@@ -418,6 +705,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-io", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -430,6 +718,14 @@ def main():
         if rank != 0:
             return 0
         return run_batched(args, local)
+    if args.workload == "rmat21":
+        if rank != 0:
+            return 0
+        return run_outofcore(args, local)
+    if args.workload == "adjoint100k":
+        if rank != 0:
+            return 0
+        return run_adjoint(args, local)
 
     import torch
     import dbd_gb300 as dbd
@@ -462,6 +758,9 @@ def main():
         c.divide_Blocks()
         return c.distribute_Workload("kernel")
 
+    tuned = None
+    if not args.no_autotune:
+        tuned, tune_ms = ctx.autotune(repeats=2)
     for _ in range(args.warmup):
         step()
         flush.zero_()
@@ -499,12 +798,15 @@ def main():
     Cp = np.empty(A.n_rows + 1, np.int64)
     ctx._lib.dbd_result_copy(ctx.handle, Cp.ctypes.data, None, None)
     nnz_r = np.diff(Cp)
-    sym, num = bins(A, rowP, nnz_r, span_words(A))
+    sym, num = bins(A, rowP, nnz_r, span_words(A), ctx.tuning)
+    bins_match = bool(np.array_equal(np.bincount(num, minlength=12)[:12], np.array(stats[-1]["rows_per_bin"])))
     kb = kernel_bytes(A, rowP, nnz_r, sym, num)
     pctx = dbd.Context(cpu_gib=96, gpu_gib=200, rows_per_block=rpb, device=local, time_kernels=True)
     pctx.set_stream(stream.cuda_stream)
     pctx.initialize_A(D)
     pctx.initialize_B(D)
+    if tuned:
+        pctx.set_tuning(**tuned)
     pstats = []
     for i in range(args.warmup + 3):
         st_i = step(pctx)
@@ -519,14 +821,15 @@ def main():
             ktime[("num", b)] = ktime.get(("num", b), 0.0) + s["t_num_bin_ms"][b]
         for b in SYM_NAMES:
             ktime[("sym", b)] = ktime.get(("sym", b), 0.0) + s["t_sym_bin_ms"][b]
-    dom = max(ktime, key=ktime.get)
-    dom_ms = ktime[dom] / len(pstats)
-    dom_name, dom_bytes = kb[dom]
-    peak, peak_kind = peaks()
-    achieved = dom_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
-    traffic = profiled_traffic().get((args.workload, dom_name))
+    ktime = {k: v / len(pstats) for k, v in ktime.items()}
+    roof = roofline(ktime, kb, fp64_flops(rowP, num), torch, dev)
+    roof["traffic"] = profiled_traffic().get((args.workload, roof["kernel"]))
+    roof["bins_match_library"] = bins_match
+    peak = roof["hbm"]["peak"]
     bytes_alg = 12 * P + 12 * A.nnz + 4 * (A.n_rows + 1) + 12 * nnzC + 8 * (A.n_rows + 1)
-    shares = {f"{kb[k][0]}": round(v / len(pstats), 4) for k, v in sorted(ktime.items(), key=lambda x: -x[1]) if v}
+    roof["pipeline"] = {"bytes_alg": bytes_alg, "achieved": round(bytes_alg / t_step / 1e9, 2),
+                        "frac": round(bytes_alg / t_step / 1e9 / peak, 4),
+                        "fp64_frac": round(2 * P / t_step / 1e12 / roof["fp64"]["peak"], 4)}
 
     line = {"metric": METRIC, "value": round(value, 4), "unit": "GFLOPS", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 4), "higher_is_better": True,
@@ -535,15 +838,10 @@ def main():
             "config": {"workload": desc, "n": A.n_rows, "nnz": A.nnz, "products": P, "nnz_c": nnzC,
                        "rows_per_block": rpb, "scope": "kernel (inputs resident in HBM, C left in HBM)",
                        "l2": "flushed between steps (512 MiB device write outside the timed events)",
-                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                       "tuning": ctx.tuning, "autotuned": tuned is not None},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 2), "peak": peak,
-                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "peak_kind": f"of {peak_kind}", "algorithmic_bytes_per_launch": dom_bytes,
-                         "launch_ms": round(dom_ms, 4),
-                         "pipeline": {"bytes_alg": bytes_alg, "achieved": round(bytes_alg / t_step / 1e9, 2),
-                                      "frac": round(bytes_alg / t_step / 1e9 / peak, 4)},
-                         "kernel_ms_per_step": shares},
+            "roofline": roof,
             "wall_s": round(t_wall, 3)}
     line["clocks"] = clk.summary()
 

@@ -25,7 +25,7 @@ struct CsrDev {
 // of every bin.
 enum SymBin : uint8_t { SB_EMPTY = 0, SB_TINY, SB_BITW, SB_HWARP, SB_HCTA, SB_WIDE, SB_COUNT };
 enum NumBin : uint8_t {
-    NB_EMPTY = 0, NB_TINY, NB_RANKW, NB_HWARP, NB_RANKS, NB_RANKL, NB_HCTA_S, NB_HCTA_L, NB_DENSE, NB_COUNT
+    NB_EMPTY = 0, NB_TINY, NB_RANKW, NB_HWARP, NB_RANKS, NB_RANKL, NB_HCTA_S, NB_HCTA_L, NB_DENSE, NB_DENSEW, NB_COUNT
 };
 constexpr int kMaxBins = 12;
 constexpr int kTileRows = 256;     // granularity of the per-bin offset tables
@@ -42,6 +42,7 @@ constexpr int kNumCtaLTable = 8192, kNumCtaLMax = 4096;
 constexpr int kDenseWindow = 8192;           // FP64 columns per dense window (64 KiB)
 constexpr int kWideWindowBitsMax = 1 << 20;  // symbolic bitmap window (128 KiB)
 constexpr int kWarpSpanWords = 64;           // warp-level bitmap rows: span <= 2048 columns
+constexpr int kDenseWarpWords = 16;          // warp dense-window rows: span <= 512 columns
 constexpr int kRankWordsMax = 8192;          // CTA rank rows: span <= 2^18 columns
 constexpr int kWideHashSpanWords = 2048;     // symbolic: P <= kSymCtaMax rows hash above this span
 
@@ -61,6 +62,7 @@ struct Tuning {
     int32_t rankWordsMax = kRankWordsMax;     // CTA rank kernels for windows up to this many words
     int32_t rankSharedMax = kNumCtaLMax;      // rank rows accumulating in shared memory
     int32_t symHashSpanWords = kWideHashSpanWords;  // symbolic CTA rows hash above this span
+    int32_t denseWarpWords = kDenseWarpWords; // numeric rows on one warp's dense window
 };
 
 __host__ __device__ __forceinline__ uint8_t sym_bin_of(int64_t P, int32_t nA, int sw, const Tuning &t) {
@@ -76,6 +78,7 @@ __host__ __device__ __forceinline__ uint8_t num_bin_of(int64_t P, int32_t nA, in
                                                        const Tuning &t) {
     if (nnz == 0) return NB_EMPTY;
     if (P <= kTinyMax && nA <= 32) return NB_TINY;
+    if (sw <= t.denseWarpWords) return NB_DENSEW;
     if (sw <= t.warpSpanWords && nnz <= t.numWarpMax) return NB_RANKW;
     if (nnz <= t.numWarpMax) return NB_HWARP;
     if (sw <= t.rankWordsMax) return nnz <= t.rankSharedMax ? NB_RANKS : NB_RANKL;
@@ -93,6 +96,7 @@ inline Tuning clamp_tuning(Tuning t) {
     t.rankWordsMax = cl(t.rankWordsMax, 1, kRankWordsMax);
     t.rankSharedMax = cl(t.rankSharedMax, 1, kNumCtaLMax);
     t.symHashSpanWords = cl(t.symHashSpanWords, 0, 1 << 26);
+    t.denseWarpWords = cl(t.denseWarpWords, 0, kDenseWarpWords);
     return t;
 }
 
@@ -144,6 +148,7 @@ struct SymArgs {
     int *err;
     const int32_t *rowLo = nullptr;  // per-row column window (RowInfo)
     const int32_t *rowHi = nullptr;
+    const int64_t *rowP = nullptr;   // per-row products (RowInfo)
     // Optional store of the wide rows' column bitmaps for the numeric rank
     // kernel (null: not kept): kRankWordsMax words per wide row (the row's
     // window from word lo/32 on), at the row's position in the wide bin;

@@ -494,6 +494,7 @@ int symbolic(dbd_ctx *c) {
     sa.ctr = nullptr;
     sa.err = c->err.as<int>();
     sa.rowLo = c->rowLo.as<int32_t>();
+    sa.rowP = c->rowP.as<int64_t>();
     sa.rowHi = c->rowHi.as<int32_t>();
     sa.tune = c->tune;
     // Keep the wide rows' column bitmaps (one slot of kRankWordsMax words per
@@ -573,7 +574,8 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     const int64_t t1 = (r1 >= c->m) ? c->ntiles : r1 / kTileRows;
     // Bins run concurrently, one stream each; heaviest first so that their
     // long CTAs start early.
-    static const int order[] = {NB_DENSE, NB_RANKL, NB_HCTA_L, NB_RANKS, NB_HCTA_S, NB_HWARP, NB_RANKW, NB_TINY};
+    static const int order[] = {NB_DENSE,  NB_RANKL, NB_HCTA_L, NB_RANKS, NB_HCTA_S,
+                                NB_HWARP, NB_RANKW, NB_DENSEW, NB_TINY};
     Fork fk(c);
     for (int b : order) {
         const int32_t lo = c->numTileOff_h[(size_t)t0 * kMaxBins + b];
@@ -1441,6 +1443,7 @@ int dbd_get_tuning(const dbd_ctx *c, dbd_tuning *t) {
     t->rank_words_max = c->tune.rankWordsMax;
     t->rank_shared_max_nnz = c->tune.rankSharedMax;
     t->sym_hash_span_words = c->tune.symHashSpanWords;
+    t->dense_warp_span_words = c->tune.denseWarpWords;
     return DBD_OK;
 }
 
@@ -1453,6 +1456,7 @@ int dbd_set_tuning(dbd_ctx *c, const dbd_tuning *t) {
     u.rankWordsMax = t->rank_words_max;
     u.rankSharedMax = t->rank_shared_max_nnz;
     u.symHashSpanWords = t->sym_hash_span_words;
+    u.denseWarpWords = t->dense_warp_span_words;
     const Tuning v = clamp_tuning(u);
     if (memcmp(&u, &v, sizeof(u)) != 0) return set_err(c, DBD_ERR_INVALID, "a tuning value is out of its range");
     c->tune = u;
@@ -1490,6 +1494,7 @@ int dbd_autotune(dbd_ctx *c, int repeats, dbd_tuning *best, double *best_ms) {
         {&Tuning::rankSharedMax, {512, 1024, 2048, 4096}},
         {&Tuning::symWarpMax, {128, 256, 512}},
         {&Tuning::symHashSpanWords, {512, 2048, 8192}},
+        {&Tuning::denseWarpWords, {0, 4, 8, 16}},
     };
     const Tuning start = c->tune;
     Tuning cur = start;

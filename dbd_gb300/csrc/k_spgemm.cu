@@ -27,9 +27,14 @@
 //                               skipped by their next column
 //
 // Structure is decided by index only (a column belongs to a row as soon as a
-// product lands on it).  Products are rounded to FP64 before accumulation
-// (__dmul_rn, no FMA contraction), so the tiny path reproduces the sequential
-// oracle bit for bit and the other paths differ only by summation order.
+// product lands on it).  GB300's FP64 pipe is narrow (about two FP64
+// instructions per SM per clock), so the numeric kernels spend one FP64
+// instruction per product: a fused multiply-add into the accumulator (plain,
+// or inside a compare-and-swap loop where lanes may collide), or a multiply
+// whose sum the L2 performs (global reductions).  The tiny path rounds each
+// product (__dmul_rn) and adds in the oracle's order, reproducing it bit for
+// bit; the other paths differ from it by summation order and by the fused
+// roundings, well inside the 1e-12 tolerance.
 #include "dbd_internal.h"
 
 #include <algorithm>
@@ -49,6 +54,18 @@ __device__ __forceinline__ uint32_t hslot(int32_t c, int shift) {
 }
 
 __device__ __forceinline__ void raise(int *err, int code) { atomicCAS(err, 0, code); }
+
+// *acc += a * b with one rounding, atomically (a compare-and-swap loop around
+// one DFMA; shared or global memory).
+__device__ __forceinline__ void atomic_fma(double *acc, double a, double b) {
+    unsigned long long *p = reinterpret_cast<unsigned long long *>(acc);
+    unsigned long long old = *reinterpret_cast<volatile unsigned long long *>(p), seen;
+    do {
+        seen = old;
+        old = atomicCAS(p, seen, (unsigned long long)__double_as_longlong(
+                                     __fma_rn(a, b, __longlong_as_double((long long)seen))));
+    } while (old != seen);
+}
 
 // A column's offset in its row's window: true when inside [0, limit), else
 // records DEV_OUT_OF_WINDOW (the window came from B's row ranges, so this
@@ -453,33 +470,80 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
     if (tid == 0) a.rowNnz[row] = cnt;
 }
 
+// Products of one row for one warp, calling f(j, av) for every product (B
+// position j, A value av) on the lane that owns it.  Row-wise (long B rows):
+// the A entries one after another, the lanes over the B row; f calls of one
+// A entry see distinct columns when B's rows are strictly ascending, and a
+// __syncwarp separates consecutive A entries.  Flattened (short B rows):
+// 32 products of up to 32 A entries per step (Chunk).
+template <class F>
+__device__ __forceinline__ void warp_products(const CsrDev &A, const CsrDev &B, int32_t e0, int32_t e1, bool rowwise,
+                                              int lane, F &&f) {
+    if (rowwise) {
+        for (int32_t eb = e0; eb < e1; eb += 32) {
+            int32_t bs = 0, len = 0;
+            double av = 0.0;
+            if (eb + lane < e1) {
+                const int32_t k = A.idx[eb + lane];
+                bs = B.ptr[k];
+                len = B.ptr[k + 1] - bs;
+                av = A.val[eb + lane];
+            }
+            const int n = min(32, e1 - eb);
+            for (int q = 0; q < n; ++q) {
+                const int32_t bq = __shfl_sync(FULL, bs, q);
+                const int32_t lq = __shfl_sync(FULL, len, q);
+                const double aq = __shfl_sync(FULL, av, q);
+                for (int32_t i = lane; i < lq; i += 32) f(bq + i, aq);
+                __syncwarp();
+            }
+        }
+    } else {
+        for (int32_t e = e0; e < e1; e += 32) {
+            const Chunk c = load_chunk(A, B, e, e1, lane);
+            for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+                const int32_t t = t0 + lane;
+                double av;
+                const int32_t j = chunk_pos(c, t, &av);
+                if (t < c.total) f(j, av);
+            }
+        }
+    }
+}
+
+// Average B row length from which a row is enumerated row-wise.
+constexpr int kRowwiseMinLen = 16;
+
 // Narrow rows (window of at most kWarpSpanWords words): one warp per row,
-// a bitmap of the window in shared memory.
+// one flag byte per column of the window in shared memory; the row's size is
+// the number of flags set.
 template <int ROWS>
-__global__ void __launch_bounds__(32 * ROWS) k_sym_bitw(SymArgs a, int32_t begin, int32_t count) {
-    __shared__ uint32_t bms[ROWS][kWarpSpanWords];
+__global__ void __launch_bounds__(32 * ROWS) k_sym_flagw(SymArgs a, int32_t begin, int32_t count) {
+    constexpr int kWords = kWarpSpanWords * 8;  // 32 flag bytes per window word
+    __shared__ uint32_t fls[ROWS][kWords];
     const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t item = (int64_t)blockIdx.x * ROWS + g;
     if (item >= count) return;
-    uint32_t *bm = bms[g];
+    uint32_t *fw = fls[g];
+    uint8_t *fb = reinterpret_cast<uint8_t *>(fw);
     const int32_t row = a.list[begin + item];
-    const int32_t base = (a.rowLo[row] >> 5) << 5;
-    for (int i = lane; i < kWarpSpanWords; i += 32) bm[i] = 0u;
+    const int32_t rlo = a.rowLo[row];
+    const int32_t base = (rlo >> 5) << 5;
+    const int sw = min(span_words(rlo, a.rowHi[row]), kWarpSpanWords);
+    const uint32_t nb = (uint32_t)sw * 32u;
+    for (int i = lane; i < sw * 8; i += 32) fw[i] = 0u;
     __syncwarp();
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
-    for (int32_t e = e0; e < e1; e += 32) {
-        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
-        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
-            const int32_t t = t0 + lane;
-            const int32_t j = chunk_pos(c, t, nullptr);
-            const uint32_t rel = t < c.total ? (uint32_t)(a.B.idx[j] - base) : 0u;
-            const bool v = t < c.total && in_window(rel, kWarpSpanWords * 32, a.err);
-            or_bits_runs(bm, v, rel);
-        }
-    }
+    const bool rowwise = a.rowP[row] >= (int64_t)kRowwiseMinLen * (e1 - e0);
+    int *err = a.err;
+    const int32_t *bidx = a.B.idx;
+    warp_products(a.A, a.B, e0, e1, rowwise, lane, [&](int32_t j, double) {
+        const uint32_t rel = (uint32_t)(bidx[j] - base);
+        if (in_window(rel, nb, err)) fb[rel] = 1;
+    });
     __syncwarp();
     int cnt = 0;
-    for (int i = lane; i < kWarpSpanWords; i += 32) cnt += __popc(bm[i]);
+    for (int i = lane; i < sw * 8; i += 32) cnt += __popc(fw[i]);
     cnt = warp_sum_i(cnt);
     if (lane == 0) a.rowNnz[row] = cnt;
 }
@@ -625,7 +689,7 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t 
             const int32_t j = chunk_pos(c, t, &av);
             if (t < c.total) {
                 const int s = hash_insert_slot<TABLE>(keys, a.B.idx[j], a.err);
-                if (s >= 0) atomicAdd(&vals[s], __dmul_rn(av, a.B.val[j]));
+                if (s >= 0) atomic_fma(&vals[s], av, a.B.val[j]);
             }
         }
     }
@@ -662,7 +726,7 @@ __global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo)
         warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
             if (v) {
                 const int s = hash_insert_slot<TABLE>(keys, a.B.idx[pos], a.err);
-                if (s >= 0) atomicAdd(&vals[s], __dmul_rn(av[e], a.B.val[pos]));
+                if (s >= 0) atomic_fma(&vals[s], av[e], a.B.val[pos]);
             }
         });
         __syncthreads();
@@ -797,13 +861,88 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
                     if (v && (uint32_t)c < (uint32_t)nwords * 32u) {
                         const int w = c >> 5;
                         const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u)) - s0;
-                        if (r >= 0 && r < ns) atomicAdd(&vals[r], __dmul_rn(av[e], a.B.val[pos]));
+                        if (r >= 0 && r < ns) atomic_fma(&vals[r], av[e], a.B.val[pos]);
                     }
                 });
                 __syncthreads();
             }
             for (int i = tid; i < ns; i += THREADS) a.Cv[obase + s0 + i] = vals[i];
             __syncthreads();
+        }
+    }
+}
+
+// Narrowest rows (window of at most kDenseWarpWords words): one warp per row
+// with a dense FP64 accumulator and a flag byte per column of the window in
+// shared memory.  Row-wise enumeration over strictly ascending B rows adds
+// each column's products in A's entry order with plain fused multiply-adds
+// (deterministic); otherwise atomic ones.  The flags give the columns in
+// order: no bitmap ranks, no sorting.
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_num_densew(NumArgs a, int32_t lo, int32_t count) {
+    constexpr int kCols = kDenseWarpWords * 32;
+    __shared__ double vs[ROWS][kCols];
+    __shared__ __align__(16) uint32_t fls[ROWS][kCols / 4];
+    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    if (item >= count) return;
+    double *vals = vs[g];
+    uint32_t *fw = fls[g];
+    uint8_t *fb = reinterpret_cast<uint8_t *>(fw);
+    const int32_t row = a.list[lo + item];
+    const int32_t rlo = a.rowLo[row];
+    const int32_t cbase = (rlo >> 5) << 5;
+    const int sw = min(span_words(rlo, a.rowHi[row]), kDenseWarpWords);
+    const uint32_t nb = (uint32_t)sw * 32u;
+    const int32_t obc = cbase - col_shift(a, row);  // column written for flag 0
+    const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+    const int64_t obase = a.Cp[row] - a.outBase;
+    for (int i = lane; i < (int)nb; i += 32) vals[i] = 0.0;
+    for (int i = lane; i < sw * 8; i += 32) fw[i] = 0u;
+    __syncwarp();
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    const bool rowwise = a.rowP[row] >= (int64_t)kRowwiseMinLen * (e1 - e0);
+    const bool plain = rowwise && a.bSorted;
+    int *err = a.err;
+    const int32_t *bidx = a.B.idx;
+    const double *bval = a.B.val;
+    warp_products(a.A, a.B, e0, e1, rowwise, lane, [&](int32_t j, double av) {
+        const uint32_t rel = (uint32_t)(bidx[j] - cbase);
+        if (in_window(rel, nb, err)) {
+            if (plain) vals[rel] = __fma_rn(av, bval[j], vals[rel]);
+            else atomic_fma(&vals[rel], av, bval[j]);
+            fb[rel] = 1;
+        }
+    });
+    __syncwarp();
+    // Lane l owns columns [16 l, 16 l + 16) of the window.
+    const uint4 f4 = reinterpret_cast<const uint4 *>(fw)[lane];
+    const bool mine = lane * 16 < (int)nb;
+    const int cnt = mine ? __popc(f4.x) + __popc(f4.y) + __popc(f4.z) + __popc(f4.w) : 0;
+    int incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d) incl += y;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    if (lane == 0 && total != expect) raise(a.err, DEV_COUNT_MISMATCH);
+    if (mine) {
+        int64_t p = incl - cnt;
+        const uint32_t wv[4] = {f4.x, f4.y, f4.z, f4.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                if ((wv[q] >> (8 * b)) & 0xffu) {
+                    const int col = lane * 16 + q * 4 + b;
+                    if (p < expect) {
+                        a.Ci[obase + p] = obc + col;
+                        a.Cv[obase + p] = vals[col];
+                    }
+                    ++p;
+                }
+            }
         }
     }
 }
@@ -879,7 +1018,7 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_rankw(NumArgs a, int32_t lo, 
             if (t < c.total && (uint32_t)col < (uint32_t)(kWarpSpanWords * 32)) {
                 const int w = col >> 5;
                 const int r = wp[w] + __popc(bm[w] & ((1u << (col & 31)) - 1u));
-                if (r < kNumWarpMax) atomicAdd(&vals[r], __dmul_rn(av, a.B.val[j]));
+                if (r < kNumWarpMax) atomic_fma(&vals[r], av, a.B.val[j]);
             }
         }
     }
@@ -980,7 +1119,7 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
                         // smallest next column); the guard keeps a malformed row
                         // inside shared memory all the same
                         const int rel = v ? max(c - c_lo, 0) : 0;
-                        if (v) atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[p]));
+                        if (v) atomic_fma(&dense[rel], av, a.B.val[p]);
                         or_bits_runs(bits, v, (uint32_t)rel);
                         const int n = __popc(m);
                         cur += n;
@@ -995,7 +1134,7 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
                         const int32_t c = q < end ? a.B.idx[q] : INT_MAX;
                         const bool v = c >= c_lo && c < c_hi;
                         const int rel = v ? c - c_lo : 0;
-                        if (v) atomicAdd(&dense[rel], __dmul_rn(av, a.B.val[q]));
+                        if (v) atomic_fma(&dense[rel], av, a.B.val[q]);
                         or_bits_runs(bits, v, (uint32_t)rel);
                         if (!v && c >= c_hi) {
                             nxt = min(nxt, c);
@@ -1126,6 +1265,7 @@ constexpr size_t kSmemRankSMax = StageLayout<kRankSThreads>::bytes + 8 * (size_t
 constexpr size_t kSmemRankLMax = StageLayout<kRankLThreads>::bytes + 8 * (size_t)kRankWordsMax;
 constexpr int kBitwRows = 8;
 constexpr int kRankwRows = 8;
+constexpr int kDensewRows = 8;
 
 }  // namespace
 
@@ -1174,7 +1314,7 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
             k_sym_tiny<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(a, begin, n);
             break;
         case SB_BITW:
-            k_sym_bitw<kBitwRows><<<(unsigned)ceil_div(n, kBitwRows), 32 * kBitwRows, 0, s>>>(a, begin, n);
+            k_sym_flagw<kBitwRows><<<(unsigned)ceil_div(n, kBitwRows), 32 * kBitwRows, 0, s>>>(a, begin, n);
             break;
         case SB_HWARP:
             k_sym_hash_warp<kSymWarpRows, kSymWarpTable>
@@ -1211,6 +1351,9 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
         case NB_HWARP:
             k_num_hash_warp<kNumWarpRows, kNumWarpTable>
                 <<<(unsigned)ceil_div(n, kNumWarpRows), 32 * kNumWarpRows, kSmemNumWarp, s>>>(a, lo, n);
+            break;
+        case NB_DENSEW:
+            k_num_densew<kDensewRows><<<(unsigned)ceil_div(n, kDensewRows), 32 * kDensewRows, 0, s>>>(a, lo, n);
             break;
         case NB_RANKW:
             k_num_rankw<kRankwRows><<<(unsigned)ceil_div(n, kRankwRows), 32 * kRankwRows, 0, s>>>(a, lo, n);

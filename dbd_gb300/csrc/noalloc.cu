@@ -215,6 +215,7 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     sa.ctr = nullptr;
     sa.err = flags;
     sa.rowLo = ri.lo;
+    sa.rowP = ri.rowP;
     sa.rowHi = ri.hi;
     int launches = 0;
     for (int bin = SB_TINY; bin < SB_COUNT; ++bin)

@@ -119,21 +119,35 @@ def mixed_rows(rng, m, k, n):
     return A, B
 
 
+def random_band(rng, n, k, half):
+    """n x n, k distinct columns per row drawn from [i - half, i + half]."""
+    rows, cols = [], []
+    for i in range(n):
+        lo, hi = max(0, i - half), min(n - 1, i + half)
+        c = rng.choice(hi - lo + 1, size=min(k, hi - lo + 1), replace=False) + lo
+        rows.append(np.full(c.size, i))
+        cols.append(c)
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    return gen._from_coo(n, n, rows, cols, rng.uniform(-1, 1, rows.size))
+
+
 def test_every_numeric_bin_exercised(ctx, orc):
-    """Rows in every numeric bin: narrow rows (banded, warp rank), rows within
-    2^18 columns (CTA rank, shared and in place), and rows spanning more than
-    2^18 columns (CTA hash of both sizes, dense windows)."""
+    """Rows in every numeric bin: narrow rows (bands: warp dense windows and
+    warp rank), rows within 2^18 columns (CTA rank, shared and in place), and
+    rows spanning more than 2^18 columns (CTA hash of both sizes, dense
+    windows)."""
     rng = np.random.default_rng(11)
     used = set()
     sym_used = set()
     cases = [mixed_rows(rng, 600, 3000, 20000), mixed_rows(rng, 600, 3000, 600000),
-             (gen.banded(3000, 8, seed=3), gen.banded(3000, 8, seed=4))]
+             (gen.banded(3000, 8, seed=3), gen.banded(3000, 8, seed=4)),
+             (random_band(rng, 2000, 8, 400), random_band(rng, 2000, 8, 400))]
     for A, B in cases:
         res = ctx.spgemm(A, B, scope="kernel")
         check(res.C, A, B, orc)
         used |= set(bins_used(res.stats))
         sym_used |= {i for i, v in enumerate(res.stats["sym_rows_per_bin"]) if v}
-    assert used >= set(range(1, 9)), used
+    assert used >= set(range(1, 10)), used
     assert sym_used >= set(range(1, 6)), sym_used
 
 
