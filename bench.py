@@ -68,13 +68,13 @@ def thresholds(tuning=None):
     and the runtime knobs of a context (dbd_tuning; defaults when None)."""
     text = open(os.path.join(ROOT, "dbd_gb300", "csrc", "dbd_internal.h")).read()
     names = ["kTinyMax", "kSymWarpMax", "kSymCtaMax", "kNumWarpMax", "kNumCtaSMax", "kNumCtaLMax",
-             "kWarpSpanWords", "kRankWordsMax", "kWideHashSpanWords", "kDenseWarpWords"]
+             "kWarpSpanWords", "kRankWordsMax", "kWideHashSpanWords", "kDenseWarpWords", "kMidSpanWords"]
     t = {n: int(re.search(rf"\b{n}\s*=\s*(\d+)", text).group(1)) for n in names}
     if tuning:
         t.update(kWarpSpanWords=tuning["warp_span_words"], kNumWarpMax=tuning["warp_max_nnz"],
                  kSymWarpMax=tuning["sym_warp_max_products"], kRankWordsMax=tuning["rank_words_max"],
                  kRankSharedMax=tuning["rank_shared_max_nnz"], kWideHashSpanWords=tuning["sym_hash_span_words"],
-                 kDenseWarpWords=tuning["dense_warp_span_words"])
+                 kDenseWarpWords=tuning["dense_warp_span_words"], kMidSpanWords=tuning["mid_span_words"])
     t.setdefault("kRankSharedMax", t["kNumCtaLMax"])
     return t
 
@@ -108,9 +108,10 @@ def bins(A, rowP, nnz_r, sw, tuning=None):
                      (rowP <= t["kSymCtaMax"]) & (sw > t["kWideHashSpanWords"])], [0, 1, 2, 3, 4], 5)
     num = np.select([nnz_r == 0, tiny, sw <= t["kDenseWarpWords"],
                      (sw <= t["kWarpSpanWords"]) & (nnz_r <= t["kNumWarpMax"]),
+                     (sw <= t["kMidSpanWords"]) & (nnz_r <= t["kNumWarpMax"]),
                      nnz_r <= t["kNumWarpMax"], (sw <= t["kRankWordsMax"]) & (nnz_r <= t["kRankSharedMax"]),
                      sw <= t["kRankWordsMax"], nnz_r <= t["kNumCtaSMax"], nnz_r <= t["kNumCtaLMax"]],
-                    [0, 1, 9, 2, 3, 4, 5, 6, 7], 8)
+                    [0, 1, 9, 2, 10, 3, 4, 5, 6, 7], 8)
     return sym, num
 
 
@@ -118,7 +119,7 @@ SYM_NAMES = {1: "k_sym_tiny", 2: "k_sym_flagw<8>", 3: "k_sym_hash_warp<8,1024>",
              5: "k_sym_wide<512>"}
 NUM_NAMES = {1: "k_num_tiny", 2: "k_num_rankw<8>", 3: "k_num_hash_warp<4,512>", 4: "k_num_rank<256,shared>",
              5: "k_num_rank<512,in-place>", 6: "k_num_hash_cta<256,2048>", 7: "k_num_hash_cta<512,8192>",
-             8: "k_num_dense<512,8192>", 9: "k_num_densew<8>"}
+             8: "k_num_dense<512,8192>", 9: "k_num_densew<8>", 10: "k_num_rankm<5>"}
 
 
 def kernel_bytes(A, rowP, nnz_r, sym, num):
@@ -343,7 +344,7 @@ def run_batched(args, local):
     import dbd_gb300 as dbd
     from dbd_gb300 import generators as gen
     from dbd_gb300.csr import CSR
-    count = 512
+    count = int(args.workload[len("batched"):] or 512)
     pairs = gen.batched_pairs(count, seed=0)
     As = [a for a, _, _ in pairs]
     Bs = [b for _, b, _ in pairs]
@@ -465,7 +466,7 @@ def run_batched(args, local):
             "warmup": args.warmup, "ms_per_step": round(t_batch * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded pairs, numpy PCG64)",
-            "config": {"workload": "batched: 512 independent A_q*B_q, n_q log-uniform in [1024, 65536], "
+            "config": {"workload": f"batched: {count} independent A_q*B_q, n_q log-uniform in [1024, 65536], "
                        "uniform Poisson(12) rows or band |i-j|<=32 (50/50 by seed), values U[-1,1], seed 0",
                        "pairs": count, "banded_pairs": int(sum(k == "banded" for k in kinds)),
                        "rows": int(len(rowP)), "nnz_a": int(sum(A.nnz for A in As)),
@@ -480,7 +481,7 @@ def run_batched(args, local):
                               "what": "dbd_update_values: new device values for every pair, the captured "
                                       "CUDA graph of the numeric kernels replayed (C's values recomputed)"},
             "sequential": {"gflops": g(t_seq), "ms": round(t_seq * 1e3, 3),
-                           "what": "512 plain dbd_spgemm calls (kernel scope) on the same device-resident pairs"},
+                           "what": f"{count} plain dbd_spgemm calls (kernel scope) on the same device-resident pairs"},
             "batched_vs_sequential": round(t_seq / t_batch, 3),
             "e2e": {"value": g(te), "unit": "GFLOPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": round(te * 1e3, 3),
@@ -714,7 +715,7 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
-    if args.workload == "batched512":
+    if args.workload.startswith("batched"):
         if rank != 0:
             return 0
         return run_batched(args, local)
@@ -784,11 +785,9 @@ def main():
     torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in evs]
     t_step = float(np.mean(ms)) / 1e3
-    if dist:
-        tt = torch.tensor([t_step], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
-    value = world * 2.0 * P / t_step / 1e9
+    from dbd_gb300 import replicas
+    t_step = replicas.max_over_ranks(t_step, dist, dev)
+    value = replicas.job_rate(2.0 * P, t_step, world) / 1e9
     nnzC = int(stats[-1]["nnz_c"])
     launches = int(sum(s["gpu_launches"] for s in stats))
 

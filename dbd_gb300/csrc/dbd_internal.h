@@ -25,7 +25,8 @@ struct CsrDev {
 // of every bin.
 enum SymBin : uint8_t { SB_EMPTY = 0, SB_TINY, SB_BITW, SB_HWARP, SB_HCTA, SB_WIDE, SB_COUNT };
 enum NumBin : uint8_t {
-    NB_EMPTY = 0, NB_TINY, NB_RANKW, NB_HWARP, NB_RANKS, NB_RANKL, NB_HCTA_S, NB_HCTA_L, NB_DENSE, NB_DENSEW, NB_COUNT
+    NB_EMPTY = 0, NB_TINY, NB_RANKW, NB_HWARP, NB_RANKS, NB_RANKL, NB_HCTA_S, NB_HCTA_L, NB_DENSE, NB_DENSEW, NB_RANKM,
+    NB_COUNT
 };
 constexpr int kMaxBins = 12;
 constexpr int kTileRows = 256;     // granularity of the per-bin offset tables
@@ -43,8 +44,10 @@ constexpr int kDenseWindow = 8192;           // FP64 columns per dense window (6
 constexpr int kWideWindowBitsMax = 1 << 20;  // symbolic bitmap window (128 KiB)
 constexpr int kWarpSpanWords = 64;           // warp-level bitmap rows: span <= 2048 columns
 constexpr int kDenseWarpWords = 16;          // warp dense-window rows: span <= 512 columns
+constexpr int kMidSpanWords = 2048;          // warp rank rows over their own window: span <= 2^16 columns
 constexpr int kRankWordsMax = 8192;          // CTA rank rows: span <= 2^18 columns
 constexpr int kWideHashSpanWords = 2048;     // symbolic: P <= kSymCtaMax rows hash above this span
+constexpr int kWideTouchMax = 8192;          // words a wide-row window clears one by one
 
 __host__ __device__ __forceinline__ int span_words(int32_t lo, int32_t hi) {
     return hi >= lo ? (hi >> 5) - (lo >> 5) + 1 : 0;
@@ -63,6 +66,7 @@ struct Tuning {
     int32_t rankSharedMax = kNumCtaLMax;      // rank rows accumulating in shared memory
     int32_t symHashSpanWords = kWideHashSpanWords;  // symbolic CTA rows hash above this span
     int32_t denseWarpWords = kDenseWarpWords; // numeric rows on one warp's dense window
+    int32_t midSpanWords = kMidSpanWords;     // numeric rows on one warp's rank window
 };
 
 __host__ __device__ __forceinline__ uint8_t sym_bin_of(int64_t P, int32_t nA, int sw, const Tuning &t) {
@@ -80,6 +84,7 @@ __host__ __device__ __forceinline__ uint8_t num_bin_of(int64_t P, int32_t nA, in
     if (P <= kTinyMax && nA <= 32) return NB_TINY;
     if (sw <= t.denseWarpWords) return NB_DENSEW;
     if (sw <= t.warpSpanWords && nnz <= t.numWarpMax) return NB_RANKW;
+    if (sw <= t.midSpanWords && nnz <= t.numWarpMax) return NB_RANKM;
     if (nnz <= t.numWarpMax) return NB_HWARP;
     if (sw <= t.rankWordsMax) return nnz <= t.rankSharedMax ? NB_RANKS : NB_RANKL;
     if (nnz <= kNumCtaSMax) return NB_HCTA_S;
@@ -97,6 +102,7 @@ inline Tuning clamp_tuning(Tuning t) {
     t.rankSharedMax = cl(t.rankSharedMax, 1, kNumCtaLMax);
     t.symHashSpanWords = cl(t.symHashSpanWords, 0, 1 << 26);
     t.denseWarpWords = cl(t.denseWarpWords, 0, kDenseWarpWords);
+    t.midSpanWords = cl(t.midSpanWords, 0, kMidSpanWords);
     return t;
 }
 
@@ -111,7 +117,7 @@ struct RowInfo {
 enum DevErr : int { DEV_OK = 0, DEV_TABLE_FULL = 1, DEV_COUNT_MISMATCH = 2, DEV_ROW_TOO_LONG = 3, DEV_OUT_OF_WINDOW = 4 };
 
 // Counter slots for dynamically scheduled kernels (zeroed per multiply).
-enum CounterSlot : int { CTR_SYM_TINY = 0, CTR_SYM_HWARP, CTR_SYM_HCTA, CTR_SYM_WIDE, CTR_COUNT = 16 };
+enum CounterSlot : int { CTR_SYM_TINY = 0, CTR_SYM_HWARP, CTR_SYM_HCTA, CTR_SYM_WIDE, CTR_NUM_GDENSE, CTR_COUNT = 16 };
 
 struct Binning {
     uint8_t *bin = nullptr;     // m bin ids
@@ -126,7 +132,7 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // ---- launchers (k_analysis.cu) ----
 // First and last column of every row of B (bmin = INT32_MAX, bmax = -1 for
 // empty rows; any column order).
-void launch_row_minmax(const CsrDev &B, int32_t *bmin, int32_t *bmax, cudaStream_t s, int num_sms);
+void launch_row_minmax(const CsrDev &B, int32_t *bmin, int32_t *bmax, int *unsorted, cudaStream_t s, int num_sms);
 void launch_row_products(const CsrDev &A, const int32_t *Bp, const int32_t *bmin, const int32_t *bmax,
                          const RowInfo &ri, uint8_t *symBin, int *err, const Tuning &t, cudaStream_t s,
                          int num_sms);
@@ -136,7 +142,6 @@ void launch_bin_lists(int64_t m, const Binning &b, int nbins, cudaStream_t s);
 void launch_num_bins(int64_t m, const int32_t *Ap, const RowInfo &ri, const int32_t *rowNnz,
                      uint8_t *numBin, const Tuning &t, cudaStream_t s, int num_sms);
 void launch_row_scan(int64_t m, const int32_t *rowNnz, int64_t *part, int64_t *Cp, cudaStream_t s);
-void launch_check_sorted(const CsrDev &B, int *unsorted, cudaStream_t s, int num_sms);
 
 // ---- launchers (k_spgemm.cu) ----
 struct SymArgs {
@@ -156,6 +161,8 @@ struct SymArgs {
     uint32_t *wideBits = nullptr;
     int32_t *wideSlot = nullptr;
     Tuning tune;
+    int numSms = 0;  // persistent kernels size their grid by it; ctr holds their zeroed row counters
+    int bSorted = 0; // B's rows have strictly ascending columns
 };
 // Launches the symbolic kernel of bin `bin` over list[begin, begin + n).
 void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cudaStream_t s, int *launches);
@@ -185,7 +192,19 @@ struct NumArgs {
     const uint32_t *wideBits = nullptr;
     const int32_t *wideSlot = nullptr;
     Tuning tune;
+    int numSms = 0;  // persistent kernels size their grid by it
+    // Global slots for the dense bin (null: shared-memory windows): gSlots
+    // slots of gStride columns, each a bitmap and its word ranks; bitmaps
+    // are zero between rows.
+    uint32_t *gBits = nullptr;
+    uint32_t *gWpre = nullptr;
+    int64_t gStride = 0;   // multiple of 1024
+    int gSlots = 0;
+    uint32_t *ctr = nullptr;  // zeroed row counters (CTR_NUM_GDENSE)
 };
+// Bytes of one global dense slot of `stride` columns.
+inline size_t gdense_slot_bytes(int64_t stride) { return (size_t)stride / 4; }
+constexpr int kGdenseSumMax = 8192;  // summary words in shared memory: C up to 2^23 columns
 // Runs the numeric kernels of bin b over list[lo, hi).
 void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,
                         int *launches);

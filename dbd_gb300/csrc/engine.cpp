@@ -132,6 +132,10 @@ struct dbd_ctx {
     DevBuf rowP, symBin, numBin, rowNnz, symList, numList, hist, symTileOff, numTileOff, symStart,
         numStart, part, Cp, cursor, err, blockP, flags;
     DevBuf Ci, Cv;           // resident product or device output ring
+    DevBuf ctrs;             // row counters of the persistent kernels
+    DevBuf gdense;           // global dense slots of the dense bin
+    int gSlots = 0;
+    int64_t gStride = 0;
     DevBuf wideBits, wideSlot;  // column bitmaps of wide rows kept for the numeric pass
     bool wideKept = false;      // the symbolic pass of this multiply kept them
     DevBuf rowLo, rowHi;        // column window of every row of C
@@ -361,14 +365,14 @@ int load_operand(dbd_ctx *c, Operand &op, const dbd_csr_view *v, const char *nam
 // Sortedness and row column ranges of an operand now on the device.
 int finish_operand(dbd_ctx *c, Operand &op, const CsrDev &d) {
     op.dev = d;
-    // B's rows ascending lets the dense windows use cursors.
+    // Row column ranges (the column windows of the products' rows) and
+    // whether every row ascends strictly (cursors, plain accumulation, runs).
     CK(c, c->flags.ensure(4 * sizeof(int)));
     CK(c, cudaMemsetAsync(c->flags.as<int>() + 2, 0, sizeof(int), c->stream));
-    launch_check_sorted(d, c->flags.as<int>() + 2, c->stream, c->num_sms);
-    // Row column ranges, for the column windows of the products' rows.
     CK(c, op.bmin.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(d.m, 1)));
     CK(c, op.bmax.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(d.m, 1)));
-    launch_row_minmax(d, op.bmin.as<int32_t>(), op.bmax.as<int32_t>(), c->stream, c->num_sms);
+    launch_row_minmax(d, op.bmin.as<int32_t>(), op.bmax.as<int32_t>(), c->flags.as<int>() + 2, c->stream,
+                      c->num_sms);
     int unsorted = 0;
     CK(c, cudaMemcpyAsync(&unsorted, c->flags.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
@@ -491,7 +495,11 @@ int symbolic(dbd_ctx *c) {
     sa.list = c->symList.as<int32_t>();
     sa.binStart = c->symStart.as<int32_t>();
     sa.rowNnz = c->rowNnz.as<int32_t>();
-    sa.ctr = nullptr;
+    CK(c, c->ctrs.ensure(sizeof(uint32_t) * CTR_COUNT));
+    CK(c, cudaMemsetAsync(c->ctrs.p, 0, sizeof(uint32_t) * CTR_COUNT, c->stream));
+    sa.ctr = c->ctrs.as<uint32_t>();
+    sa.numSms = c->num_sms;
+    sa.bSorted = opB_sorted(c);
     sa.err = c->err.as<int>();
     sa.rowLo = c->rowLo.as<int32_t>();
     sa.rowP = c->rowP.as<int64_t>();
@@ -565,6 +573,17 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     na.rowLo = c->rowLo.as<int32_t>();
     na.rowHi = c->rowHi.as<int32_t>();
     na.tune = c->tune;
+    na.numSms = c->num_sms;
+    na.ctr = c->ctrs.as<uint32_t>();
+    if (c->gSlots > 0) {
+        const size_t slot = gdense_slot_bytes(c->gStride);
+        char *base = c->gdense.as<char>();
+        na.gBits = reinterpret_cast<uint32_t *>(base);
+        na.gWpre = reinterpret_cast<uint32_t *>(base + (size_t)c->gSlots * (c->gStride / 8));
+        na.gStride = c->gStride;
+        na.gSlots = c->gSlots;
+        (void)slot;
+    }
     if (c->wideKept) {
         na.wideBits = c->wideBits.as<uint32_t>();
         na.wideSlot = c->wideSlot.as<int32_t>();
@@ -574,8 +593,8 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     const int64_t t1 = (r1 >= c->m) ? c->ntiles : r1 / kTileRows;
     // Bins run concurrently, one stream each; heaviest first so that their
     // long CTAs start early.
-    static const int order[] = {NB_DENSE,  NB_RANKL, NB_HCTA_L, NB_RANKS, NB_HCTA_S,
-                                NB_HWARP, NB_RANKW, NB_DENSEW, NB_TINY};
+    static const int order[] = {NB_DENSE, NB_RANKL, NB_HCTA_L, NB_RANKS, NB_HCTA_S,
+                                NB_HWARP, NB_RANKM, NB_RANKW, NB_DENSEW, NB_TINY};
     Fork fk(c);
     for (int b : order) {
         const int32_t lo = c->numTileOff_h[(size_t)t0 * kMaxBins + b];
@@ -683,6 +702,21 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     const auto t0 = Clock::now();
     int rc = symbolic(c);
     if (rc) return rc;
+    // Global dense slots for the dense bin: up to two per SM, within an
+    // eighth of the GPU budget; too few fit -> shared-memory windows.
+    c->gSlots = 0;
+    if (c->numStart_h[NB_DENSE + 1] > c->numStart_h[NB_DENSE]) {
+        const int64_t stride = (c->ncols + 1023) / 1024 * 1024;
+        const size_t slot = gdense_slot_bytes(stride);
+        const int64_t fit = (int64_t)(c->cfg.gpu_gib * kGiB / 8 / (double)slot);
+        const int slots = (int)std::min<int64_t>(2 * (int64_t)c->num_sms, fit);
+        if (slots >= c->num_sms / 2 && slots > 0 && stride / 1024 <= kGdenseSumMax) {
+            CK(c, c->gdense.ensure(slot * (size_t)slots));
+            CK(c, cudaMemsetAsync(c->gdense.p, 0, slot * (size_t)slots, c->stream));
+            c->gSlots = slots;
+            c->gStride = stride;
+        }
+    }
     const int64_t m = c->m, nnz = c->nnzC;
     const double gpu_budget = c->cfg.gpu_gib * kGiB;
     const double host_budget = c->cfg.host_gib * kGiB;
@@ -692,7 +726,8 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     const double used = (double)(c->A.ptr.cap + c->A.idx.cap + c->A.val.cap + c->B.ptr.cap + c->B.idx.cap +
                                  c->B.val.cap + c->rowP.cap + c->symBin.cap + c->numBin.cap + c->rowNnz.cap +
                                  c->symList.cap + c->numList.cap + c->hist.cap + c->symTileOff.cap +
-                                 c->numTileOff.cap + c->part.cap + c->Cp.cap + c->cursor.cap);
+                                 c->numTileOff.cap + c->part.cap + c->Cp.cap + c->cursor.cap +
+                                 (c->gSlots ? c->gdense.cap : 0) + c->wideBits.cap);
     const double dev_avail = std::min(gpu_budget - used, (double)free_b - 512.0 * 1024 * 1024);
     const double out_bytes = 12.0 * (double)nnz;
     const bool resident = out_bytes <= std::max(0.0, dev_avail) && scope == DBD_SCOPE_KERNEL;
@@ -1060,7 +1095,8 @@ void dbd_destroy(dbd_ctx *c) {
                       &c->rowP, &c->symBin, &c->numBin, &c->rowNnz, &c->symList, &c->numList, &c->hist,
                       &c->symTileOff, &c->numTileOff, &c->symStart, &c->numStart, &c->part, &c->Cp, &c->cursor,
                       &c->err, &c->blockP, &c->flags, &c->Ci, &c->Cv, &c->wideBits, &c->wideSlot, &c->adjG,
-                      &c->adjA, &c->adjB, &c->rowLo, &c->rowHi, &c->A.bmin, &c->A.bmax, &c->B.bmin, &c->B.bmax})
+                      &c->adjA, &c->adjB, &c->rowLo, &c->rowHi, &c->A.bmin, &c->A.bmax, &c->B.bmin, &c->B.bmax,
+                      &c->ctrs, &c->gdense})
         b->release();
     c->hCp.release();
     c->hCi.release();
@@ -1444,6 +1480,7 @@ int dbd_get_tuning(const dbd_ctx *c, dbd_tuning *t) {
     t->rank_shared_max_nnz = c->tune.rankSharedMax;
     t->sym_hash_span_words = c->tune.symHashSpanWords;
     t->dense_warp_span_words = c->tune.denseWarpWords;
+    t->mid_span_words = c->tune.midSpanWords;
     return DBD_OK;
 }
 
@@ -1457,6 +1494,7 @@ int dbd_set_tuning(dbd_ctx *c, const dbd_tuning *t) {
     u.rankSharedMax = t->rank_shared_max_nnz;
     u.symHashSpanWords = t->sym_hash_span_words;
     u.denseWarpWords = t->dense_warp_span_words;
+    u.midSpanWords = t->mid_span_words;
     const Tuning v = clamp_tuning(u);
     if (memcmp(&u, &v, sizeof(u)) != 0) return set_err(c, DBD_ERR_INVALID, "a tuning value is out of its range");
     c->tune = u;
@@ -1495,6 +1533,7 @@ int dbd_autotune(dbd_ctx *c, int repeats, dbd_tuning *best, double *best_ms) {
         {&Tuning::symWarpMax, {128, 256, 512}},
         {&Tuning::symHashSpanWords, {512, 2048, 8192}},
         {&Tuning::denseWarpWords, {0, 4, 8, 16}},
+        {&Tuning::midSpanWords, {0, 256, 1024, 2048}},
     };
     const Tuning start = c->tune;
     Tuning cur = start;

@@ -19,16 +19,20 @@ namespace {
 constexpr unsigned FULL = 0xffffffffu;
 
 // First and last column of every B row (one warp per row, any column order).
-__global__ void k_row_minmax(CsrDev B, int32_t *__restrict__ bmin, int32_t *__restrict__ bmax) {
+__global__ void k_row_minmax(CsrDev B, int32_t *__restrict__ bmin, int32_t *__restrict__ bmax,
+                             int *__restrict__ unsorted) {
     const int lane = threadIdx.x & 31;
     int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t stride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    bool down = false;  // some column not above its predecessor
     for (; row < B.m; row += stride) {
         int32_t lo = INT32_MAX, hi = -1;
-        for (int32_t i = B.ptr[row] + lane; i < B.ptr[row + 1]; i += 32) {
+        const int32_t s = B.ptr[row], e = B.ptr[row + 1];
+        for (int32_t i = s + lane; i < e; i += 32) {
             const int32_t c = B.idx[i];
             lo = min(lo, c);
             hi = max(hi, c);
+            if (i > s && c <= B.idx[i - 1]) down = true;
         }
 #pragma unroll
         for (int d = 16; d; d >>= 1) {
@@ -40,6 +44,7 @@ __global__ void k_row_minmax(CsrDev B, int32_t *__restrict__ bmin, int32_t *__re
             bmax[row] = hi;
         }
     }
+    if (down) atomicExch(unsorted, 1);
 }
 
 // Products per row, P_r = sum over k in A_r of |B_k|, and the row's column
@@ -285,15 +290,6 @@ __global__ void k_scan_final(int64_t m, const int32_t *__restrict__ cnt,
 }
 
 // Flags B rows whose columns are not strictly ascending.
-__global__ void k_check_sorted(CsrDev B, int *unsorted) {
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < B.m;
-         r += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t s = B.ptr[r], e = B.ptr[r + 1];
-        for (int32_t i = s + 1; i < e; ++i)
-            if (B.idx[i] <= B.idx[i - 1]) { atomicExch(unsorted, 1); break; }
-    }
-}
-
 __global__ void k_f32_to_f64(const float *__restrict__ src, double *__restrict__ dst, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         dst[i] = (double)src[i];
@@ -320,10 +316,10 @@ __global__ void k_validate_idx(const int32_t *__restrict__ idx, int64_t nnz, int
 
 }  // namespace
 
-void launch_row_minmax(const CsrDev &B, int32_t *bmin, int32_t *bmax, cudaStream_t s, int num_sms) {
+void launch_row_minmax(const CsrDev &B, int32_t *bmin, int32_t *bmax, int *unsorted, cudaStream_t s, int num_sms) {
     if (B.m == 0) return;
     const int grid = (int)std::min<int64_t>(ceil_div(B.m * 32, 256), (int64_t)num_sms * 8);
-    k_row_minmax<<<grid, 256, 0, s>>>(B, bmin, bmax);
+    k_row_minmax<<<grid, 256, 0, s>>>(B, bmin, bmax, unsorted);
 }
 
 void launch_row_products(const CsrDev &A, const int32_t *Bp, const int32_t *bmin, const int32_t *bmax,
@@ -366,12 +362,6 @@ void launch_row_scan(int64_t m, const int32_t *rowNnz, int64_t *part, int64_t *C
     } else {
         cudaMemsetAsync(Cp, 0, sizeof(int64_t), s);
     }
-}
-
-void launch_check_sorted(const CsrDev &B, int *unsorted, cudaStream_t s, int num_sms) {
-    if (B.m == 0) return;
-    const int grid = (int)std::min<int64_t>(ceil_div(B.m, 256), (int64_t)num_sms * 8);
-    k_check_sorted<<<grid, 256, 0, s>>>(B, unsorted);
 }
 
 void launch_f32_to_f64(const float *src, double *dst, int64_t n, cudaStream_t s) {

@@ -240,6 +240,12 @@ __device__ __forceinline__ void warp_range(const int32_t *pre, const int32_t *bs
     int e0 = find_entry(pre, nb, tb);
     for (int32_t t0 = tb; t0 < te; t0 += 32) {
         const int32_t t = t0 + lane;
+        const bool valid = t < te;
+        if (e0 + 1 >= nb || pre[e0 + 1] > t0 + 31) {
+            // All 32 products lie in entry e0 (long B rows): no search.
+            f(valid, bst[e0] + (t - pre[e0]), e0);
+            continue;
+        }
         const int ej = e0 + 1 + lane;
         const int32_t bnd = ej <= nb ? pre[ej] : INT_MAX;
         int o = 0;
@@ -249,7 +255,6 @@ __device__ __forceinline__ void warp_range(const int32_t *pre, const int32_t *bs
             if (v <= t) o += step;
         }
         const int e = min(e0 + o, nb - 1);
-        const bool valid = t < te;
         f(valid, bst[e] + (t - pre[e]), e);
         e0 = __shfl_sync(FULL, e, 31);
     }
@@ -260,11 +265,17 @@ __device__ __forceinline__ void warp_range(const int32_t *pre, const int32_t *bs
 // row hold ascending columns, so equal words sit in adjacent lanes; a
 // segmented OR over such runs leaves each run's bits in its first lane.
 // Bits of equal words in non-adjacent lanes are ORed more than once, which
-// is harmless.  All lanes call; `v` marks lanes with a bit.
+// is harmless.  When no two adjacent lanes share a word (sparse rows, the
+// common case of power-law matrices) every lane ORs its own bit directly.
+// All lanes call; `v` marks lanes with a bit.
 __device__ __forceinline__ void or_bits_runs(uint32_t *bm, bool v, uint32_t rel) {
     const int lane = threadIdx.x & 31;
     const int32_t w = v ? (int32_t)(rel >> 5) : -1 - lane;
     uint32_t acc = v ? 1u << (rel & 31) : 0u;
+    if (!__any_sync(FULL, __shfl_up_sync(FULL, w, 1) == w && lane > 0)) {
+        if (v) atomicOr(&bm[w], acc);
+        return;
+    }
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
         const int32_t ow = __shfl_down_sync(FULL, w, d);
@@ -422,52 +433,109 @@ __global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t beg
     if (tid == 0) a.rowNnz[row] = cnt;
 }
 
-// Wide rows: one CTA per row, a shared bitmap over windows of winBits
-// columns; the row's size is the bitmap's popcount.
+// or_bits_runs that also counts and records: returns the number of bits this
+// lane newly set (popc of its OR against the word's old value), and appends
+// every word it finds zero to touched[] (through *nt; entries past cap are
+// dropped, *nt still counts them).  All lanes call.
+__device__ __forceinline__ int or_bits_count(uint32_t *bm, bool v, uint32_t rel, int32_t *touched, int *nt,
+                                             int cap) {
+    const int lane = threadIdx.x & 31;
+    const int32_t w = v ? (int32_t)(rel >> 5) : -1 - lane;
+    uint32_t acc = v ? 1u << (rel & 31) : 0u;
+    bool head = v;
+    if (__any_sync(FULL, __shfl_up_sync(FULL, w, 1) == w && lane > 0)) {
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int32_t ow = __shfl_down_sync(FULL, w, d);
+            const uint32_t ob = __shfl_down_sync(FULL, acc, d);
+            if (lane + d < 32 && ow == w) acc |= ob;
+        }
+        const int32_t pw = __shfl_up_sync(FULL, w, 1);
+        head = v && (lane == 0 || pw != w);
+    }
+    if (!head) return 0;
+    const uint32_t old = atomicOr(&bm[w], acc);
+    if (old == 0u) {
+        const int k = atomicAdd(nt, 1);
+        if (k < cap) touched[k] = w;
+    }
+    return __popc(acc & ~old);
+}
+
+// Words a wide-row window clears one by one: past a quarter of the window a
+// full clear is as cheap.
+__host__ __device__ __forceinline__ int wide_touch_cap(int winBits) {
+    return min(kWideTouchMax, (winBits >> 5) / 4);
+}
+
+// Wide rows: persistent CTAs take rows from a counter (heavy rows spread
+// over the whole grid).  A shared bitmap over windows of winBits columns
+// stays zero between rows: every window records the words it touched and
+// clears only those (the whole window when more than kWideTouchMax were
+// touched).  The row's size is the sum of newly set bits, so no popcount
+// pass over the window either: a row costs its products, not its span.
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, int winBits) {
+__global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, int32_t count, int winBits) {
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
     __shared__ int32_t sh[THREADS / 32];
+    __shared__ int nt;
+    __shared__ int32_t next;
     int32_t *pre = reinterpret_cast<int32_t *>(smem + L::pre);
     int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
     uint32_t *bm = reinterpret_cast<uint32_t *>(smem + L::bytes);
+    int32_t *touched = reinterpret_cast<int32_t *>(bm + (winBits >> 5));
+    const int cap = wide_touch_cap(winBits);
     const int tid = threadIdx.x;
-    const int32_t row = a.list[begin + blockIdx.x];
-    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
-    // The row's window [lo, hi], in windows of winBits columns from lo's word.
-    const int32_t rlo = a.rowLo[row], rhi = a.rowHi[row];
-    const int sw = span_words(rlo, rhi);
-    const int64_t base = (int64_t)(rlo >> 5) << 5;
-    const int64_t end = (int64_t)rhi + 1;
-    int cnt = 0;
-    for (int64_t c_lo = base; c_lo < end; c_lo += winBits) {
-        const int words = (int)min((int64_t)winBits, end - c_lo + 31) >> 5;
-        for (int i = tid; i < words; i += THREADS) bm[i] = 0u;
-        for (int32_t eb = e0; eb < e1; eb += THREADS) {
-            int nb;
-            const int32_t total =
-                stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
-            int32_t tb, te;
-            warp_share<THREADS>(total, &tb, &te);
-            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-                const int64_t rel = v ? (int64_t)a.B.idx[pos] - c_lo : -1;
-                const bool in = rel >= 0 && rel < winBits;
-                or_bits_runs(bm, in, in ? (uint32_t)rel : 0u);
-            });
+    for (int i = tid; i < (winBits >> 5); i += THREADS) bm[i] = 0u;
+    for (;;) {
+        if (tid == 0) next = (int32_t)atomicAdd(&a.ctr[CTR_SYM_WIDE], 1u);
+        __syncthreads();
+        const int32_t item = next;
+        if (item >= count) break;
+        const int32_t row = a.list[begin + item];
+        const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+        // The row's window [lo, hi], in windows of winBits columns from lo's word.
+        const int32_t rlo = a.rowLo[row], rhi = a.rowHi[row];
+        const int sw = span_words(rlo, rhi);
+        const int64_t base = (int64_t)(rlo >> 5) << 5;
+        const int64_t end = (int64_t)rhi + 1;
+        int cnt = 0;
+        for (int64_t c_lo = base; c_lo < end; c_lo += winBits) {
+            const int words = (int)min((int64_t)winBits, end - c_lo + 31) >> 5;
+            if (tid == 0) nt = 0;
+            __syncthreads();
+            for (int32_t eb = e0; eb < e1; eb += THREADS) {
+                int nb;
+                const int32_t total =
+                    stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
+                int32_t tb, te;
+                warp_share<THREADS>(total, &tb, &te);
+                warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
+                    const int64_t rel = v ? (int64_t)a.B.idx[pos] - c_lo : -1;
+                    const bool in = rel >= 0 && rel < winBits;
+                    cnt += or_bits_count(bm, in, in ? (uint32_t)rel : 0u, touched, &nt, cap);
+                });
+                __syncthreads();
+            }
+            if (a.wideBits && sw <= kRankWordsMax) {
+                // One window covers the row here; keep its bitmap for the numeric pass.
+                uint32_t *dst = a.wideBits + (size_t)item * kRankWordsMax;
+                for (int i = tid; i < sw; i += THREADS) dst[i] = bm[i];
+                if (tid == 0) a.wideSlot[row] = item;
+                __syncthreads();
+            }
+            const int n = nt;
+            if (n <= cap) {
+                for (int i = tid; i < n; i += THREADS) bm[touched[i]] = 0u;
+            } else {
+                for (int i = tid; i < words; i += THREADS) bm[i] = 0u;
+            }
             __syncthreads();
         }
-        if (a.wideBits && sw <= kRankWordsMax) {
-            // One window covers the row here; keep its bitmap for the numeric pass.
-            uint32_t *dst = a.wideBits + (size_t)blockIdx.x * kRankWordsMax;
-            for (int i = tid; i < sw; i += THREADS) dst[i] = bm[i];
-            if (tid == 0) a.wideSlot[row] = (int32_t)blockIdx.x;
-        }
-        for (int i = tid; i < words; i += THREADS) cnt += __popc(bm[i]);
-        __syncthreads();
+        cnt = block_sum_i<THREADS>(cnt, sh);
+        if (tid == 0) a.rowNnz[row] = cnt;
     }
-    cnt = block_sum_i<THREADS>(cnt, sh);
-    if (tid == 0) a.rowNnz[row] = cnt;
 }
 
 // Products of one row for one warp, calling f(j, av) for every product (B
@@ -537,10 +605,46 @@ __global__ void __launch_bounds__(32 * ROWS) k_sym_flagw(SymArgs a, int32_t begi
     const bool rowwise = a.rowP[row] >= (int64_t)kRowwiseMinLen * (e1 - e0);
     int *err = a.err;
     const int32_t *bidx = a.B.idx;
-    warp_products(a.A, a.B, e0, e1, rowwise, lane, [&](int32_t j, double) {
-        const uint32_t rel = (uint32_t)(bidx[j] - base);
-        if (in_window(rel, nb, err)) fb[rel] = 1;
-    });
+    if (rowwise) {
+        // One A entry at a time.  A B row whose columns form one contiguous
+        // run (banded and stencil matrices) flags its run a word (4 columns)
+        // per lane; any other B row flags a column per lane.
+        for (int32_t eb = e0; eb < e1; eb += 32) {
+            int32_t bs = 0, len = 0;
+            if (eb + lane < e1) {
+                const int32_t k = a.A.idx[eb + lane];
+                bs = a.B.ptr[k];
+                len = a.B.ptr[k + 1] - bs;
+            }
+            const int n = min(32, e1 - eb);
+            for (int q = 0; q < n; ++q) {
+                const int32_t bq = __shfl_sync(FULL, bs, q);
+                const int32_t lq = __shfl_sync(FULL, len, q);
+                if (lq == 0) continue;
+                const int32_t first = bidx[bq], last = bidx[bq + lq - 1];
+                const uint32_t r0 = (uint32_t)(first - base), r1 = (uint32_t)(last - base);
+                if (a.bSorted && last - first == lq - 1 && r0 < nb && r1 < nb) {
+                    for (uint32_t w = (r0 >> 2) + lane; w <= (r1 >> 2); w += 32) {
+                        uint32_t m = 0x01010101u;
+                        if (w == (r0 >> 2)) m &= 0xffffffffu << (8 * (r0 & 3));
+                        if (w == (r1 >> 2)) m &= 0xffffffffu >> (8 * (3 - (r1 & 3)));
+                        atomicOr(&fw[w], m);
+                    }
+                } else {
+                    for (int32_t i = lane; i < lq; i += 32) {
+                        const uint32_t rel = (uint32_t)(bidx[bq + i] - base);
+                        if (in_window(rel, nb, err)) fb[rel] = 1;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    } else {
+        warp_products(a.A, a.B, e0, e1, false, lane, [&](int32_t j, double) {
+            const uint32_t rel = (uint32_t)(bidx[j] - base);
+            if (in_window(rel, nb, err)) fb[rel] = 1;
+        });
+    }
     __syncwarp();
     int cnt = 0;
     for (int i = lane; i < sw * 8; i += 32) cnt += __popc(fw[i]);
@@ -906,14 +1010,50 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_densew(NumArgs a, int32_t lo,
     int *err = a.err;
     const int32_t *bidx = a.B.idx;
     const double *bval = a.B.val;
-    warp_products(a.A, a.B, e0, e1, rowwise, lane, [&](int32_t j, double av) {
-        const uint32_t rel = (uint32_t)(bidx[j] - cbase);
+    auto add = [&](uint32_t rel, double av, double bv) {
         if (in_window(rel, nb, err)) {
-            if (plain) vals[rel] = __fma_rn(av, bval[j], vals[rel]);
-            else atomic_fma(&vals[rel], av, bval[j]);
+            if (plain) vals[rel] = __fma_rn(av, bv, vals[rel]);
+            else atomic_fma(&vals[rel], av, bv);
             fb[rel] = 1;
         }
-    });
+    };
+    if (rowwise) {
+        // One A entry at a time; each lane loads up to four of the B row's
+        // products before using any, so their loads are in flight together.
+        for (int32_t eb = e0; eb < e1; eb += 32) {
+            int32_t bs = 0, len = 0;
+            double avl = 0.0;
+            if (eb + lane < e1) {
+                const int32_t k = a.A.idx[eb + lane];
+                bs = a.B.ptr[k];
+                len = a.B.ptr[k + 1] - bs;
+                avl = a.A.val[eb + lane];
+            }
+            const int n = min(32, e1 - eb);
+            for (int q = 0; q < n; ++q) {
+                const int32_t bq = __shfl_sync(FULL, bs, q);
+                const int32_t lq = __shfl_sync(FULL, len, q);
+                const double aq = __shfl_sync(FULL, avl, q);
+                for (int32_t i0 = 0; i0 < lq; i0 += 128) {
+                    int32_t c[4];
+                    double v[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int32_t i = i0 + 32 * u + lane;
+                        c[u] = i < lq ? bidx[bq + i] : INT_MIN;
+                        v[u] = i < lq ? bval[bq + i] : 0.0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (c[u] != INT_MIN) add((uint32_t)(c[u] - cbase), aq, v[u]);
+                }
+                __syncwarp();
+            }
+        }
+    } else {
+        warp_products(a.A, a.B, e0, e1, false, lane,
+                      [&](int32_t j, double av) { add((uint32_t)(bidx[j] - cbase), av, bval[j]); });
+    }
     __syncwarp();
     // Lane l owns columns [16 l, 16 l + 16) of the window.
     const uint4 f4 = reinterpret_cast<const uint4 *>(fw)[lane];
@@ -1027,13 +1167,253 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_rankw(NumArgs a, int32_t lo, 
     for (int64_t i = lane; i < nout; i += 32) a.Cv[obase + i] = vals[i];
 }
 
-// Dense rows: one CTA per row sweeps windows of W columns.  The per-entry
-// state (cursor into the B row, its end, the A value, the next column at or
-// past the cursor) is staged in shared memory for THREADS entries at a time;
-// rows with more entries keep it in a.state between windows.  One warp per
-// entry scans its B row from the cursor 32 products per step; with B rows
-// ascending the products inside the window are a prefix found by ballot.
-// Without sorted B rows every window rescans whole B rows and filters.
+// or_bits_runs that also marks, in a summary bitmap (one bit per word),
+// every word it finds zero.  All lanes call.
+__device__ __forceinline__ void or_bits_mark(uint32_t *bm, uint32_t *sum, bool v, uint32_t rel) {
+    const int lane = threadIdx.x & 31;
+    const int32_t w = v ? (int32_t)(rel >> 5) : -1 - lane;
+    uint32_t acc = v ? 1u << (rel & 31) : 0u;
+    bool head = v;
+    if (__any_sync(FULL, __shfl_up_sync(FULL, w, 1) == w && lane > 0)) {
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int32_t ow = __shfl_down_sync(FULL, w, d);
+            const uint32_t ob = __shfl_down_sync(FULL, acc, d);
+            if (lane + d < 32 && ow == w) acc |= ob;
+        }
+        const int32_t pw = __shfl_up_sync(FULL, w, 1);
+        head = v && (lane == 0 || pw != w);
+    }
+    if (head && atomicOr(&bm[w], acc) == 0u) atomicOr(&sum[w >> 5], 1u << (w & 31));
+}
+
+// Rows of at most kNumWarpMax entries whose window spans at most
+// kMidSpanWords words: persistent warps, one row at a time, the rank method
+// over the row's own window.  A summary bitmap (one bit per window word)
+// lists the words the row touched, so word ranks, output and the clean-up
+// for the next row visit only those words: a row costs its products and
+// entries, not its span.  No hash table, no sort.
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_num_rankm(NumArgs a, int32_t lo, int32_t count) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int kSumWords = kMidSpanWords / 32;
+    constexpr size_t kWarpBytes =
+        8 * (size_t)kNumWarpMax + 4 * (size_t)kMidSpanWords + 4 * (size_t)kSumWords + 2 * (size_t)kMidSpanWords;
+    const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *vals = reinterpret_cast<double *>(smem + g * kWarpBytes);
+    uint32_t *bm = reinterpret_cast<uint32_t *>(vals + kNumWarpMax);
+    uint32_t *sum = bm + kMidSpanWords;
+    uint16_t *wp = reinterpret_cast<uint16_t *>(sum + kSumWords);
+    for (int i = lane; i < kMidSpanWords; i += 32) bm[i] = 0u;
+    for (int i = lane; i < kSumWords; i += 32) sum[i] = 0u;
+    for (int i = lane; i < kNumWarpMax; i += 32) vals[i] = 0.0;
+    __syncwarp();
+    const int64_t warps = (int64_t)gridDim.x * ROWS;
+    for (int64_t item = (int64_t)blockIdx.x * ROWS + g; item < count; item += warps) {
+        const int32_t row = a.list[lo + item];
+        const int32_t rlo = a.rowLo[row];
+        const int32_t cbase = (rlo >> 5) << 5;
+        const int nw = min(span_words(rlo, a.rowHi[row]), kMidSpanWords);
+        const uint32_t nbits = (uint32_t)nw * 32u;
+        const int32_t obc = cbase - col_shift(a, row);  // column written for bit 0
+        const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+        const int64_t obase = a.Cp[row] - a.outBase;
+        const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+        for (int32_t e = e0; e < e1; e += 32) {
+            const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+            for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+                const int32_t t = t0 + lane;
+                const int32_t j = chunk_pos(c, t, nullptr);
+                const uint32_t rel = t < c.total ? (uint32_t)(a.B.idx[j] - cbase) : 0u;
+                const bool v = t < c.total && in_window(rel, nbits, a.err);
+                or_bits_mark(bm, sum, v, rel);
+            }
+        }
+        __syncwarp();
+        // Lane l owns window words [64 l, 64 l + 64): summary words 2l, 2l + 1.
+        const uint32_t s0 = sum[2 * lane], s1 = sum[2 * lane + 1];
+        int cnt = 0;
+        for (uint32_t m = s0; m; m &= m - 1u) cnt += __popc(bm[64 * lane + __ffs(m) - 1]);
+        for (uint32_t m = s1; m; m &= m - 1u) cnt += __popc(bm[64 * lane + 32 + __ffs(m) - 1]);
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(FULL, incl, d);
+            if (lane >= d) incl += y;
+        }
+        const int total = __shfl_sync(FULL, incl, 31);
+        if (lane == 0 && total != expect) raise(a.err, DEV_COUNT_MISMATCH);
+        int64_t p = incl - cnt;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            for (uint32_t m = h ? s1 : s0; m; m &= m - 1u) {
+                const int w = 64 * lane + 32 * h + __ffs(m) - 1;
+                wp[w] = (uint16_t)p;
+                uint32_t word = bm[w];
+                while (word) {
+                    const int b = __ffs(word) - 1;
+                    word &= word - 1u;
+                    if (p < expect) a.Ci[obase + p] = obc + (w << 5) + b;
+                    ++p;
+                }
+            }
+        }
+        __syncwarp();
+        for (int32_t e = e0; e < e1; e += 32) {
+            const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+            for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+                const int32_t t = t0 + lane;
+                double av;
+                const int32_t j = chunk_pos(c, t, &av);
+                const int32_t col = t < c.total ? a.B.idx[j] - cbase : 0;
+                if (t < c.total && (uint32_t)col < nbits) {
+                    const int w = col >> 5;
+                    const int r = wp[w] + __popc(bm[w] & ((1u << (col & 31)) - 1u));
+                    if (r < kNumWarpMax) atomic_fma(&vals[r], av, a.B.val[j]);
+                }
+            }
+        }
+        __syncwarp();
+        const int nout = (int)min(expect, (int64_t)kNumWarpMax);
+        for (int i = lane; i < nout; i += 32) {
+            a.Cv[obase + i] = vals[i];
+            vals[i] = 0.0;
+        }
+        // Leave the bitmap and summary clean for the next row.
+        for (uint32_t m = s0; m; m &= m - 1u) bm[64 * lane + __ffs(m) - 1] = 0u;
+        for (uint32_t m = s1; m; m &= m - 1u) bm[64 * lane + 32 + __ffs(m) - 1] = 0u;
+        sum[2 * lane] = 0u;
+        sum[2 * lane + 1] = 0u;
+        __syncwarp();
+    }
+}
+
+// Dense rows with a global slot: persistent CTAs, one slot each, take rows
+// from a counter; the rank method over the whole row, its bitmap and word
+// ranks in the slot (two bits per column of C, so the slots of all CTAs stay
+// in L2 for millions of columns) and the summary bitmap (one bit per bitmap
+// word) in shared memory.  Pass 1 sets every product's column bit by an L2
+// reduction (no round trip) and its word's summary bit in shared memory.  The word ranks are computed over the summary
+// bits of the row's window in order (the row's entries plus its span / 1024),
+// which also writes C's columns.  Pass 2 adds every product into C's row in
+// place at its rank (FP64 L2 reductions).  The clean-up clears the words it
+// set.  Reads after reductions go to L2 (__ldcg), past the SM's L1.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_num_gdense(NumArgs a, int32_t lo, int32_t count) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    using L = StageLayout<THREADS>;
+    constexpr int NW = THREADS / 32;
+    __shared__ int32_t sh[NW];
+    __shared__ int32_t next;
+    int32_t *pre = reinterpret_cast<int32_t *>(smem + L::pre);
+    int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
+    double *av = reinterpret_cast<double *>(smem + L::av);
+    uint32_t *sum = reinterpret_cast<uint32_t *>(smem + L::bytes);
+    const int tid = threadIdx.x;
+    uint32_t *bits = a.gBits + (size_t)blockIdx.x * (a.gStride >> 5);
+    uint32_t *wpre = a.gWpre + (size_t)blockIdx.x * (a.gStride >> 5);
+    const uint32_t ncols = (uint32_t)min(a.gStride, a.B.n);
+    int *err = a.err;
+    for (int i = tid; i < (int)(a.gStride >> 10); i += THREADS) sum[i] = 0u;
+    for (;;) {
+        if (tid == 0) next = (int32_t)atomicAdd(&a.ctr[CTR_NUM_GDENSE], 1u);
+        __syncthreads();
+        const int32_t item = next;
+        if (item >= count) break;
+        const int32_t row = a.list[lo + item];
+        const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+        const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+        const int64_t obase = a.Cp[row] - a.outBase;
+        const int32_t shift = col_shift(a, row);
+        // Pass 1: bits.
+        for (int32_t eb = e0; eb < e1; eb += THREADS) {
+            int nb;
+            const int32_t total =
+                stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
+            int32_t tb, te;
+            warp_share<THREADS>(total, &tb, &te);
+            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
+                if (v) {
+                    const uint32_t c = (uint32_t)a.B.idx[pos];
+                    if (in_window(c, ncols, err)) {
+                        atomicOr(&bits[c >> 5], 1u << (c & 31));
+                        atomicOr(&sum[c >> 10], 1u << ((c >> 5) & 31));  // shared
+                    }
+                }
+            });
+            __syncthreads();
+        }
+        __threadfence();
+        __syncthreads();
+        // Word ranks and C's columns; thread t owns a contiguous run of the
+        // window's summary words.
+        const int32_t s0 = a.rowLo[row] >> 10, s1 = a.rowHi[row] >> 10;
+        const int nsum = s1 - s0 + 1;
+        const int per = (nsum + THREADS - 1) / THREADS;
+        const int q0 = s0 + min(nsum, tid * per), q1 = s0 + min(nsum, tid * per + per);
+        int cnt = 0;
+        for (int q = q0; q < q1; ++q)
+            for (uint32_t m = sum[q]; m; m &= m - 1u) cnt += __popc(__ldcg(&bits[q * 32 + __ffs(m) - 1]));
+        int32_t tot;
+        int64_t pos = block_excl_scan<THREADS>(cnt, &tot, sh);
+        if (tid == 0 && tot != expect) raise(a.err, DEV_COUNT_MISMATCH);
+        for (int q = q0; q < q1; ++q) {
+            for (uint32_t m = sum[q]; m; m &= m - 1u) {
+                const int w = q * 32 + __ffs(m) - 1;
+                __stcg(&wpre[w], (uint32_t)pos);
+                uint32_t word = __ldcg(&bits[w]);
+                while (word) {
+                    const int b = __ffs(word) - 1;
+                    word &= word - 1u;
+                    if (pos < expect) a.Ci[obase + pos] = w * 32 + b - shift;
+                    ++pos;
+                }
+            }
+        }
+        for (int64_t i = tid; i < expect; i += THREADS) __stcg(&a.Cv[obase + i], 0.0);
+        __threadfence();
+        __syncthreads();
+        // Pass 2: values in place at their ranks.
+        for (int32_t eb = e0; eb < e1; eb += THREADS) {
+            int nb;
+            const int32_t total =
+                stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
+            int32_t tb, te;
+            warp_share<THREADS>(total, &tb, &te);
+            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t p, int e) {
+                if (v) {
+                    const uint32_t c = (uint32_t)a.B.idx[p];
+                    if (c < ncols) {
+                        const int w = (int)(c >> 5);
+                        const int64_t r = (int64_t)__ldcg(&wpre[w]) + __popc(__ldcg(&bits[w]) & ((1u << (c & 31)) - 1u));
+                        if (r < expect) atomicAdd(&a.Cv[obase + r], __dmul_rn(av[e], a.B.val[p]));
+                    }
+                }
+            });
+            __syncthreads();
+        }
+        // Clean-up: the words this row set, then its summary words.
+        for (int q = q0; q < q1; ++q) {
+            for (uint32_t m = sum[q]; m; m &= m - 1u) __stcg(&bits[q * 32 + __ffs(m) - 1], 0u);
+            sum[q] = 0u;
+        }
+        __threadfence();
+        __syncthreads();
+    }
+}
+
+// Dense rows: one CTA per row sweeps windows of W columns.  Every A entry
+// keeps a cursor into its B row and the next column at or past it, in shared
+// memory for rows of at most ECAP entries and in a.state otherwise.  Per
+// window, each warp reads the next columns of 32 entries at a time (one
+// coalesced load), and only entries with products inside the window are
+// worked on: the warp scans that entry's B row from its cursor 32 products
+// per step (with B rows ascending the products inside the window are a
+// prefix, found by ballot).  No block barrier runs per entry, only per
+// window.  Without sorted B rows every window rescans whole B rows and
+// filters.  The window is zeroed once and every written column is zeroed as
+// it is written out, so a window costs its products and C entries, not its
+// width.
 template <int THREADS, int W, int ECAP, bool SORTED>
 __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1041,21 +1421,21 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
     constexpr int NW = THREADS / 32;
     double *dense = reinterpret_cast<double *>(smem);
     uint32_t *bits = reinterpret_cast<uint32_t *>(smem + 8 * (size_t)W);
-    double *sav = reinterpret_cast<double *>(smem + 8 * (size_t)W + W / 8);
-    int32_t *scur = reinterpret_cast<int32_t *>(sav + ECAP);
-    int32_t *send = scur + ECAP;
-    int32_t *snext = send + ECAP;
+    int32_t *scur = reinterpret_cast<int32_t *>(smem + 8 * (size_t)W + W / 8);
+    int32_t *snext = scur + ECAP;
     __shared__ int32_t sh[NW];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int32_t row = a.list[lo + blockIdx.x];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     const int32_t nA = e1 - e0;
     const bool resident = nA <= ECAP;
-    int32_t *gcur = a.state;             // cursor per A entry
-    int32_t *gnext = a.state + a.A.nnz;  // next column per A entry
+    int32_t *cur_of = resident ? scur : a.state + e0;              // cursor per A entry
+    int32_t *next_of = resident ? snext : a.state + a.A.nnz + e0;  // next column per A entry
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
     const int64_t obase = a.Cp[row] - a.outBase;
     const int32_t shift = col_shift(a, row);
+    for (int i = tid; i < W; i += THREADS) dense[i] = 0.0;
+    for (int i = tid; i < W / 32; i += THREADS) bits[i] = 0u;
 
     // Initial state of every entry.
     int32_t mymin = INT_MAX;
@@ -1069,45 +1449,27 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
             for (int32_t q = s; q < t; ++q) nx = min(nx, a.B.idx[q]);
         }
         mymin = min(mymin, nx);
-        if (resident) {
-            scur[i] = s;
-            send[i] = t;
-            sav[i] = a.A.val[e0 + i];
-            snext[i] = nx;
-        } else {
-            gcur[e0 + i] = s;
-            gnext[e0 + i] = nx;
-        }
+        cur_of[i] = s;
+        next_of[i] = nx;
     }
     int32_t cmin = block_min_i32<THREADS>(mymin, sh);
     int64_t run = 0;
     while (cmin != INT_MAX) {
         const int32_t c_lo = (cmin / W) * W;
         const int64_t c_hi = (int64_t)c_lo + W;
-        for (int i = tid; i < W; i += THREADS) dense[i] = 0.0;
-        for (int i = tid; i < W / 32; i += THREADS) bits[i] = 0u;
         mymin = INT_MAX;
-        for (int32_t eb = 0; eb < nA; eb += ECAP) {
-            const int nb = min(ECAP, nA - eb);
-            if (!resident) {
-                for (int i = tid; i < nb; i += THREADS) {
-                    const int32_t e = e0 + eb + i;
-                    scur[i] = gcur[e];
-                    send[i] = a.B.ptr[a.A.idx[e] + 1];
-                    sav[i] = a.A.val[e];
-                    snext[i] = gnext[e];
-                }
-            }
-            __syncthreads();
-            for (int i = warp; i < nb; i += NW) {
-                const int32_t nx = snext[i];
-                if (nx >= c_hi) {
-                    mymin = min(mymin, nx);
-                    continue;
-                }
-                int32_t cur = scur[i];
-                const int32_t end = send[i];
-                const double av = sav[i];
+        for (int32_t g = warp * 32; g < nA; g += NW * 32) {
+            const int32_t nxl = g + lane < nA ? next_of[g + lane] : INT_MAX;
+            unsigned act = __ballot_sync(FULL, nxl < c_hi);
+            if (nxl >= c_hi) mymin = min(mymin, nxl);
+            while (act) {
+                const int q = __ffs(act) - 1;
+                act &= act - 1u;
+                const int32_t i = g + q;
+                const int32_t k = a.A.idx[e0 + i];
+                const int32_t end = a.B.ptr[k + 1];
+                const double av = a.A.val[e0 + i];
+                int32_t cur = SORTED ? cur_of[i] : a.B.ptr[k];
                 int32_t nxt = INT_MAX;
                 if constexpr (SORTED) {
                     for (;;) {
@@ -1130,36 +1492,27 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
                     }
                 } else {
                     for (int32_t q0 = cur; q0 < end; q0 += 32) {
-                        const int32_t q = q0 + lane;
-                        const int32_t c = q < end ? a.B.idx[q] : INT_MAX;
+                        const int32_t p = q0 + lane;
+                        const int32_t c = p < end ? a.B.idx[p] : INT_MAX;
                         const bool v = c >= c_lo && c < c_hi;
                         const int rel = v ? c - c_lo : 0;
-                        if (v) atomic_fma(&dense[rel], av, a.B.val[q]);
+                        if (v) atomic_fma(&dense[rel], av, a.B.val[p]);
                         or_bits_runs(bits, v, (uint32_t)rel);
-                        if (!v && c >= c_hi) {
-                            nxt = min(nxt, c);
-                        }
+                        if (!v && c >= c_hi) nxt = min(nxt, c);
                     }
 #pragma unroll
                     for (int d = 16; d; d >>= 1) nxt = min(nxt, __shfl_xor_sync(FULL, nxt, d));
                 }
                 mymin = min(mymin, nxt);
                 if (lane == 0) {
-                    if constexpr (SORTED) scur[i] = cur;
-                    snext[i] = nxt;
+                    if constexpr (SORTED) cur_of[i] = cur;
+                    next_of[i] = nxt;
                 }
-            }
-            __syncthreads();
-            if (!resident) {
-                for (int i = tid; i < nb; i += THREADS) {
-                    const int32_t e = e0 + eb + i;
-                    gcur[e] = scur[i];
-                    gnext[e] = snext[i];
-                }
-                __syncthreads();
             }
         }
+        __syncthreads();
         uint32_t word = tid < W / 32 ? bits[tid] : 0u;
+        if (tid < W / 32) bits[tid] = 0u;
         int32_t tot;
         const int32_t off = block_excl_scan<THREADS>(__popc(word), &tot, sh);
         int64_t pos = run + off;
@@ -1171,6 +1524,7 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
                 a.Ci[obase + pos] = c_lo - shift + rel;
                 a.Cv[obase + pos] = dense[rel];
             }
+            dense[rel] = 0.0;
             ++pos;
         }
         run += tot;
@@ -1250,14 +1604,14 @@ constexpr int kSymCtaThreads = 256;
 constexpr int kNumCtaSThreads = 256;
 constexpr int kNumCtaLThreads = 512;
 constexpr int kDenseThreads = 512;
-constexpr int kDenseStage = 256;
+constexpr int kDenseStage = 1024;  // entries whose cursors stay in shared memory
 constexpr int kWideThreads = 512;
 constexpr size_t kSmemSymWarp = (size_t)kSymWarpRows * kSymWarpTable * 4;
 constexpr size_t kSmemSymCta = StageLayout<kSymCtaThreads>::bytes + (size_t)kSymCtaTable * 4;
 constexpr size_t kSmemNumWarp = (size_t)kNumWarpRows * kNumWarpTable * 12;
 constexpr size_t kSmemNumCtaS = StageLayout<kNumCtaSThreads>::bytes + (size_t)kNumCtaSTable * 12;
 constexpr size_t kSmemNumCtaL = StageLayout<kNumCtaLThreads>::bytes + (size_t)kNumCtaLTable * 12;
-constexpr size_t kSmemDense = (size_t)kDenseWindow * 8 + kDenseWindow / 8 + (size_t)kDenseStage * 20;
+constexpr size_t kSmemDense = (size_t)kDenseWindow * 8 + kDenseWindow / 8 + (size_t)kDenseStage * 8;
 constexpr size_t kSmemWideBase = StageLayout<kWideThreads>::bytes;
 constexpr int kRankSThreads = 256, kRankSVcap = kNumCtaLMax;
 constexpr int kRankLThreads = 512;  // global accumulation: staging + bitmap + ranks only
@@ -1266,6 +1620,11 @@ constexpr size_t kSmemRankLMax = StageLayout<kRankLThreads>::bytes + 8 * (size_t
 constexpr int kBitwRows = 8;
 constexpr int kRankwRows = 8;
 constexpr int kDensewRows = 8;
+constexpr int kGdenseThreads = 512;
+constexpr size_t kSmemGdenseBase = StageLayout<kGdenseThreads>::bytes;
+constexpr int kRankmRows = 5;  // 14.6 KiB per warp: three CTAs (15 warps) per SM
+constexpr size_t kSmemRankm =
+    (size_t)kRankmRows * (6 * (size_t)kMidSpanWords + 4 * (size_t)(kMidSpanWords / 32) + 8 * (size_t)kNumWarpMax);
 
 }  // namespace
 
@@ -1275,7 +1634,7 @@ void init_kernel_attributes() {
     cudaFuncSetAttribute(k_sym_hash_cta<kSymCtaThreads, kSymCtaTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemSymCta);
     cudaFuncSetAttribute(k_sym_wide<kWideThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(kSmemWideBase + kWideWindowBitsMax / 8));
+                         (int)(kSmemWideBase + kWideWindowBitsMax / 8 + 4 * (size_t)kWideTouchMax));
     cudaFuncSetAttribute(k_num_hash_warp<kNumWarpRows, kNumWarpTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumWarp);
     cudaFuncSetAttribute(k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>,
@@ -1290,6 +1649,9 @@ void init_kernel_attributes() {
                          (int)kSmemRankSMax);
     cudaFuncSetAttribute(k_num_rank<kRankLThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kSmemRankLMax);
+    cudaFuncSetAttribute(k_num_rankm<kRankmRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemRankm);
+    cudaFuncSetAttribute(k_num_gdense<kGdenseThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(kSmemGdenseBase + 4 * (size_t)kGdenseSumMax));
 }
 
 // Dynamic shared memory of the rank kernel: staging, bitmap and word ranks of
@@ -1324,8 +1686,13 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
             k_sym_hash_cta<kSymCtaThreads, kSymCtaTable><<<(unsigned)n, kSymCtaThreads, kSmemSymCta, s>>>(a, begin);
             break;
         case SB_WIDE: {
+            // Persistent: as many CTAs as fit on the GPU at once (the bitmap
+            // and touch list keep one per SM), rows taken from a counter.
             const int wb = wide_window_bits(a.B.n);
-            k_sym_wide<kWideThreads><<<(unsigned)n, kWideThreads, kSmemWideBase + (size_t)wb / 8, s>>>(a, begin, wb);
+            const size_t smem = kSmemWideBase + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb);
+            const int per_sm = std::max(1, std::min(2048 / kWideThreads, (int)((227 * 1024) / (smem + 1024))));
+            const int grid = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1) * per_sm);
+            k_sym_wide<kWideThreads><<<(unsigned)grid, kWideThreads, smem, s>>>(a, begin, n, wb);
             break;
         }
         default:
@@ -1355,6 +1722,12 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
         case NB_DENSEW:
             k_num_densew<kDensewRows><<<(unsigned)ceil_div(n, kDensewRows), 32 * kDensewRows, 0, s>>>(a, lo, n);
             break;
+        case NB_RANKM: {
+            // Persistent: three CTAs of kRankmRows warps per SM.
+            const int grid = (int)std::min<int64_t>(ceil_div(n, kRankmRows), (int64_t)std::max(a.numSms, 1) * 3);
+            k_num_rankm<kRankmRows><<<(unsigned)grid, 32 * kRankmRows, kSmemRankm, s>>>(a, lo, n);
+            break;
+        }
         case NB_RANKW:
             k_num_rankw<kRankwRows><<<(unsigned)ceil_div(n, kRankwRows), 32 * kRankwRows, 0, s>>>(a, lo, n);
             break;
@@ -1374,7 +1747,12 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
             k_num_hash_cta<kNumCtaLThreads, kNumCtaLTable><<<(unsigned)n, kNumCtaLThreads, kSmemNumCtaL, s>>>(a, lo);
             break;
         case NB_DENSE:
-            if (a.bSorted)
+            if (a.gBits) {
+                cudaMemsetAsync(a.ctr + CTR_NUM_GDENSE, 0, sizeof(uint32_t), s);
+                const int grid = (int)std::min<int64_t>(n, a.gSlots);
+                const size_t smem = kSmemGdenseBase + 4 * (size_t)(a.gStride >> 10);
+                k_num_gdense<kGdenseThreads><<<(unsigned)grid, kGdenseThreads, smem, s>>>(a, lo, n);
+            } else if (a.bSorted)
                 k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, true>
                     <<<(unsigned)n, kDenseThreads, kSmemDense, s>>>(a, lo);
             else

@@ -99,6 +99,7 @@ size_t scratch_bytes(int64_t m, int64_t nnzA, int64_t mB) {
     c.take<int64_t>((size_t)ceil_div(m, kScanTile) + 1);  // part
     c.take<int32_t>(2 * (size_t)nnzA);             // dense-window state
     c.take<int>(4);                                // err + flags
+    c.take<uint32_t>(CTR_COUNT);                   // persistent kernels' row counters
     return c.off;
 }
 
@@ -169,9 +170,11 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     int64_t *part = c.take<int64_t>((size_t)ceil_div(m, kScanTile) + 1);
     int32_t *state = c.take<int32_t>(2 * (size_t)a->nnz);
     int *flags = c.take<int>(4);  // [0] device error word, [1] bad row_ptr, [2] bad index, [3] B unsorted
+    uint32_t *ctrs = c.take<uint32_t>(CTR_COUNT);
 
     // The array keeps the previous call's contents: clear what starts at zero.
     NA_CK(cudaMemsetAsync(flags, 0, 4 * sizeof(int), s));
+    NA_CK(cudaMemsetAsync(ctrs, 0, sizeof(uint32_t) * CTR_COUNT, s));
     NA_CK(cudaMemsetAsync(rowNnz, 0, sizeof(int32_t) * (size_t)(m > 0 ? m : 1), s));
     int hflags[4] = {0, 0, 0, 0};
     const dbd_csr_view *ops[2] = {a, b};
@@ -193,8 +196,7 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     B.ptr = b->row_ptr; B.idx = b->col_idx; B.val = (const double *)b->val;
     int sms = 0;
     NA_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    launch_check_sorted(B, flags + 3, s, sms);
-    launch_row_minmax(B, bmin, bmax, s, sms);
+    launch_row_minmax(B, bmin, bmax, flags + 3, s, sms);
     // Analysis: products per row, symbolic bins, row lists.
     launch_row_products(A, B.ptr, bmin, bmax, ri, symBin, flags, Tuning{}, s, sms);
     Binning sb{symBin, symList, hist, symTileOff, symStart};
@@ -212,7 +214,9 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     sa.list = symList;
     sa.binStart = symStart;
     sa.rowNnz = rowNnz;
-    sa.ctr = nullptr;
+    sa.ctr = ctrs;
+    sa.numSms = sms;
+    sa.bSorted = hflags[3] ? 0 : 1;
     sa.err = flags;
     sa.rowLo = ri.lo;
     sa.rowP = ri.rowP;
@@ -252,6 +256,7 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     na.err = flags;
     na.rowP = rowP;
     na.rowLo = ri.lo;
+    na.numSms = sms;
     na.rowHi = ri.hi;
     for (int bin = NB_TINY; bin < NB_COUNT; ++bin)
         launch_numeric_bin(na, bin, numStart_h[bin], numStart_h[bin + 1], s, &launches);

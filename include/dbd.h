@@ -126,7 +126,7 @@ typedef struct {
     int64_t blocks_per_category[3]; /* 0 dense, 1 light, 2 either (distributeWorkload.cpp:266-270) */
     int64_t rows_per_bin[DBD_NUM_BINS];   /* numeric bins: empty, tiny, warp rank, warp hash, CTA rank (shared),
                                              CTA rank (in place), CTA hash S, CTA hash L, dense windows,
-                                             warp dense window */
+                                             warp dense window, warp rank window */
     int64_t sym_rows_per_bin[DBD_NUM_BINS]; /* symbolic bins: empty, tiny, warp flags, warp hash, CTA hash, CTA bitmap */
     int64_t bytes_d2h;
     int64_t bytes_written;
@@ -298,7 +298,10 @@ int dbd_spgemm_batched(dbd_ctx *ctx, int64_t count, const dbd_csr_view *a, const
  *   sym_hash_span_words    symbolic rows with at most 4096 products hash
  *                          (instead of a bitmap) above this span (>= 0)
  *   dense_warp_span_words  numeric rows whose window spans at most this many
- *                          words accumulate in one warp's dense window (0..16) */
+ *                          words accumulate in one warp's dense window (0..16)
+ *   mid_span_words         numeric rows of at most warp_max_nnz entries whose
+ *                          window spans at most this many words use one warp's
+ *                          rank window instead of a hash table (0..2048) */
 typedef struct {
     int32_t warp_span_words;
     int32_t warp_max_nnz;
@@ -307,6 +310,7 @@ typedef struct {
     int32_t rank_shared_max_nnz;
     int32_t sym_hash_span_words;
     int32_t dense_warp_span_words;
+    int32_t mid_span_words;
 } dbd_tuning;
 
 int dbd_get_tuning(const dbd_ctx *ctx, dbd_tuning *t);

@@ -147,8 +147,59 @@ def test_every_numeric_bin_exercised(ctx, orc):
         check(res.C, A, B, orc)
         used |= set(bins_used(res.stats))
         sym_used |= {i for i, v in enumerate(res.stats["sym_rows_per_bin"]) if v}
-    assert used >= set(range(1, 10)), used
+    assert used >= set(range(1, 11)), used
     assert sym_used >= set(range(1, 6)), sym_used
+
+
+def shuffled_rows(rng, M):
+    """M with every row's entries in random order (B rows not ascending)."""
+    idx, val = M.col_idx.copy(), M.val.copy()
+    for r in range(M.n_rows):
+        s, e = M.row_ptr[r], M.row_ptr[r + 1]
+        p = rng.permutation(e - s)
+        idx[s:e], val[s:e] = idx[s:e][p], val[s:e][p]
+    return CSR(M.n_rows, M.n_cols, M.row_ptr, idx, val)
+
+
+def test_narrow_rows_every_enumeration(ctx, orc):
+    """Narrow rows (warp flag and dense-window kernels) through each path:
+    contiguous B rows (banded: flagged a word at a time), long B rows with
+    gaps (row-wise, a column at a time), short B rows (flattened), and B rows
+    out of column order (row-wise with atomics)."""
+    rng = np.random.default_rng(21)
+    band = gen.banded(1500, 24, seed=5)
+    gappy = random_band(rng, 1500, 20, 40)
+    short = random_band(rng, 1500, 3, 40)
+    for A, B in ((band, band), (gappy, gappy), (gappy, short), (band, shuffled_rows(rng, band)),
+                 (gappy, shuffled_rows(rng, gappy))):
+        res = ctx.spgemm(A, B, scope="kernel")
+        check(res.C, A, B, orc)
+        assert res.stats["sym_rows_per_bin"][2] > 0 and res.stats["rows_per_bin"][9] > 0
+
+
+def test_dense_rows_long_and_thin_b_rows(ctx, orc):
+    """Dense-window rows both ways: B rows of 2,000 consecutive columns (many
+    products per entry and window: one warp per entry) and B rows of a few
+    scattered columns over 600,000 (one thread per entry)."""
+    rng = np.random.default_rng(8)
+    n = 600_000
+    k = 400
+    starts = (np.arange(k) * 1487) % (n - 2000)
+    rows = np.repeat(np.arange(k), 2000)
+    cols = (starts[:, None] + np.arange(2000)[None, :]).ravel()
+    B_long = gen._from_coo(k, n, rows, cols, rng.uniform(-1, 1, rows.size))
+    A_long = gen.uniform_rows(48, 60, seed=4, n_cols=k, dist="uniform")
+    B_thin = gen.uniform_rows(4000, 5, seed=3, n_cols=n, dist="uniform")
+    A_thin = gen.uniform_rows(48, 1000, seed=5, n_cols=4000, dist="uniform")
+    for A, B in ((A_long, B_long), (A_thin, B_thin)):
+        res = ctx.spgemm(A, B, scope="kernel")
+        check(res.C, A, B, orc)
+        assert res.stats["rows_per_bin"][8] > 0  # dense bin (global slots)
+    # A budget too small for global slots: the shared-memory windows instead.
+    with dbd.Context(cpu_gib=4, gpu_gib=0.5) as small:
+        for A, B in ((A_long, B_long), (A_thin, B_thin)):
+            res = small.spgemm(A, B, scope="kernel")
+            check(res.C, A, B, orc)
 
 
 def test_dense_rows_unsorted_b(ctx, orc):
