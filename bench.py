@@ -707,6 +707,7 @@ def main():
     ap.add_argument("--no-io", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tune", default="", help="explicit thresholds, e.g. rank_shared_max_nnz=512 (no autotuning)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -760,7 +761,11 @@ def main():
         return c.distribute_Workload("kernel")
 
     tuned = None
-    if not args.no_autotune:
+    if args.tune:
+        tuned = {k: int(v) for k, v in (kv.split("=") for kv in args.tune.split(","))}
+        ctx.set_tuning(**tuned)
+        tuned = ctx.tuning
+    elif not args.no_autotune:
         tuned, tune_ms = ctx.autotune(repeats=2)
     for _ in range(args.warmup):
         step()
@@ -838,7 +843,7 @@ def main():
                        "rows_per_block": rpb, "scope": "kernel (inputs resident in HBM, C left in HBM)",
                        "l2": "flushed between steps (512 MiB device write outside the timed events)",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                       "tuning": ctx.tuning, "autotuned": tuned is not None},
+                       "tuning": ctx.tuning, "autotuned": tuned is not None and not args.tune},
             "gpu_launches": launches,
             "roofline": roof,
             "wall_s": round(t_wall, 3)}

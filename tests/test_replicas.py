@@ -33,7 +33,7 @@ def worker(rank, world, port, times, out):
 def test_slowest_rank_sets_the_job_time():
     world = 2
     times = [0.25, 0.5]
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.start_processes(worker, args=(world, free_port(), times, out), nprocs=world, start_method="spawn")
     for rank in range(world):
         t, rate = out[rank]
