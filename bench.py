@@ -52,7 +52,8 @@ def make_workload(name):
     if name == "laplacian256":
         return gen.laplacian_2d(256)
     if name.startswith("rmat"):
-        return gen.rmat(int(name[4:]), 8, seed=0)
+        scale, _, ef = name[4:].partition("e")  # rmat<scale>[e<edge factor>]
+        return gen.rmat(int(scale), int(ef or 8), seed=0)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -707,6 +708,7 @@ def main():
     ap.add_argument("--no-io", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--gpu-gib", type=float, default=200.0, help="device budget of the multiply (kernel scope)")
     ap.add_argument("--tune", default="", help="explicit thresholds, e.g. rank_shared_max_nnz=512 (no autotuning)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -750,7 +752,7 @@ def main():
     D = CSR.from_device(A.n_rows, A.n_cols, A.nnz, tp.data_ptr(), ti.data_ptr(), tv.data_ptr())
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
 
-    ctx = dbd.Context(cpu_gib=96, gpu_gib=200, rows_per_block=rpb, device=local)
+    ctx = dbd.Context(cpu_gib=96, gpu_gib=args.gpu_gib, rows_per_block=rpb, device=local)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
     ctx.initialize_A(D)
@@ -805,7 +807,7 @@ def main():
     sym, num = bins(A, rowP, nnz_r, span_words(A), ctx.tuning)
     bins_match = bool(np.array_equal(np.bincount(num, minlength=12)[:12], np.array(stats[-1]["rows_per_bin"])))
     kb = kernel_bytes(A, rowP, nnz_r, sym, num)
-    pctx = dbd.Context(cpu_gib=96, gpu_gib=200, rows_per_block=rpb, device=local, time_kernels=True)
+    pctx = dbd.Context(cpu_gib=96, gpu_gib=args.gpu_gib, rows_per_block=rpb, device=local, time_kernels=True)
     pctx.set_stream(stream.cuda_stream)
     pctx.initialize_A(D)
     pctx.initialize_B(D)
