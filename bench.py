@@ -397,7 +397,10 @@ def run_batched(args, local):
     batched = lambda: ctx.spgemm_batched(dA, dB, scope="kernel", fetch=False)
     t_default, _ = timed(batched, max(1, min(args.steps, 3)), 1)
     tuned = None
-    if not args.no_autotune:
+    if args.tune:
+        ctx.set_tuning(**{k: int(v) for k, v in (kv.split("=") for kv in args.tune.split(","))})
+        tuned = ctx.tuning
+    elif not args.no_autotune:
         tuned, _ = ctx.autotune(repeats=1)
     with Clocks(local) as clk:
         t_batch, res = timed(batched, args.steps, args.warmup)

@@ -720,12 +720,90 @@ __device__ __forceinline__ void group_bitonic(uint64_t *buf, int N, int gt) {
     }
 }
 
+// One warp orders n <= kBucketN packed (column << 32 | slot) entries of a
+// row whose columns lie in [lo, lo + span): a counting sort by bucket
+// (256 buckets of equal column width, each lane owning 8), then insertion
+// sort inside each bucket.  Rows of uniform columns put a few entries in
+// each bucket, so this costs a few operations per entry instead of a
+// bitonic network.  Returns false (nothing written) when a bucket holds
+// more than 32 entries (clustered columns); the caller sorts otherwise.
+constexpr int kBuckets = 256;
+__device__ __forceinline__ bool warp_bucket_order(const uint64_t *in, int n, int32_t lo, int64_t span, int *cnts,
+                                                  uint64_t *out) {
+    const int lane = threadIdx.x & 31;
+    for (int b = lane; b < kBuckets; b += 32) cnts[b] = 0;
+    __syncwarp();
+    constexpr int PER = kNumWarpMax / 32;  // entries per lane
+    uint64_t key[PER];
+    int bk[PER], rk[PER];
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int i = lane + 32 * u;
+        bk[u] = -1;
+        if (i < n) {
+            key[u] = in[i];
+            const int64_t rel = (int64_t)(int32_t)(key[u] >> 32) - lo;
+            bk[u] = (int)min((int64_t)kBuckets - 1, max((int64_t)0, rel * kBuckets / span));
+            rk[u] = atomicAdd(&cnts[bk[u]], 1);
+        }
+    }
+    __syncwarp();
+    // Lane l owns buckets [8 l, 8 l + 8): counts -> starts.
+    int c8[8], mine = 0, mx = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        c8[q] = cnts[8 * lane + q];
+        mine += c8[q];
+        mx = max(mx, c8[q]);
+    }
+#pragma unroll
+    for (int d = 16; d; d >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, d));
+    if (mx > 32) return false;
+    int incl = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d) incl += y;
+    }
+    int st = incl - mine;
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        cnts[8 * lane + q] = st;
+        st += c8[q];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < PER; ++u)
+        if (bk[u] >= 0) out[cnts[bk[u]] + rk[u]] = key[u];
+    __syncwarp();
+    // Insertion sort inside each of this lane's buckets (by column).
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int s0 = cnts[8 * lane + q], c = c8[q];
+        for (int i = 1; i < c; ++i) {
+            const uint64_t v = out[s0 + i];
+            int j = i - 1;
+            while (j >= 0 && (out[s0 + j] >> 32) > (v >> 32)) {
+                out[s0 + j + 1] = out[s0 + j];
+                --j;
+            }
+            out[s0 + j + 1] = v;
+        }
+    }
+    __syncwarp();
+    return true;
+}
+
 // Compacts the occupied slots of a (keys, vals) table into sbuf (which
 // aliases keys) as packed (column, slot) pairs, sorts them and writes the
-// row.  GROUP threads per row; all of them call.
+// row.  GROUP threads per row; all of them call.  One-warp rows pass
+// bucket buffers (cnts, bbuf) and are ordered by warp_bucket_order when
+// their columns spread evenly.
 template <int GROUP, int ROWS, int TABLE>
 __device__ __forceinline__ void table_write_sorted(NumArgs &a, int32_t row, int32_t *keys, const double *vals,
-                                                   int *gcnt, int gt) {
+                                                   int *gcnt, int gt, int *cnts = nullptr,
+                                                   uint64_t *bbuf = nullptr) {
     constexpr int KPT = TABLE / GROUP;
     constexpr int NMAX = TABLE / 2;
     const int lane = threadIdx.x & 31;
@@ -751,20 +829,36 @@ __device__ __forceinline__ void table_write_sorted(NumArgs &a, int32_t row, int3
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
     if (gt == 0 && (n != expect || n > NMAX)) raise(a.err, DEV_COUNT_MISMATCH);
     const int nn = min(n, NMAX);
-    int N = 1;
-    while (N < nn) N <<= 1;
-    for (int i = nn + gt; i < N; i += GROUP) sbuf[i] = ~0ull;
-    group_sync<GROUP, ROWS>();
-    group_bitonic<GROUP, ROWS>(sbuf, N, gt);
+    const uint64_t *sorted = sbuf;
+    bool done = false;
+    if constexpr (GROUP == 32 && ROWS > 1 && NMAX <= kNumWarpMax) {
+        if (cnts) {
+            const int32_t lo = a.rowLo[row];
+            const int64_t span = max((int64_t)1, (int64_t)a.rowHi[row] - lo + 1);
+            done = warp_bucket_order(sbuf, nn, lo, span, cnts, bbuf);
+            if (done) sorted = bbuf;
+        }
+    }
+    if (!done) {
+        int N = 1;
+        while (N < nn) N <<= 1;
+        for (int i = nn + gt; i < N; i += GROUP) sbuf[i] = ~0ull;
+        group_sync<GROUP, ROWS>();
+        group_bitonic<GROUP, ROWS>(sbuf, N, gt);
+    }
     const int64_t obase = a.Cp[row] - a.outBase;
     const int32_t shift = col_shift(a, row);
     const int wn = (int)min((int64_t)nn, expect);
     for (int i = gt; i < wn; i += GROUP) {
-        const uint64_t v = sbuf[i];
+        const uint64_t v = sorted[i];
         a.Ci[obase + i] = (int32_t)(v >> 32) - shift;
         a.Cv[obase + i] = vals[(uint32_t)v];
     }
 }
+
+// Shared bytes per warp of the warp hash kernel: keys, values, the bucket
+// order's output and counters.
+constexpr size_t warp_hash_bytes(int table) { return 12 * (size_t)table + 4 * (size_t)table + 4 * (size_t)kBuckets; }
 
 // Warp hash rows: keys int32[TABLE] then values double[TABLE] per row.
 template <int ROWS, int TABLE>
@@ -774,9 +868,11 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t 
     const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t item = (int64_t)blockIdx.x * ROWS + g;
     if (item >= count) return;
-    unsigned char *base_ptr = smem + (size_t)g * (12 * (size_t)TABLE);
+    unsigned char *base_ptr = smem + (size_t)g * warp_hash_bytes(TABLE);
     int32_t *keys = reinterpret_cast<int32_t *>(base_ptr);
     double *vals = reinterpret_cast<double *>(base_ptr + 4 * (size_t)TABLE);
+    uint64_t *bbuf = reinterpret_cast<uint64_t *>(base_ptr + 12 * (size_t)TABLE);
+    int *cnts = reinterpret_cast<int *>(bbuf + TABLE / 2);
     const int32_t row = a.list[lo + item];
     for (int i = lane; i < TABLE; i += 32) {
         keys[i] = EMPTY;
@@ -798,7 +894,7 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t 
         }
     }
     __syncwarp();
-    table_write_sorted<32, ROWS, TABLE>(a, row, keys, vals, &gcnt[g], lane);
+    table_write_sorted<32, ROWS, TABLE>(a, row, keys, vals, &gcnt[g], lane, cnts, bbuf);
 }
 
 // CTA hash rows: one CTA per row, products spread over all threads.
@@ -1608,7 +1704,7 @@ constexpr int kDenseStage = 1024;  // entries whose cursors stay in shared memor
 constexpr int kWideThreads = 512;
 constexpr size_t kSmemSymWarp = (size_t)kSymWarpRows * kSymWarpTable * 4;
 constexpr size_t kSmemSymCta = StageLayout<kSymCtaThreads>::bytes + (size_t)kSymCtaTable * 4;
-constexpr size_t kSmemNumWarp = (size_t)kNumWarpRows * kNumWarpTable * 12;
+constexpr size_t kSmemNumWarp = (size_t)kNumWarpRows * warp_hash_bytes(kNumWarpTable);
 constexpr size_t kSmemNumCtaS = StageLayout<kNumCtaSThreads>::bytes + (size_t)kNumCtaSTable * 12;
 constexpr size_t kSmemNumCtaL = StageLayout<kNumCtaLThreads>::bytes + (size_t)kNumCtaLTable * 12;
 constexpr size_t kSmemDense = (size_t)kDenseWindow * 8 + kDenseWindow / 8 + (size_t)kDenseStage * 8;
