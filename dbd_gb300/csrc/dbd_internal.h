@@ -66,7 +66,8 @@ struct Tuning {
     int32_t rankSharedMax = kNumCtaLMax;      // rank rows accumulating in shared memory
     int32_t symHashSpanWords = kWideHashSpanWords;  // symbolic CTA rows hash above this span
     int32_t denseWarpWords = kDenseWarpWords; // numeric rows on one warp's dense window
-    int32_t midSpanWords = kMidSpanWords;     // numeric rows on one warp's rank window
+    int32_t midSpanWords = 0;                 // numeric rows on one warp's rank window (off: the
+                                              // bucket-sorted warp hash measures faster)
 };
 
 __host__ __device__ __forceinline__ uint8_t sym_bin_of(int64_t P, int32_t nA, int sw, const Tuning &t) {
