@@ -455,7 +455,7 @@ __device__ __forceinline__ int or_bits_count(uint32_t *bm, bool v, uint32_t rel,
     }
     if (!head) return 0;
     const uint32_t old = atomicOr(&bm[w], acc);
-    if (old == 0u) {
+    if (cap > 0 && old == 0u) {
         const int k = atomicAdd(nt, 1);
         if (k < cap) touched[k] = w;
     }
@@ -500,10 +500,13 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
         const int sw = span_words(rlo, rhi);
         const int64_t base = (int64_t)(rlo >> 5) << 5;
         const int64_t end = (int64_t)rhi + 1;
+        // Rows with more products than the list holds touch more words than
+        // it holds as a rule: they skip the bookkeeping and clear in full.
+        const int rowCap = a.rowP[row] <= cap ? cap : 0;
         int cnt = 0;
         for (int64_t c_lo = base; c_lo < end; c_lo += winBits) {
             const int words = (int)min((int64_t)winBits, end - c_lo + 31) >> 5;
-            if (tid == 0) nt = 0;
+            if (tid == 0) nt = rowCap ? 0 : cap + 1;
             __syncthreads();
             for (int32_t eb = e0; eb < e1; eb += THREADS) {
                 int nb;
@@ -514,14 +517,14 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
                 warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
                     const int64_t rel = v ? (int64_t)a.B.idx[pos] - c_lo : -1;
                     const bool in = rel >= 0 && rel < winBits;
-                    cnt += or_bits_count(bm, in, in ? (uint32_t)rel : 0u, touched, &nt, cap);
+                    cnt += or_bits_count(bm, in, in ? (uint32_t)rel : 0u, touched, &nt, rowCap);
                 });
                 __syncthreads();
             }
             if (a.wideBits && sw <= kRankWordsMax) {
                 // One window covers the row here; keep its bitmap for the numeric pass.
                 uint32_t *dst = a.wideBits + (size_t)item * kRankWordsMax;
-                for (int i = tid; i < sw; i += THREADS) dst[i] = bm[i];
+                for (int i = tid; i < sw; i += THREADS) __stcs(&dst[i], bm[i]);
                 if (tid == 0) a.wideSlot[row] = item;
                 __syncthreads();
             }
@@ -969,7 +972,7 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
     if (a.wideBits && sym_bin_of(a.rowP[row], e1 - e0, nwords, a.tune) == SB_WIDE) {
         // The symbolic pass kept this row's bitmap.
         const uint32_t *src = a.wideBits + (size_t)a.wideSlot[row] * kRankWordsMax;
-        for (int i = tid; i < nwords; i += THREADS) bits[i] = src[i];
+        for (int i = tid; i < nwords; i += THREADS) bits[i] = __ldcs(&src[i]);
         __syncthreads();
     } else {
         for (int i = tid; i < nwords; i += THREADS) bits[i] = 0u;
@@ -1020,7 +1023,7 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
         while (word) {
             const int b = __ffs(word) - 1;
             word &= word - 1u;
-            if (p < expect) a.Ci[obase + p] = obc + (w << 5) + b;
+            if (p < expect) __stcs(&a.Ci[obase + p], obc + (w << 5) + b);
             ++p;
         }
     }
