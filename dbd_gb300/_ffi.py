@@ -47,7 +47,7 @@ class Tuning(C.Structure):
     _fields_ = [("warp_span_words", C.c_int32), ("warp_max_nnz", C.c_int32), ("sym_warp_max_products", C.c_int32),
                 ("rank_words_max", C.c_int32), ("rank_shared_max_nnz", C.c_int32),
                 ("sym_hash_span_words", C.c_int32), ("dense_warp_span_words", C.c_int32),
-                ("mid_span_words", C.c_int32)]
+                ("mid_span_words", C.c_int32), ("dense_method", C.c_int32)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

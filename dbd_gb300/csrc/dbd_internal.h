@@ -68,6 +68,7 @@ struct Tuning {
     int32_t denseWarpWords = kDenseWarpWords; // numeric rows on one warp's dense window
     int32_t midSpanWords = 0;                 // numeric rows on one warp's rank window (off: the
                                               // bucket-sorted warp hash measures faster)
+    int32_t denseMethod = 0;                  // dense bin: 0 rank windows, 1 global slots, 2 FP64 windows
 };
 
 __host__ __device__ __forceinline__ uint8_t sym_bin_of(int64_t P, int32_t nA, int sw, const Tuning &t) {
@@ -104,6 +105,7 @@ inline Tuning clamp_tuning(Tuning t) {
     t.symHashSpanWords = cl(t.symHashSpanWords, 0, 1 << 26);
     t.denseWarpWords = cl(t.denseWarpWords, 0, kDenseWarpWords);
     t.midSpanWords = cl(t.midSpanWords, 0, kMidSpanWords);
+    t.denseMethod = cl(t.denseMethod, 0, 2);
     return t;
 }
 

@@ -705,7 +705,7 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     // Global dense slots for the dense bin: up to two per SM, within an
     // eighth of the GPU budget; too few fit -> shared-memory windows.
     c->gSlots = 0;
-    if (c->numStart_h[NB_DENSE + 1] > c->numStart_h[NB_DENSE]) {
+    if (c->tune.denseMethod == 1 && c->numStart_h[NB_DENSE + 1] > c->numStart_h[NB_DENSE]) {
         const int64_t stride = (c->ncols + 1023) / 1024 * 1024;
         const size_t slot = gdense_slot_bytes(stride);
         const int64_t fit = (int64_t)(c->cfg.gpu_gib * kGiB / 8 / (double)slot);
@@ -1481,6 +1481,7 @@ int dbd_get_tuning(const dbd_ctx *c, dbd_tuning *t) {
     t->sym_hash_span_words = c->tune.symHashSpanWords;
     t->dense_warp_span_words = c->tune.denseWarpWords;
     t->mid_span_words = c->tune.midSpanWords;
+    t->dense_method = c->tune.denseMethod;
     return DBD_OK;
 }
 
@@ -1495,6 +1496,7 @@ int dbd_set_tuning(dbd_ctx *c, const dbd_tuning *t) {
     u.symHashSpanWords = t->sym_hash_span_words;
     u.denseWarpWords = t->dense_warp_span_words;
     u.midSpanWords = t->mid_span_words;
+    u.denseMethod = t->dense_method;
     const Tuning v = clamp_tuning(u);
     if (memcmp(&u, &v, sizeof(u)) != 0) return set_err(c, DBD_ERR_INVALID, "a tuning value is out of its range");
     c->tune = u;
@@ -1534,6 +1536,7 @@ int dbd_autotune(dbd_ctx *c, int repeats, dbd_tuning *best, double *best_ms) {
         {&Tuning::symHashSpanWords, {512, 2048, 8192}},
         {&Tuning::denseWarpWords, {0, 4, 8, 16}},
         {&Tuning::midSpanWords, {0, 256, 1024, 2048}},
+        {&Tuning::denseMethod, {0, 1, 2}},
     };
     const Tuning start = c->tune;
     Tuning cur = start;

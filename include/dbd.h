@@ -301,7 +301,10 @@ int dbd_spgemm_batched(dbd_ctx *ctx, int64_t count, const dbd_csr_view *a, const
  *                          words accumulate in one warp's dense window (0..16)
  *   mid_span_words         numeric rows of at most warp_max_nnz entries whose
  *                          window spans at most this many words use one warp's
- *                          rank window instead of a hash table (0..2048) */
+ *                          rank window instead of a hash table (0..2048)
+ *   dense_method           rows of the dense bin: 0 rank windows of 2^20 columns in
+ *                          shared memory, 1 rank over the whole row in global slots,
+ *                          2 FP64 windows of 8192 columns swept by cursors */
 typedef struct {
     int32_t warp_span_words;
     int32_t warp_max_nnz;
@@ -311,6 +314,7 @@ typedef struct {
     int32_t sym_hash_span_words;
     int32_t dense_warp_span_words;
     int32_t mid_span_words;
+    int32_t dense_method;
 } dbd_tuning;
 
 int dbd_get_tuning(const dbd_ctx *ctx, dbd_tuning *t);

@@ -198,12 +198,17 @@ def test_dense_rows_long_and_thin_b_rows(ctx, orc):
     A_long = gen.uniform_rows(48, 60, seed=4, n_cols=k, dist="uniform")
     B_thin = gen.uniform_rows(4000, 5, seed=3, n_cols=n, dist="uniform")
     A_thin = gen.uniform_rows(48, 1000, seed=5, n_cols=4000, dist="uniform")
-    for A, B in ((A_long, B_long), (A_thin, B_thin)):
-        res = ctx.spgemm(A, B, scope="kernel")
-        check(res.C, A, B, orc)
-        assert res.stats["rows_per_bin"][8] > 0  # dense bin (global slots)
-    # A budget too small for global slots: the shared-memory windows instead.
+    # Every method of the dense bin: rank windows, global slots, FP64 windows.
+    for method in (0, 1, 2):
+        with dbd.Context(cpu_gib=8, gpu_gib=16) as c:
+            c.set_tuning(dense_method=method)
+            for A, B in ((A_long, B_long), (A_thin, B_thin)):
+                res = c.spgemm(A, B, scope="kernel")
+                check(res.C, A, B, orc)
+                assert res.stats["rows_per_bin"][8] > 0  # the dense bin
+    # Global slots without room for them (a small budget): FP64 windows.
     with dbd.Context(cpu_gib=4, gpu_gib=0.5) as small:
+        small.set_tuning(dense_method=1)
         for A, B in ((A_long, B_long), (A_thin, B_thin)):
             res = small.spgemm(A, B, scope="kernel")
             check(res.C, A, B, orc)

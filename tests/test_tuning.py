@@ -11,11 +11,13 @@ pytestmark = pytest.mark.gpu
 
 EXTREMES = [
     dict(warp_span_words=1, warp_max_nnz=1, sym_warp_max_products=32, rank_words_max=1, rank_shared_max_nnz=1,
-         sym_hash_span_words=0, dense_warp_span_words=0, mid_span_words=0),
+         sym_hash_span_words=0, dense_warp_span_words=0, mid_span_words=0, dense_method=1),
     dict(warp_span_words=64, warp_max_nnz=256, sym_warp_max_products=512, rank_words_max=8192,
-         rank_shared_max_nnz=4096, sym_hash_span_words=1 << 26, dense_warp_span_words=16, mid_span_words=2048),
+         rank_shared_max_nnz=4096, sym_hash_span_words=1 << 26, dense_warp_span_words=16, mid_span_words=2048,
+         dense_method=2),
     dict(warp_span_words=8, warp_max_nnz=64, sym_warp_max_products=128, rank_words_max=1024,
-         rank_shared_max_nnz=512, sym_hash_span_words=512, dense_warp_span_words=4, mid_span_words=100),
+         rank_shared_max_nnz=512, sym_hash_span_words=512, dense_warp_span_words=4, mid_span_words=100,
+         dense_method=0),
 ]
 
 
@@ -36,7 +38,7 @@ def test_out_of_range_tuning_refused(ctx):
     before = ctx.tuning
     for k, v in [("warp_span_words", 65), ("warp_max_nnz", 0), ("sym_warp_max_products", 513),
                  ("rank_words_max", 8193), ("rank_shared_max_nnz", 4097), ("sym_hash_span_words", -1),
-                 ("dense_warp_span_words", 17), ("mid_span_words", 2049)]:
+                 ("dense_warp_span_words", 17), ("mid_span_words", 2049), ("dense_method", 3)]:
         with pytest.raises(dbd.DBDError):
             ctx.set_tuning(**{k: v})
     assert ctx.tuning == before
