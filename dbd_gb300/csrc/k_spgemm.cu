@@ -1814,7 +1814,8 @@ constexpr int kNumCtaSThreads = 256;
 constexpr int kNumCtaLThreads = 512;
 constexpr int kDenseThreads = 512;
 constexpr int kDenseStage = 1024;  // entries whose cursors stay in shared memory
-constexpr int kWideThreads = 512;
+constexpr int kWideThreads = 512;       // several CTAs per SM (windows up to 2^18 columns)
+constexpr int kWideThreadsBig = 1024;   // one CTA per SM (a 2^20-column window fills shared memory)
 constexpr size_t kSmemSymWarp = (size_t)kSymWarpRows * kSymWarpTable * 4;
 constexpr size_t kSmemSymCta = StageLayout<kSymCtaThreads>::bytes + (size_t)kSymCtaTable * 4;
 constexpr size_t kSmemNumWarp = (size_t)kNumWarpRows * warp_hash_bytes(kNumWarpTable);
@@ -1830,7 +1831,7 @@ constexpr int kBitwRows = 8;
 constexpr int kRankwRows = 8;
 constexpr int kDensewRows = 8;
 constexpr int kGdenseThreads = 512;
-constexpr int kRankWinThreads = 512;
+constexpr int kRankWinThreads = 1024;  // one CTA per SM: all its warps
 constexpr int kRankWinWords = 32768;  // 2^20 columns per window
 constexpr size_t kSmemRankWin = StageLayout<kRankWinThreads>::bytes + 6 * (size_t)kRankWinWords +
                                 4 * (size_t)(kRankWinWords / 256);
@@ -1848,6 +1849,8 @@ void init_kernel_attributes() {
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemSymCta);
     cudaFuncSetAttribute(k_sym_wide<kWideThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(kSmemWideBase + kWideWindowBitsMax / 8 + 4 * (size_t)kWideTouchMax));
+    cudaFuncSetAttribute(k_sym_wide<kWideThreadsBig>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(StageLayout<kWideThreadsBig>::bytes + kWideWindowBitsMax / 8 + 4 * (size_t)kWideTouchMax));
     cudaFuncSetAttribute(k_num_hash_warp<kNumWarpRows, kNumWarpTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumWarp);
     cudaFuncSetAttribute(k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>,
@@ -1905,6 +1908,14 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
             // and touch list keep one per SM), rows taken from a counter.
             const int wb = wide_window_bits(a.B.n);
             const size_t smem = kSmemWideBase + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb);
+            if (smem > 110 * 1024) {
+                // Only one CTA fits on an SM: give it all the SM's warps.
+                const size_t smemBig =
+                    StageLayout<kWideThreadsBig>::bytes + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb);
+                const int gridBig = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1));
+                k_sym_wide<kWideThreadsBig><<<(unsigned)gridBig, kWideThreadsBig, smemBig, s>>>(a, begin, n, wb);
+                break;
+            }
             const int per_sm = std::max(1, std::min(2048 / kWideThreads, (int)((227 * 1024) / (smem + 1024))));
             const int grid = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1) * per_sm);
             k_sym_wide<kWideThreads><<<(unsigned)grid, kWideThreads, smem, s>>>(a, begin, n, wb);
