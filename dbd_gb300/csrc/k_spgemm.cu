@@ -501,8 +501,11 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
         const int64_t base = (int64_t)(rlo >> 5) << 5;
         const int64_t end = (int64_t)rhi + 1;
         // Rows with more products than the list holds touch more words than
-        // it holds as a rule: they skip the bookkeeping and clear in full.
+        // it holds as a rule: they set their bits with plain ORs (no old
+        // values, no bookkeeping) and count, keep and clear the window in one
+        // sweep over its words.
         const int rowCap = a.rowP[row] <= cap ? cap : 0;
+        const bool keep = a.wideBits && sw <= kRankWordsMax;
         int cnt = 0;
         for (int64_t c_lo = base; c_lo < end; c_lo += winBits) {
             const int words = (int)min((int64_t)winBits, end - c_lo + 31) >> 5;
@@ -514,14 +517,33 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
                     stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
-                warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-                    const int64_t rel = v ? (int64_t)a.B.idx[pos] - c_lo : -1;
-                    const bool in = rel >= 0 && rel < winBits;
-                    cnt += or_bits_count(bm, in, in ? (uint32_t)rel : 0u, touched, &nt, rowCap);
-                });
+                if (rowCap) {
+                    warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
+                        const int64_t rel = v ? (int64_t)a.B.idx[pos] - c_lo : -1;
+                        const bool in = rel >= 0 && rel < winBits;
+                        cnt += or_bits_count(bm, in, in ? (uint32_t)rel : 0u, touched, &nt, rowCap);
+                    });
+                } else {
+                    warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
+                        const int64_t rel = v ? (int64_t)a.B.idx[pos] - c_lo : -1;
+                        if (rel >= 0 && rel < winBits) atomicOr(&bm[rel >> 5], 1u << (rel & 31));
+                    });
+                }
                 __syncthreads();
             }
-            if (a.wideBits && sw <= kRankWordsMax) {
+            if (!rowCap) {
+                uint32_t *dst = keep ? a.wideBits + (size_t)item * kRankWordsMax : nullptr;
+                for (int i = tid; i < words; i += THREADS) {
+                    const uint32_t x = bm[i];
+                    cnt += __popc(x);
+                    if (dst) __stcs(&dst[i], x);
+                    bm[i] = 0u;
+                }
+                if (keep && tid == 0) a.wideSlot[row] = item;
+                __syncthreads();
+                continue;
+            }
+            if (keep) {
                 // One window covers the row here; keep its bitmap for the numeric pass.
                 uint32_t *dst = a.wideBits + (size_t)item * kRankWordsMax;
                 for (int i = tid; i < sw; i += THREADS) __stcs(&dst[i], bm[i]);
