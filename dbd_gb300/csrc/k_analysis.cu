@@ -49,17 +49,33 @@ __global__ void k_row_minmax(CsrDev B, int32_t *__restrict__ bmin, int32_t *__re
 
 // Products per row, P_r = sum over k in A_r of |B_k|, and the row's column
 // window [lo, hi] from the B rows' first and last columns.  Eight lanes per
-// row.
-__global__ void k_row_products(CsrDev A, const int32_t *__restrict__ Bp, const int32_t *__restrict__ bmin,
-                               const int32_t *__restrict__ bmax, RowInfo ri, uint8_t *__restrict__ symBin,
-                               int *err, Tuning tune) {
-    const int lane = threadIdx.x & 31;
+// row; rows of more than kLongRow entries (power-law hubs, whose serial walk
+// by eight lanes would set the kernel's duration) are left to a second
+// stage in which a whole CTA takes each of them.
+constexpr int kLongRow = 256;
+
+__device__ __forceinline__ void row_products_out(const CsrDev &A, int64_t row, int64_t sum, int32_t lo, int32_t hi,
+                                                 RowInfo &ri, uint8_t *symBin, int *err, const Tuning &tune) {
+    const int32_t n = A.ptr[row + 1] - A.ptr[row];
+    ri.rowP[row] = sum;
+    ri.lo[row] = lo;
+    ri.hi[row] = hi;
+    symBin[row] = sym_bin_of(sum, n, span_words(lo, hi), tune);
+    if (sum > 0x7fffffffLL) atomicCAS(err, 0, (int)DEV_ROW_TOO_LONG);
+}
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_row_products(CsrDev A, const int32_t *__restrict__ Bp,
+                                                          const int32_t *__restrict__ bmin,
+                                                          const int32_t *__restrict__ bmax, RowInfo ri,
+                                                          uint8_t *__restrict__ symBin, int *err, Tuning tune) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int sub = lane & 7;
     const unsigned gmask = 0xffu << (lane & 24);
-    int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 3;
-    const int64_t stride = ((int64_t)gridDim.x * blockDim.x) >> 3;
-    for (; row < A.m; row += stride) {
+    const int64_t stride = ((int64_t)gridDim.x * THREADS) >> 3;
+    for (int64_t row = (blockIdx.x * (int64_t)THREADS + tid) >> 3; row < A.m; row += stride) {
         const int32_t s = A.ptr[row], e = A.ptr[row + 1];
+        if (e - s > kLongRow) continue;  // the whole group skips together
         int64_t sum = 0;
         int32_t lo = INT32_MAX, hi = -1;
         for (int32_t i = s + sub; i < e; i += 8) {
@@ -74,12 +90,54 @@ __global__ void k_row_products(CsrDev A, const int32_t *__restrict__ Bp, const i
             lo = min(lo, __shfl_xor_sync(gmask, lo, d, 8));
             hi = max(hi, __shfl_xor_sync(gmask, hi, d, 8));
         }
-        if (sub == 0) {
-            ri.rowP[row] = sum;
-            ri.lo[row] = lo;
-            ri.hi[row] = hi;
-            symBin[row] = sym_bin_of(sum, e - s, span_words(lo, hi), tune);
-            if (sum > 0x7fffffffLL) atomicCAS(err, 0, (int)DEV_ROW_TOO_LONG);
+        if (sub == 0) row_products_out(A, row, sum, lo, hi, ri, symBin, err, tune);
+    }
+
+    // Long rows: each CTA finds them in its tiles of THREADS rows and takes
+    // them one by one with all its threads.
+    __shared__ int32_t longRows[THREADS];
+    __shared__ int nLong;
+    __shared__ int64_t rs[THREADS / 32];
+    __shared__ int32_t rlo[THREADS / 32], rhi[THREADS / 32];
+    for (int64_t t0 = (int64_t)blockIdx.x * THREADS; t0 < A.m; t0 += (int64_t)gridDim.x * THREADS) {
+        if (tid == 0) nLong = 0;
+        __syncthreads();
+        const int64_t row = t0 + tid;
+        if (row < A.m && A.ptr[row + 1] - A.ptr[row] > kLongRow) longRows[atomicAdd(&nLong, 1)] = (int32_t)row;
+        __syncthreads();
+        const int nl = nLong;
+        for (int j = 0; j < nl; ++j) {
+            const int32_t r = longRows[j];
+            const int32_t s = A.ptr[r], e = A.ptr[r + 1];
+            int64_t sum = 0;
+            int32_t lo = INT32_MAX, hi = -1;
+            for (int32_t i = s + tid; i < e; i += THREADS) {
+                const int32_t k = A.idx[i];
+                sum += (int64_t)(Bp[k + 1] - Bp[k]);
+                lo = min(lo, bmin[k]);
+                hi = max(hi, bmax[k]);
+            }
+#pragma unroll
+            for (int d = 16; d; d >>= 1) {
+                sum += __shfl_xor_sync(FULL, sum, d);
+                lo = min(lo, __shfl_xor_sync(FULL, lo, d));
+                hi = max(hi, __shfl_xor_sync(FULL, hi, d));
+            }
+            if (lane == 0) {
+                rs[warp] = sum;
+                rlo[warp] = lo;
+                rhi[warp] = hi;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                for (int w = 1; w < THREADS / 32; ++w) {
+                    sum += rs[w];
+                    lo = min(lo, rlo[w]);
+                    hi = max(hi, rhi[w]);
+                }
+                row_products_out(A, r, sum, lo, hi, ri, symBin, err, tune);
+            }
+            __syncthreads();
         }
     }
 }
@@ -326,10 +384,10 @@ void launch_row_products(const CsrDev &A, const int32_t *Bp, const int32_t *bmin
                          const RowInfo &ri, uint8_t *symBin, int *err, const Tuning &t, cudaStream_t s,
                          int num_sms) {
     if (A.m == 0) return;
-    const int threads = 256;
+    constexpr int threads = 256;
     const int64_t need = ceil_div(A.m * 8, threads);
     const int grid = (int)std::min<int64_t>(need, (int64_t)num_sms * 8);
-    k_row_products<<<grid, threads, 0, s>>>(A, Bp, bmin, bmax, ri, symBin, err, t);
+    k_row_products<threads><<<grid, threads, 0, s>>>(A, Bp, bmin, bmax, ri, symBin, err, t);
 }
 
 void launch_block_products(int64_t m, const int64_t *rowP, int64_t rows_per_block, int64_t *blockP,

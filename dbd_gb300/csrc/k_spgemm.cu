@@ -230,20 +230,23 @@ __device__ __forceinline__ int find_entry(const int32_t *pre, int nb, int32_t t)
 
 // One warp walks products [tb, te) of a staged batch, 32 per step, calling
 // f(valid, pos, e) on every lane (pos = position in B, e = staged entry;
-// meaningful when valid).  Each lane finds its entry by a 5-step shuffle
-// search among the 32 entry starts after the step's first entry.
+// meaningful when valid).  A step whose products all lie in the current
+// entry (long B rows) takes their positions from registers; otherwise each
+// lane finds its entry by a 5-step shuffle search among the 32 entry starts
+// after the step's first entry.
 template <class F>
 __device__ __forceinline__ void warp_range(const int32_t *pre, const int32_t *bst, int nb, int32_t tb,
                                            int32_t te, F &&f) {
     if (tb >= te) return;
     const int lane = threadIdx.x & 31;
     int e0 = find_entry(pre, nb, tb);
+    // Entry e0 holds products [p0, p1), starting at position b0 of B.
+    int32_t p0 = pre[e0], b0 = bst[e0], p1 = e0 + 1 < nb ? pre[e0 + 1] : INT_MAX;
     for (int32_t t0 = tb; t0 < te; t0 += 32) {
         const int32_t t = t0 + lane;
         const bool valid = t < te;
-        if (e0 + 1 >= nb || pre[e0 + 1] > t0 + 31) {
-            // All 32 products lie in entry e0 (long B rows): no search.
-            f(valid, bst[e0] + (t - pre[e0]), e0);
+        if (p1 > t0 + 31) {
+            f(valid, b0 + (t - p0), e0);
             continue;
         }
         const int ej = e0 + 1 + lane;
@@ -257,6 +260,9 @@ __device__ __forceinline__ void warp_range(const int32_t *pre, const int32_t *bs
         const int e = min(e0 + o, nb - 1);
         f(valid, bst[e] + (t - pre[e]), e);
         e0 = __shfl_sync(FULL, e, 31);
+        p0 = pre[e0];
+        b0 = bst[e0];
+        p1 = e0 + 1 < nb ? pre[e0 + 1] : INT_MAX;
     }
 }
 
