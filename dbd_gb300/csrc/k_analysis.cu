@@ -93,16 +93,18 @@ __global__ void __launch_bounds__(THREADS) k_row_products(CsrDev A, const int32_
         if (sub == 0) row_products_out(A, row, sum, lo, hi, ri, symBin, err, tune);
     }
 
-    // Long rows: each CTA finds them in its tiles of THREADS rows and takes
-    // them one by one with all its threads.
+    // Long rows: CTA b takes the long rows r with r = b (mod gridDim.x), one
+    // by one with all its threads.  Hubs sit close together in row order
+    // (power-law generators put them at small indices), so the modular
+    // assignment spreads them over the CTAs.
     __shared__ int32_t longRows[THREADS];
     __shared__ int nLong;
     __shared__ int64_t rs[THREADS / 32];
     __shared__ int32_t rlo[THREADS / 32], rhi[THREADS / 32];
-    for (int64_t t0 = (int64_t)blockIdx.x * THREADS; t0 < A.m; t0 += (int64_t)gridDim.x * THREADS) {
+    for (int64_t t0 = 0; t0 < A.m; t0 += (int64_t)gridDim.x * THREADS) {
         if (tid == 0) nLong = 0;
         __syncthreads();
-        const int64_t row = t0 + tid;
+        const int64_t row = t0 + blockIdx.x + (int64_t)gridDim.x * tid;
         if (row < A.m && A.ptr[row + 1] - A.ptr[row] > kLongRow) longRows[atomicAdd(&nLong, 1)] = (int32_t)row;
         __syncthreads();
         const int nl = nLong;
