@@ -266,6 +266,61 @@ __device__ __forceinline__ void warp_range(const int32_t *pre, const int32_t *bs
     }
 }
 
+// warp_range in groups of U steps with the loads of a group issued before
+// any is used: ld(pos) reads what a product needs from B (read-only loads),
+// use(valid, x, e) consumes it.  A warp keeps U loads in flight instead of
+// one, which hides the L2 latency of B's rows on long product runs.  use is
+// called by all lanes for each step, so it may hold warp collectives.
+template <int U, class LD, class USE>
+__device__ __forceinline__ void warp_range_ld(const int32_t *pre, const int32_t *bst, int nb, int32_t tb,
+                                              int32_t te, LD &&ld, USE &&use) {
+    if (tb >= te) return;
+    const int lane = threadIdx.x & 31;
+    int e0 = find_entry(pre, nb, tb);
+    int32_t p0 = pre[e0], b0 = bst[e0], p1 = e0 + 1 < nb ? pre[e0 + 1] : INT_MAX;
+    for (int32_t g0 = tb; g0 < te; g0 += 32 * U) {
+        int32_t pos[U];
+        int ent[U];
+        bool val[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int32_t t0 = g0 + 32 * u;
+            const int32_t t = t0 + lane;
+            val[u] = t < te;
+            ent[u] = e0;
+            pos[u] = b0 + (t - p0);
+            if (t0 >= te || p1 > t0 + 31) continue;  // past the range, or all in entry e0
+            const int ej = e0 + 1 + lane;
+            const int32_t bnd = ej <= nb ? pre[ej] : INT_MAX;
+            int o = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int32_t v = __shfl_sync(FULL, bnd, o + step - 1);
+                if (v <= t) o += step;
+            }
+            const int e = min(e0 + o, nb - 1);
+            ent[u] = e;
+            pos[u] = bst[e] + (t - pre[e]);
+            e0 = __shfl_sync(FULL, e, 31);
+            p0 = pre[e0];
+            b0 = bst[e0];
+            p1 = e0 + 1 < nb ? pre[e0 + 1] : INT_MAX;
+        }
+        using T = decltype(ld(0));
+        T x[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) x[u] = val[u] ? ld(pos[u]) : T{};
+#pragma unroll
+        for (int u = 0; u < U; ++u) use(val[u], x[u], ent[u]);
+    }
+}
+
+// Column and value of a product, as loaded by warp_range_ld.
+struct ColVal {
+    int32_t c;
+    double v;
+};
+
 // Sets one bit per lane in a shared bitmap with one atomicOr per run of
 // lanes that share a word.  Lanes whose products come from the same sorted B
 // row hold ascending columns, so equal words sit in adjacent lanes; a
@@ -468,6 +523,9 @@ __device__ __forceinline__ int or_bits_count(uint32_t *bm, bool v, uint32_t rel,
     return __popc(acc & ~old);
 }
 
+// Steps of B loads a wide-row warp keeps in flight on rows past the touch list.
+constexpr int kWideLoads = 4;
+
 // Words a wide-row window clears one by one: past a quarter of the window a
 // full clear is as cheap.
 __host__ __device__ __forceinline__ int wide_touch_cap(int winBits) {
@@ -530,10 +588,12 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
                         cnt += or_bits_count(bm, in, in ? (uint32_t)rel : 0u, touched, &nt, rowCap);
                     });
                 } else {
-                    warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-                        const int64_t rel = v ? (int64_t)a.B.idx[pos] - c_lo : -1;
-                        if (rel >= 0 && rel < winBits) atomicOr(&bm[rel >> 5], 1u << (rel & 31));
-                    });
+                    warp_range_ld<kWideLoads>(
+                        pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
+                        [&](bool v, int32_t col, int) {
+                            const int64_t rel = v ? (int64_t)col - c_lo : -1;
+                            if (rel >= 0 && rel < winBits) atomicOr(&bm[rel >> 5], 1u << (rel & 31));
+                        });
                 }
                 __syncthreads();
             }
@@ -1066,14 +1126,17 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
                 stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
             int32_t tb, te;
             warp_share<THREADS>(total, &tb, &te);
-            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
-                const int32_t c = v ? a.B.idx[pos] - cbase : 0;
-                if (v && (uint32_t)c < (uint32_t)nwords * 32u) {
-                    const int w = c >> 5;
-                    const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
-                    if (r < expect) atomicAdd(&cv[r], __dmul_rn(av[e], a.B.val[pos]));
-                }
-            });
+            warp_range_ld<4>(
+                pre, bst, nb, tb, te,
+                [&](int32_t pos) { return ColVal{__ldg(&a.B.idx[pos]), __ldg(&a.B.val[pos])}; },
+                [&](bool v, const ColVal &x, int e) {
+                    const int32_t c = x.c - cbase;
+                    if (v && (uint32_t)c < (uint32_t)nwords * 32u) {
+                        const int w = c >> 5;
+                        const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
+                        if (r < expect) atomicAdd(&cv[r], __dmul_rn(av[e], x.v));
+                    }
+                });
             __syncthreads();
         }
     } else {
@@ -1455,10 +1518,12 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo) 
                 stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
             int32_t tb, te;
             warp_share<THREADS>(total, &tb, &te);
-            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-                const uint32_t rel = v ? (uint32_t)((int64_t)a.B.idx[pos] - c_lo) : 0u;
-                or_bits_runs(bits, v && rel < nbits, rel);
-            });
+            warp_range_ld<4>(
+                pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
+                [&](bool v, int32_t col, int) {
+                    const uint32_t rel = v ? (uint32_t)((int64_t)col - c_lo) : 0u;
+                    or_bits_runs(bits, v && rel < nbits, rel);
+                });
             __syncthreads();
         }
         // Word ranks: each warp takes whole 256-word groups.
@@ -1509,15 +1574,19 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo) 
                 stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
             int32_t tb, te;
             warp_share<THREADS>(total, &tb, &te);
-            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
-                const uint32_t c = v ? (uint32_t)((int64_t)a.B.idx[pos] - c_lo) : 0u;
-                if (v && c < nbits) {
-                    const int w = (int)(c >> 5);
-                    const int64_t r =
-                        run + (int64_t)gbase[w >> 8] + wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
-                    if (r < expect) atomicAdd(&a.Cv[obase + r], __dmul_rn(av[e], a.B.val[pos]));
-                }
-            });
+            // Only products inside the window read their B value (rows
+            // over several windows would read it once per window).
+            warp_range_ld<4>(
+                pre, bst, nb, tb, te, [&](int32_t pos) { return make_int2(__ldg(&a.B.idx[pos]), pos); },
+                [&](bool v, int2 x, int e) {
+                    const uint32_t c = v ? (uint32_t)((int64_t)x.x - c_lo) : 0u;
+                    if (v && c < nbits) {
+                        const int w = (int)(c >> 5);
+                        const int64_t r =
+                            run + (int64_t)gbase[w >> 8] + wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
+                        if (r < expect) atomicAdd(&a.Cv[obase + r], __dmul_rn(av[e], __ldg(&a.B.val[x.y])));
+                    }
+                });
             __syncthreads();
         }
         run += tot;
