@@ -228,49 +228,16 @@ __device__ __forceinline__ int find_entry(const int32_t *pre, int nb, int32_t t)
     return lo;
 }
 
-// One warp walks products [tb, te) of a staged batch, 32 per step, calling
-// f(valid, pos, e) on every lane (pos = position in B, e = staged entry;
-// meaningful when valid).  A step whose products all lie in the current
-// entry (long B rows) takes their positions from registers; otherwise each
-// lane finds its entry by a 5-step shuffle search among the 32 entry starts
-// after the step's first entry.
-template <class F>
-__device__ __forceinline__ void warp_range(const int32_t *pre, const int32_t *bst, int nb, int32_t tb,
-                                           int32_t te, F &&f) {
-    if (tb >= te) return;
-    const int lane = threadIdx.x & 31;
-    int e0 = find_entry(pre, nb, tb);
-    // Entry e0 holds products [p0, p1), starting at position b0 of B.
-    int32_t p0 = pre[e0], b0 = bst[e0], p1 = e0 + 1 < nb ? pre[e0 + 1] : INT_MAX;
-    for (int32_t t0 = tb; t0 < te; t0 += 32) {
-        const int32_t t = t0 + lane;
-        const bool valid = t < te;
-        if (p1 > t0 + 31) {
-            f(valid, b0 + (t - p0), e0);
-            continue;
-        }
-        const int ej = e0 + 1 + lane;
-        const int32_t bnd = ej <= nb ? pre[ej] : INT_MAX;
-        int o = 0;
-#pragma unroll
-        for (int step = 16; step >= 1; step >>= 1) {
-            const int32_t v = __shfl_sync(FULL, bnd, o + step - 1);
-            if (v <= t) o += step;
-        }
-        const int e = min(e0 + o, nb - 1);
-        f(valid, bst[e] + (t - pre[e]), e);
-        e0 = __shfl_sync(FULL, e, 31);
-        p0 = pre[e0];
-        b0 = bst[e0];
-        p1 = e0 + 1 < nb ? pre[e0 + 1] : INT_MAX;
-    }
-}
-
-// warp_range in groups of U steps with the loads of a group issued before
-// any is used: ld(pos) reads what a product needs from B (read-only loads),
-// use(valid, x, e) consumes it.  A warp keeps U loads in flight instead of
-// one, which hides the L2 latency of B's rows on long product runs.  use is
-// called by all lanes for each step, so it may hold warp collectives.
+// One warp walks products [tb, te) of a staged batch, 32 per step, in
+// groups of U steps whose B loads are all issued before any is used:
+// ld(pos) reads what a product needs from B (read-only loads), use(valid, x,
+// e) consumes it on every lane (e = staged entry; meaningful when valid).
+// A warp keeps U loads in flight instead of one, which hides the L2 latency
+// of B's rows.  A step whose products all lie in the current entry (long B
+// rows) takes their positions from registers; otherwise each lane finds its
+// entry by a 5-step shuffle search among the 32 entry starts after the
+// step's first entry.  use is called by all lanes for each step, so it may
+// hold warp collectives.
 template <int U, class LD, class USE>
 __device__ __forceinline__ void warp_range_ld(const int32_t *pre, const int32_t *bst, int nb, int32_t tb,
                                               int32_t te, LD &&ld, USE &&use) {
@@ -485,9 +452,11 @@ __global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t beg
             stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
         int32_t tb, te;
         warp_share<THREADS>(total, &tb, &te);
-        warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-            if (v) cnt += hash_insert_key<TABLE>(keys, a.B.idx[pos], a.err);
-        });
+        warp_range_ld<4>(
+            pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
+            [&](bool v, int32_t col, int) {
+                if (v) cnt += hash_insert_key<TABLE>(keys, col, a.err);
+            });
         __syncthreads();
     }
     cnt = block_sum_i<THREADS>(cnt, sh);
@@ -525,6 +494,8 @@ __device__ __forceinline__ int or_bits_count(uint32_t *bm, bool v, uint32_t rel,
 
 // Steps of B loads a wide-row warp keeps in flight on rows past the touch list.
 constexpr int kWideLoads = 4;
+// Steps of B loads a warp-hash row keeps in flight.
+constexpr int kHashWarpLoads = 2;
 
 // Words a wide-row window clears one by one: past a quarter of the window a
 // full clear is as cheap.
@@ -582,11 +553,13 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
                 if (rowCap) {
-                    warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-                        const int64_t rel = v ? (int64_t)a.B.idx[pos] - c_lo : -1;
-                        const bool in = rel >= 0 && rel < winBits;
-                        cnt += or_bits_count(bm, in, in ? (uint32_t)rel : 0u, touched, &nt, rowCap);
-                    });
+                    warp_range_ld<kWideLoads>(
+                        pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
+                        [&](bool v, int32_t col, int) {
+                            const int64_t rel = v ? (int64_t)col - c_lo : -1;
+                            const bool in = rel >= 0 && rel < winBits;
+                            cnt += or_bits_count(bm, in, in ? (uint32_t)rel : 0u, touched, &nt, rowCap);
+                        });
                 } else {
                     warp_range_ld<kWideLoads>(
                         pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
@@ -701,18 +674,25 @@ __global__ void __launch_bounds__(32 * ROWS) k_sym_flagw(SymArgs a, int32_t begi
         // run (banded and stencil matrices) flags its run a word (4 columns)
         // per lane; any other B row flags a column per lane.
         for (int32_t eb = e0; eb < e1; eb += 32) {
-            int32_t bs = 0, len = 0;
+            // Each lane loads its entry's B row bounds and first and last
+            // columns up front, so the entries below need no loads of their
+            // own before flagging.
+            int32_t bs = 0, len = 0, fc = 0, lc = 0;
             if (eb + lane < e1) {
                 const int32_t k = a.A.idx[eb + lane];
                 bs = a.B.ptr[k];
                 len = a.B.ptr[k + 1] - bs;
+                if (len > 0) {
+                    fc = __ldg(&bidx[bs]);
+                    lc = __ldg(&bidx[bs + len - 1]);
+                }
             }
             const int n = min(32, e1 - eb);
             for (int q = 0; q < n; ++q) {
                 const int32_t bq = __shfl_sync(FULL, bs, q);
                 const int32_t lq = __shfl_sync(FULL, len, q);
+                const int32_t first = __shfl_sync(FULL, fc, q), last = __shfl_sync(FULL, lc, q);
                 if (lq == 0) continue;
-                const int32_t first = bidx[bq], last = bidx[bq + lq - 1];
                 const uint32_t r0 = (uint32_t)(first - base), r1 = (uint32_t)(last - base);
                 if (a.bSorted && last - first == lq - 1 && r0 < nb && r1 < nb) {
                     for (uint32_t w = (r0 >> 2) + lane; w <= (r1 >> 2); w += 32) {
@@ -974,13 +954,32 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t 
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     for (int32_t e = e0; e < e1; e += 32) {
         const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
-        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
-            const int32_t t = t0 + lane;
-            double av;
-            const int32_t j = chunk_pos(c, t, &av);
-            if (t < c.total) {
-                const int s = hash_insert_slot<TABLE>(keys, a.B.idx[j], a.err);
-                if (s >= 0) atomic_fma(&vals[s], av, a.B.val[j]);
+        // kHashWarpLoads steps at a time: positions first, then all their B
+        // loads, then the inserts.
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32 * kHashWarpLoads) {
+            int32_t j[kHashWarpLoads], col[kHashWarpLoads];
+            double av[kHashWarpLoads], bv[kHashWarpLoads];
+#pragma unroll
+            for (int u = 0; u < kHashWarpLoads; ++u) {
+                j[u] = -1;
+                av[u] = 0.0;
+                const int32_t t = t0 + 32 * u + lane;
+                if (t0 + 32 * u < c.total) {
+                    const int32_t jj = chunk_pos(c, t, &av[u]);
+                    if (t < c.total) j[u] = jj;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kHashWarpLoads; ++u) {
+                col[u] = j[u] >= 0 ? __ldg(&a.B.idx[j[u]]) : 0;
+                bv[u] = j[u] >= 0 ? __ldg(&a.B.val[j[u]]) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kHashWarpLoads; ++u) {
+                if (j[u] >= 0) {
+                    const int s = hash_insert_slot<TABLE>(keys, col[u], a.err);
+                    if (s >= 0) atomic_fma(&vals[s], av[u], bv[u]);
+                }
             }
         }
     }
@@ -1014,12 +1013,15 @@ __global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo)
             stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
         int32_t tb, te;
         warp_share<THREADS>(total, &tb, &te);
-        warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
-            if (v) {
-                const int s = hash_insert_slot<TABLE>(keys, a.B.idx[pos], a.err);
-                if (s >= 0) atomic_fma(&vals[s], av[e], a.B.val[pos]);
-            }
-        });
+        warp_range_ld<4>(
+            pre, bst, nb, tb, te,
+            [&](int32_t pos) { return ColVal{__ldg(&a.B.idx[pos]), __ldg(&a.B.val[pos])}; },
+            [&](bool v, const ColVal &x, int e) {
+                if (v) {
+                    const int s = hash_insert_slot<TABLE>(keys, x.c, a.err);
+                    if (s >= 0) atomic_fma(&vals[s], av[e], x.v);
+                }
+            });
         __syncthreads();
     }
     table_write_sorted<THREADS, 1, TABLE>(a, row, keys, vals, &gcnt, tid);
@@ -1034,7 +1036,7 @@ __global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo)
 // GLOBAL_ACC the row's slice of C's values is zeroed and accumulated in place
 // by FP64 reductions at L2 (no shared value array, no slices).
 template <int THREADS, bool GLOBAL_ACC>
-__global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int maxWords, int vcap) {
+__global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArgs a, int32_t lo, int maxWords, int vcap) {
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
     constexpr int NW = THREADS / 32;
@@ -1070,10 +1072,12 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
                 stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
             int32_t tb, te;
             warp_share<THREADS>(total, &tb, &te);
-            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-                const uint32_t rel = v ? (uint32_t)(a.B.idx[pos] - cbase) : 0u;
-                or_bits_runs(bits, v && in_window(rel, (uint32_t)nwords * 32u, a.err), rel);
-            });
+            warp_range_ld<4>(
+                pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
+                [&](bool v, int32_t col, int) {
+                    const uint32_t rel = v ? (uint32_t)(col - cbase) : 0u;
+                    or_bits_runs(bits, v && in_window(rel, (uint32_t)nwords * 32u, a.err), rel);
+                });
             __syncthreads();
         }
     }
@@ -1150,14 +1154,17 @@ __global__ void __launch_bounds__(THREADS) k_num_rank(NumArgs a, int32_t lo, int
                     stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
-                warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int e) {
-                    const int32_t c = v ? a.B.idx[pos] - cbase : 0;
-                    if (v && (uint32_t)c < (uint32_t)nwords * 32u) {
-                        const int w = c >> 5;
-                        const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u)) - s0;
-                        if (r >= 0 && r < ns) atomic_fma(&vals[r], av[e], a.B.val[pos]);
-                    }
-                });
+                warp_range_ld<4>(
+                    pre, bst, nb, tb, te,
+                    [&](int32_t pos) { return ColVal{__ldg(&a.B.idx[pos]), __ldg(&a.B.val[pos])}; },
+                    [&](bool v, const ColVal &x, int e) {
+                        const int32_t c = x.c - cbase;
+                        if (v && (uint32_t)c < (uint32_t)nwords * 32u) {
+                            const int w = c >> 5;
+                            const int64_t r = (int64_t)wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u)) - s0;
+                            if (r >= 0 && r < ns) atomic_fma(&vals[r], av[e], x.v);
+                        }
+                    });
                 __syncthreads();
             }
             for (int i = tid; i < ns; i += THREADS) a.Cv[obase + s0 + i] = vals[i];
@@ -1638,15 +1645,17 @@ __global__ void __launch_bounds__(THREADS) k_num_gdense(NumArgs a, int32_t lo, i
                 stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
             int32_t tb, te;
             warp_share<THREADS>(total, &tb, &te);
-            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t pos, int) {
-                if (v) {
-                    const uint32_t c = (uint32_t)a.B.idx[pos];
-                    if (in_window(c, ncols, err)) {
-                        atomicOr(&bits[c >> 5], 1u << (c & 31));
-                        atomicOr(&sum[c >> 10], 1u << ((c >> 5) & 31));  // shared
+            warp_range_ld<4>(
+                pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
+                [&](bool v, int32_t col, int) {
+                    if (v) {
+                        const uint32_t c = (uint32_t)col;
+                        if (in_window(c, ncols, err)) {
+                            atomicOr(&bits[c >> 5], 1u << (c & 31));
+                            atomicOr(&sum[c >> 10], 1u << ((c >> 5) & 31));  // shared
+                        }
                     }
-                }
-            });
+                });
             __syncthreads();
         }
         __threadfence();
@@ -1686,16 +1695,20 @@ __global__ void __launch_bounds__(THREADS) k_num_gdense(NumArgs a, int32_t lo, i
                 stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
             int32_t tb, te;
             warp_share<THREADS>(total, &tb, &te);
-            warp_range(pre, bst, nb, tb, te, [&](bool v, int32_t p, int e) {
-                if (v) {
-                    const uint32_t c = (uint32_t)a.B.idx[p];
-                    if (c < ncols) {
-                        const int w = (int)(c >> 5);
-                        const int64_t r = (int64_t)__ldcg(&wpre[w]) + __popc(__ldcg(&bits[w]) & ((1u << (c & 31)) - 1u));
-                        if (r < expect) atomicAdd(&a.Cv[obase + r], __dmul_rn(av[e], a.B.val[p]));
+            warp_range_ld<4>(
+                pre, bst, nb, tb, te,
+                [&](int32_t p) { return ColVal{__ldg(&a.B.idx[p]), __ldg(&a.B.val[p])}; },
+                [&](bool v, const ColVal &x, int e) {
+                    if (v) {
+                        const uint32_t c = (uint32_t)x.c;
+                        if (c < ncols) {
+                            const int w = (int)(c >> 5);
+                            const int64_t r =
+                                (int64_t)__ldcg(&wpre[w]) + __popc(__ldcg(&bits[w]) & ((1u << (c & 31)) - 1u));
+                            if (r < expect) atomicAdd(&a.Cv[obase + r], __dmul_rn(av[e], x.v));
+                        }
                     }
-                }
-            });
+                });
             __syncthreads();
         }
         // Clean-up: the words this row set, then its summary words.
