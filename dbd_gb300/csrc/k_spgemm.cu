@@ -602,6 +602,59 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
     }
 }
 
+// Size of a row of C whose B rows are each one contiguous run of columns
+// (banded and stencil matrices), with the runs' first columns non-decreasing
+// in A's entry order: the length of the union of the runs, by a prefix
+// maximum of the runs' last columns (the run of entry i adds the part of
+// [first_i, last_i] beyond every earlier run's end).  One warp, 32 entries a
+// step, no per-column work.  Returns false (count unset) when some B row is
+// not one run or the first columns decrease; B's rows must ascend strictly.
+__device__ __forceinline__ bool interval_union_count(const CsrDev &A, const CsrDev &B, int32_t e0, int32_t e1,
+                                                     int lane, int *count) {
+    int32_t endMax = INT32_MIN, firstMax = INT32_MIN;  // over the entries of earlier steps
+    int cnt = 0;
+    for (int32_t eb = e0; eb < e1; eb += 32) {
+        bool has = false;
+        int32_t f = INT32_MIN, l = INT32_MIN;
+        bool run = true;
+        if (eb + lane < e1) {
+            const int32_t k = A.idx[eb + lane];
+            const int32_t bs = B.ptr[k], len = B.ptr[k + 1] - bs;
+            if (len > 0) {
+                has = true;
+                f = __ldg(&B.idx[bs]);
+                l = __ldg(&B.idx[bs + len - 1]);
+                run = l - f == len - 1;
+            }
+        }
+        // Inclusive prefix maxima of the first and last columns over lanes.
+        int32_t fm = f, lm = l;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int32_t yf = __shfl_up_sync(FULL, fm, d), yl = __shfl_up_sync(FULL, lm, d);
+            if (lane >= d) {
+                fm = max(fm, yf);
+                lm = max(lm, yl);
+            }
+        }
+        int32_t fPrev = __shfl_up_sync(FULL, fm, 1), lPrev = __shfl_up_sync(FULL, lm, 1);
+        if (lane == 0) {
+            fPrev = INT32_MIN;
+            lPrev = INT32_MIN;
+        }
+        fPrev = max(fPrev, firstMax);
+        lPrev = max(lPrev, endMax);
+        if (!__all_sync(FULL, run && (!has || f >= fPrev))) return false;
+        int add = 0;
+        if (has) add = (int)max(0LL, (long long)l - max((long long)f - 1, (long long)lPrev));
+        cnt += warp_sum_i(add);
+        firstMax = max(firstMax, __shfl_sync(FULL, fm, 31));
+        endMax = max(endMax, __shfl_sync(FULL, lm, 31));
+    }
+    *count = cnt;
+    return true;
+}
+
 // Products of one row for one warp, calling f(j, av) for every product (B
 // position j, A value av) on the lane that owns it.  Row-wise (long B rows):
 // the A entries one after another, the lanes over the B row; f calls of one
@@ -669,6 +722,13 @@ __global__ void __launch_bounds__(32 * ROWS) k_sym_flagw(SymArgs a, int32_t begi
     const bool rowwise = a.rowP[row] >= (int64_t)kRowwiseMinLen * (e1 - e0);
     int *err = a.err;
     const int32_t *bidx = a.B.idx;
+    if (rowwise && a.bSorted) {
+        int cnt;
+        if (interval_union_count(a.A, a.B, e0, e1, lane, &cnt)) {
+            if (lane == 0) a.rowNnz[row] = cnt;
+            return;
+        }
+    }
     if (rowwise) {
         // One A entry at a time.  A B row whose columns form one contiguous
         // run (banded and stencil matrices) flags its run a word (4 columns)

@@ -184,6 +184,43 @@ def test_narrow_rows_every_enumeration(ctx, orc):
         assert res.stats["sym_rows_per_bin"][2] > 0 and res.stats["rows_per_bin"][9] > 0
 
 
+def run_rows(rng, n, step, lmin, lmax, permute=False, gap_every=0):
+    """n x (step n + lmax): row k is one contiguous run of lmin..lmax columns
+    starting at step * k (starts ascending with k; overlapping, nested or
+    disjoint runs by the step).  permute: rows shuffled within blocks of 8
+    (starts no longer ascending); gap_every: every such row loses an interior
+    column."""
+    lens = rng.integers(lmin, lmax + 1, n)
+    rows = np.repeat(np.arange(n), lens)
+    cols = np.concatenate([step * k + np.arange(L) for k, L in enumerate(lens)])
+    keep = np.ones(cols.size, bool)
+    if gap_every:
+        starts = np.concatenate([[0], np.cumsum(lens)[:-1]])
+        keep[starts[::gap_every] + 1] = False
+    M = gen._from_coo(n, step * n + lmax, rows[keep], cols[keep], rng.uniform(-1, 1, int(keep.sum())))
+    if permute:  # rows shuffled within blocks of 8, so that the window stays narrow
+        p = np.concatenate([b0 + rng.permutation(min(8, n - b0)) for b0 in range(0, n, 8)])
+        lens2 = np.diff(M.row_ptr)[p]
+        ptr = np.concatenate([[0], np.cumsum(lens2)]).astype(np.int32)
+        take = np.concatenate([np.arange(M.row_ptr[r], M.row_ptr[r + 1]) for r in p])
+        M = CSR(n, M.n_cols, ptr, M.col_idx[take], M.val[take])
+    return M
+
+
+def test_narrow_rows_runs_of_columns(ctx, orc):
+    """Narrow rows whose B rows are single runs of columns (the symbolic
+    count is the length of the runs' union): overlapping and nested runs,
+    disjoint runs, runs whose starts do not ascend with the entry, and some
+    B rows with a gap (the warp-flag path takes over)."""
+    rng = np.random.default_rng(33)
+    A = gen.banded(1500, 24, seed=7)
+    for B in (run_rows(rng, 1500, 2, 16, 40), run_rows(rng, 1500, 1, 16, 64), run_rows(rng, 1500, 30, 16, 25),
+              run_rows(rng, 1500, 2, 16, 40, permute=True), run_rows(rng, 1500, 2, 16, 40, gap_every=97)):
+        res = ctx.spgemm(A, B, scope="kernel")
+        check(res.C, A, B, orc)
+        assert res.stats["sym_rows_per_bin"][2] > 0
+
+
 def test_dense_rows_long_and_thin_b_rows(ctx, orc):
     """Dense-window rows both ways: B rows of 2,000 consecutive columns (many
     products per entry and window: one warp per entry) and B rows of a few
