@@ -81,6 +81,11 @@ __device__ __forceinline__ bool in_window(uint32_t rel, uint32_t limit, int *err
 // product t (0 <= t < total) comes from the lane whose inclusive length
 // prefix first exceeds t.
 // ---------------------------------------------------------------------------
+// Steps of B loads a wide-row warp keeps in flight on rows past the touch list.
+constexpr int kWideLoads = 4;
+// Steps of B loads a warp-hash row keeps in flight.
+constexpr int kHashWarpLoads = 2;
+
 struct Chunk {
     int32_t bs;    // first position of B_k in B.idx
     int32_t len;   // |B_k|
@@ -422,10 +427,20 @@ __global__ void __launch_bounds__(32 * ROWS) k_sym_hash_warp(SymArgs a, int32_t 
     int cnt = 0;
     for (int32_t e = e0; e < e1; e += 32) {
         const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
-        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
-            const int32_t t = t0 + lane;
-            const int32_t j = chunk_pos(c, t, nullptr);
-            if (t < c.total) cnt += hash_insert_key<TABLE>(keys, a.B.idx[j], a.err);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32 * kHashWarpLoads) {
+            int32_t col[kHashWarpLoads];
+#pragma unroll
+            for (int u = 0; u < kHashWarpLoads; ++u) {
+                col[u] = -1;
+                const int32_t t = t0 + 32 * u + lane;
+                if (t0 + 32 * u < c.total) {
+                    const int32_t j = chunk_pos(c, t, nullptr);
+                    if (t < c.total) col[u] = __ldg(&a.B.idx[j]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kHashWarpLoads; ++u)
+                if (col[u] >= 0) cnt += hash_insert_key<TABLE>(keys, col[u], a.err);
         }
     }
     cnt = warp_sum_i(cnt);
@@ -491,11 +506,6 @@ __device__ __forceinline__ int or_bits_count(uint32_t *bm, bool v, uint32_t rel,
     }
     return __popc(acc & ~old);
 }
-
-// Steps of B loads a wide-row warp keeps in flight on rows past the touch list.
-constexpr int kWideLoads = 4;
-// Steps of B loads a warp-hash row keeps in flight.
-constexpr int kHashWarpLoads = 2;
 
 // Words a wide-row window clears one by one: past a quarter of the window a
 // full clear is as cheap.
@@ -992,6 +1002,97 @@ __device__ __forceinline__ void table_write_sorted(NumArgs &a, int32_t row, int3
 constexpr size_t warp_hash_bytes(int table) { return 12 * (size_t)table + 4 * (size_t)table + 4 * (size_t)kBuckets; }
 
 // Warp hash rows: keys int32[TABLE] then values double[TABLE] per row.
+// A row of at most kNumWarpMax products, by one warp without a hash table
+// (expand, sort, compress): every product's column and value go to shared
+// memory, a bucket counting sort (or a bitonic sort when columns cluster)
+// orders them by column, and each run of equal columns is summed by the lane
+// holding its first entry and written at the run's rank.  pk holds
+// kNumWarpMax packed (column << 32 | product) keys, pv the products' values.
+template <int ROWS>
+__device__ __forceinline__ void esc_row(NumArgs &a, int32_t row, int32_t e0, int32_t e1, int n, uint64_t *pk,
+                                        double *pv, int *cnts, uint64_t *bbuf) {
+    const int lane = threadIdx.x & 31;
+    int32_t tb = 0;  // products of the earlier chunks
+    for (int32_t e = e0; e < e1; e += 32) {
+        const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32 * kHashWarpLoads) {
+            int32_t j[kHashWarpLoads];
+            double av[kHashWarpLoads];
+#pragma unroll
+            for (int u = 0; u < kHashWarpLoads; ++u) {
+                j[u] = -1;
+                av[u] = 0.0;
+                const int32_t t = t0 + 32 * u + lane;
+                if (t0 + 32 * u < c.total) {
+                    const int32_t jj = chunk_pos(c, t, &av[u]);
+                    if (t < c.total && tb + t < n) j[u] = jj;
+                }
+            }
+            int32_t col[kHashWarpLoads];
+            double bv[kHashWarpLoads];
+#pragma unroll
+            for (int u = 0; u < kHashWarpLoads; ++u) {
+                col[u] = j[u] >= 0 ? __ldg(&a.B.idx[j[u]]) : 0;
+                bv[u] = j[u] >= 0 ? __ldg(&a.B.val[j[u]]) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kHashWarpLoads; ++u) {
+                if (j[u] >= 0) {
+                    const int t = tb + t0 + 32 * u + lane;
+                    pk[t] = ((uint64_t)(uint32_t)col[u] << 32) | (uint32_t)t;
+                    pv[t] = __dmul_rn(av[u], bv[u]);
+                }
+            }
+        }
+        tb += c.total;
+    }
+    __syncwarp();
+    const int32_t rlo = a.rowLo[row];
+    const int64_t span = max((int64_t)1, (int64_t)a.rowHi[row] - rlo + 1);
+    const uint64_t *sorted = bbuf;
+    if (!warp_bucket_order(pk, n, rlo, span, cnts, bbuf)) {
+        int N = 1;
+        while (N < n) N <<= 1;
+        for (int i = n + lane; i < N; i += 32) pk[i] = ~0ull;
+        __syncwarp();
+        group_bitonic<32, ROWS>(pk, N, lane);
+        sorted = pk;
+    }
+    // Lane l takes sorted entries [8 l, 8 l + 8): the first entry of each
+    // run of equal columns is a head; heads before it give its rank.
+    constexpr int PER = kNumWarpMax / 32;
+    uint32_t headMask = 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int i = PER * lane + q;
+        if (i < n && (i == 0 || (sorted[i] >> 32) != (sorted[i - 1] >> 32))) headMask |= 1u << q;
+    }
+    const int mine = __popc(headMask);
+    int incl = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d) incl += y;
+    }
+    const int total = __shfl_sync(FULL, incl, 31);
+    const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+    if (lane == 0 && total != expect) raise(a.err, DEV_COUNT_MISMATCH);
+    const int64_t obase = a.Cp[row] - a.outBase;
+    const int32_t shift = col_shift(a, row);
+    int64_t pos = incl - mine;
+    for (uint32_t m = headMask; m; m &= m - 1u) {
+        const int i = PER * lane + __ffs(m) - 1;
+        const uint64_t k0 = sorted[i];
+        double sum = pv[(uint32_t)k0];
+        for (int jx = i + 1; jx < n && (sorted[jx] >> 32) == (k0 >> 32); ++jx) sum = __dadd_rn(sum, pv[(uint32_t)sorted[jx]]);
+        if (pos < expect) {
+            a.Ci[obase + pos] = (int32_t)(k0 >> 32) - shift;
+            a.Cv[obase + pos] = sum;
+        }
+        ++pos;
+    }
+}
+
 template <int ROWS, int TABLE>
 __global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t lo, int32_t count) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1005,13 +1106,17 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t 
     uint64_t *bbuf = reinterpret_cast<uint64_t *>(base_ptr + 12 * (size_t)TABLE);
     int *cnts = reinterpret_cast<int *>(bbuf + TABLE / 2);
     const int32_t row = a.list[lo + item];
+    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+    if (a.rowP[row] <= kNumWarpMax && TABLE >= 2 * kNumWarpMax) {
+        esc_row<ROWS>(a, row, e0, e1, (int)a.rowP[row], reinterpret_cast<uint64_t *>(keys), vals, cnts, bbuf);
+        return;
+    }
     for (int i = lane; i < TABLE; i += 32) {
         keys[i] = EMPTY;
         vals[i] = 0.0;
     }
     if (lane == 0) gcnt[g] = 0;
     __syncwarp();
-    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     for (int32_t e = e0; e < e1; e += 32) {
         const Chunk c = load_chunk(a.A, a.B, e, e1, lane);
         // kHashWarpLoads steps at a time: positions first, then all their B
