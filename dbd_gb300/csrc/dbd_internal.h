@@ -120,7 +120,9 @@ struct RowInfo {
 enum DevErr : int { DEV_OK = 0, DEV_TABLE_FULL = 1, DEV_COUNT_MISMATCH = 2, DEV_ROW_TOO_LONG = 3, DEV_OUT_OF_WINDOW = 4 };
 
 // Counter slots for dynamically scheduled kernels (zeroed per multiply).
-enum CounterSlot : int { CTR_SYM_TINY = 0, CTR_SYM_HWARP, CTR_SYM_HCTA, CTR_SYM_WIDE, CTR_NUM_GDENSE, CTR_COUNT = 16 };
+enum CounterSlot : int {
+    CTR_SYM_TINY = 0, CTR_SYM_HWARP, CTR_SYM_HCTA, CTR_SYM_WIDE, CTR_NUM_GDENSE, CTR_NUM_RANKWIN, CTR_COUNT = 16
+};
 
 struct Binning {
     uint8_t *bin = nullptr;     // m bin ids
@@ -203,7 +205,7 @@ struct NumArgs {
     uint32_t *gWpre = nullptr;
     int64_t gStride = 0;   // multiple of 1024
     int gSlots = 0;
-    uint32_t *ctr = nullptr;  // zeroed row counters (CTR_NUM_GDENSE)
+    uint32_t *ctr = nullptr;  // row counters of the persistent dense-row kernels (zeroed per launch)
 };
 // Bytes of one global dense slot of `stride` columns.
 inline size_t gdense_slot_bytes(int64_t stride) { return (size_t)stride / 4; }

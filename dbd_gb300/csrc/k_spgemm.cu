@@ -1650,120 +1650,129 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_rankm(NumArgs a, int32_t lo, 
     }
 }
 
-// Dense rows (windows wider than the CTA rank kernel's): one CTA per row, the
-// rank method over windows of WIN words of the row's span (2^20 columns in
-// shared memory).  Per window: a pass over the row's products sets the bits
-// inside the window, a scan gives every word's rank (a 16-bit offset from a
-// 32-bit base per 256 words), C's columns are written, and a second pass
-// adds every product inside the window into C's row in place at its rank
-// (FP64 L2 reductions).  A row costs two product passes per window and its
-// span / 32 words of scans; power-law rows over millions of columns take two
-// windows.
+// Dense rows (windows wider than the CTA rank kernel's): persistent CTAs,
+// one per SM, take rows from a counter and apply the rank method over
+// windows of WIN words of the row's span (2^20 columns in shared memory).
+// Per window: a pass over the row's products sets the bits inside the
+// window; a sweep gives each thread the non-empty-word mask and bit count
+// of its 32 words (one summary word), and a scan of the counts gives every
+// thread the rank of its first column.  From there everything visits only
+// the non-empty words: their ranks (a 16-bit offset from a 32-bit base per
+// 256 words), C's columns (each thread writes a contiguous run of them), and
+// the clean-up that leaves the bitmap zero for the next window.  A second
+// pass adds every product inside the window into C's row in place at its
+// rank (FP64 L2 reductions).  Power-law rows spread thinly over millions of
+// columns pay for their entries, not for their span, past the one sweep.
 template <int THREADS, int WIN>
-__global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo) {
+__global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, int32_t count) {
+    static_assert(WIN == 32 * THREADS, "one summary word of 32 bitmap words per thread");
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
     constexpr int NW = THREADS / 32;
     __shared__ int32_t sh[NW];
+    __shared__ int32_t next;
     int32_t *pre = reinterpret_cast<int32_t *>(smem + L::pre);
     int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
     double *av = reinterpret_cast<double *>(smem + L::av);
     uint32_t *bits = reinterpret_cast<uint32_t *>(smem + L::bytes);
     uint16_t *wpre = reinterpret_cast<uint16_t *>(bits + WIN);
     int32_t *gbase = reinterpret_cast<int32_t *>(wpre + WIN);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int32_t row = a.list[lo + blockIdx.x];
-    const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
-    const int64_t expect = a.Cp[row + 1] - a.Cp[row];
-    const int64_t obase = a.Cp[row] - a.outBase;
-    const int32_t shift = col_shift(a, row);
-    const int64_t end = (int64_t)a.rowHi[row] + 1;
-    int64_t run = 0;
-    for (int64_t c_lo = (int64_t)(a.rowLo[row] >> 5) << 5; c_lo < end; c_lo += (int64_t)WIN * 32) {
-        const int nwords = (int)min((int64_t)WIN, (end - c_lo + 31) >> 5);
-        const uint32_t nbits = (uint32_t)nwords * 32u;
-        for (int i = tid; i < nwords; i += THREADS) bits[i] = 0u;
-        // Pass 1: the window's bits.
-        for (int32_t eb = e0; eb < e1; eb += THREADS) {
-            int nb;
-            const int32_t total =
-                stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
-            int32_t tb, te;
-            warp_share<THREADS>(total, &tb, &te);
-            warp_range_ld<4>(
-                pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
-                [&](bool v, int32_t col, int) {
-                    const uint32_t rel = v ? (uint32_t)((int64_t)col - c_lo) : 0u;
-                    or_bits_runs(bits, v && rel < nbits, rel);
-                });
-            __syncthreads();
-        }
-        // Word ranks: each warp takes whole 256-word groups.
-        const int per = ((nwords + NW - 1) / NW + 255) / 256 * 256;
-        const int wb = min(nwords, warp * per), we = min(nwords, wb + per);
-        int32_t wsum = 0;
-        for (int w = wb + lane; w < we; w += 32) wsum += __popc(bits[w]);
-#pragma unroll
-        for (int d = 16; d; d >>= 1) wsum += __shfl_xor_sync(FULL, wsum, d);
-        int32_t tot;
-        int32_t wrun = block_excl_scan<THREADS>(lane == 0 ? wsum : 0, &tot, sh);
-        wrun = __shfl_sync(FULL, wrun, 0);
-        int32_t gb = 0;
-        for (int w0 = wb; w0 < we; w0 += 32) {
-            if ((w0 & 255) == 0) {
-                gb = wrun;
-                if (lane == 0) gbase[w0 >> 8] = wrun;
-            }
-            const int w = w0 + lane;
-            const int32_t pc = w < we ? __popc(bits[w]) : 0;
-            int32_t incl = pc;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const int32_t y = __shfl_up_sync(FULL, incl, d);
-                if (lane >= d) incl += y;
-            }
-            if (w < we) wpre[w] = (uint16_t)(wrun + incl - pc - gb);
-            wrun += __shfl_sync(FULL, incl, 31);
-        }
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int i = tid; i < WIN; i += THREADS) bits[i] = 0u;
+    for (;;) {
+        if (tid == 0) next = (int32_t)atomicAdd(&a.ctr[CTR_NUM_RANKWIN], 1u);
         __syncthreads();
-        // C's columns of the window, and its values zeroed.
-        for (int w = tid; w < nwords; w += THREADS) {
-            uint32_t word = bits[w];
-            int64_t p = run + (int64_t)gbase[w >> 8] + wpre[w];
-            while (word) {
-                const int b = __ffs(word) - 1;
-                word &= word - 1u;
-                if (p < expect) __stcs(&a.Ci[obase + p], (int32_t)(c_lo + (w << 5) + b - shift));
-                ++p;
+        const int32_t item = next;
+        if (item >= count) break;
+        const int32_t row = a.list[lo + item];
+        const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+        const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+        const int64_t obase = a.Cp[row] - a.outBase;
+        const int32_t shift = col_shift(a, row);
+        const int64_t end = (int64_t)a.rowHi[row] + 1;
+        int64_t run = 0;
+        for (int64_t c_lo = (int64_t)(a.rowLo[row] >> 5) << 5; c_lo < end; c_lo += (int64_t)WIN * 32) {
+            const int nwords = (int)min((int64_t)WIN, (end - c_lo + 31) >> 5);
+            const uint32_t nbits = (uint32_t)nwords * 32u;
+            // Pass 1: the window's bits.
+            for (int32_t eb = e0; eb < e1; eb += THREADS) {
+                int nb;
+                const int32_t total =
+                    stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
+                int32_t tb, te;
+                warp_share<THREADS>(total, &tb, &te);
+                warp_range_ld<4>(
+                    pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
+                    [&](bool v, int32_t col, int) {
+                        const uint32_t rel = v ? (uint32_t)((int64_t)col - c_lo) : 0u;
+                        or_bits_runs(bits, v && rel < nbits, rel);
+                    });
+                __syncthreads();
             }
-        }
-        for (int64_t i = tid; i < tot && run + i < expect; i += THREADS) a.Cv[obase + run + i] = 0.0;
-        __syncthreads();
-        // Pass 2: the window's products into C's row in place.
-        for (int32_t eb = e0; eb < e1; eb += THREADS) {
-            int nb;
-            const int32_t total =
-                stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
-            int32_t tb, te;
-            warp_share<THREADS>(total, &tb, &te);
-            // Only products inside the window read their B value (rows
-            // over several windows would read it once per window).
-            warp_range_ld<4>(
-                pre, bst, nb, tb, te, [&](int32_t pos) { return make_int2(__ldg(&a.B.idx[pos]), pos); },
-                [&](bool v, int2 x, int e) {
-                    const uint32_t c = v ? (uint32_t)((int64_t)x.x - c_lo) : 0u;
-                    if (v && c < nbits) {
-                        const int w = (int)(c >> 5);
-                        const int64_t r =
-                            run + (int64_t)gbase[w >> 8] + wpre[w] + __popc(bits[w] & ((1u << (c & 31)) - 1u));
-                        if (r < expect) atomicAdd(&a.Cv[obase + r], __dmul_rn(av[e], __ldg(&a.B.val[x.y])));
+            // This thread's 32 words [32 tid, 32 tid + 32): which are
+            // non-empty and how many bits they hold.  Lanes start at
+            // different words so that a warp's loads hit 32 banks.
+            uint32_t mask = 0;
+            int32_t cnt = 0;
+#pragma unroll 8
+            for (int k = 0; k < 32; ++k) {
+                const int q = (k + lane) & 31;
+                const uint32_t x = bits[32 * tid + q];
+                if (x) mask |= 1u << q;
+                cnt += __popc(x);
+            }
+            int32_t tot;
+            const int32_t base = block_excl_scan<THREADS>(cnt, &tot, sh);
+            // 256-word groups are 8 threads: the group's base is its first
+            // thread's.
+            const int32_t gb = __shfl_sync(FULL, base, lane & ~7);
+            if ((lane & 7) == 0) gbase[tid >> 3] = base;
+            {
+                int32_t p = base;
+                for (uint32_t m = mask; m; m &= m - 1u) {
+                    const int w = 32 * tid + __ffs(m) - 1;
+                    uint32_t word = bits[w];
+                    wpre[w] = (uint16_t)(p - gb);
+                    while (word) {
+                        const int b = __ffs(word) - 1;
+                        word &= word - 1u;
+                        if (run + p < expect) __stcs(&a.Ci[obase + run + p], (int32_t)(c_lo + (w << 5) + b - shift));
+                        ++p;
                     }
-                });
+                }
+            }
+            for (int64_t i = tid; i < tot && run + i < expect; i += THREADS) a.Cv[obase + run + i] = 0.0;
             __syncthreads();
+            // Pass 2: the window's products into C's row in place.
+            for (int32_t eb = e0; eb < e1; eb += THREADS) {
+                int nb;
+                const int32_t total =
+                    stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
+                int32_t tb, te;
+                warp_share<THREADS>(total, &tb, &te);
+                // Only products inside the window read their B value (rows
+                // over several windows would read it once per window).
+                warp_range_ld<4>(
+                    pre, bst, nb, tb, te, [&](int32_t pos) { return make_int2(__ldg(&a.B.idx[pos]), pos); },
+                    [&](bool v, int2 x, int e) {
+                        const uint32_t c = v ? (uint32_t)((int64_t)x.x - c_lo) : 0u;
+                        if (v && c < nbits) {
+                            const int w = (int)(c >> 5);
+                            const int64_t r = run + (int64_t)gbase[w >> 8] + wpre[w] +
+                                              __popc(bits[w] & ((1u << (c & 31)) - 1u));
+                            if (r < expect) atomicAdd(&a.Cv[obase + r], __dmul_rn(av[e], __ldg(&a.B.val[x.y])));
+                        }
+                    });
+                __syncthreads();
+            }
+            // Leave the bitmap zero: only this thread's non-empty words.
+            for (uint32_t m = mask; m; m &= m - 1u) bits[32 * tid + __ffs(m) - 1] = 0u;
+            __syncthreads();
+            run += tot;
         }
-        run += tot;
+        if (tid == 0 && run != expect) raise(a.err, DEV_COUNT_MISMATCH);
+        __syncthreads();  // every thread has read `next` before it changes
     }
-    if (tid == 0 && run != expect) raise(a.err, DEV_COUNT_MISMATCH);
 }
 
 // Dense rows with a global slot: persistent CTAs, one slot each, take rows
@@ -2249,8 +2258,10 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
             break;
         case NB_DENSE:
             if (a.tune.denseMethod == 0) {
+                cudaMemsetAsync(a.ctr + CTR_NUM_RANKWIN, 0, sizeof(uint32_t), s);
+                const int grid = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1));
                 k_num_rankwin<kRankWinThreads, kRankWinWords>
-                    <<<(unsigned)n, kRankWinThreads, kSmemRankWin, s>>>(a, lo);
+                    <<<(unsigned)grid, kRankWinThreads, kSmemRankWin, s>>>(a, lo, n);
             } else if (a.tune.denseMethod == 1 && a.gBits) {
                 cudaMemsetAsync(a.ctr + CTR_NUM_GDENSE, 0, sizeof(uint32_t), s);
                 const int grid = (int)std::min<int64_t>(n, a.gSlots);
