@@ -195,10 +195,14 @@ __device__ __forceinline__ int block_sum_i(int v, int *sh) {
 // of |B_k| (pre[*nb] = the batch's products), bst[i] = first position of B_k,
 // av[i] = A value.  Every staged entry has at least one product, so 32
 // consecutive products span at most 32 entries.  Returns the products.
+// With clip (B's rows ascending), each entry keeps only the part of its B
+// row inside the column window [cLo, cHi) (two binary searches at most), so
+// a row walked window by window enumerates each product once.
 template <int THREADS, bool VALS>
 __device__ __forceinline__ int32_t stage_entries(const CsrDev &A, const CsrDev &B, int32_t eb, int n_in,
                                                  int32_t *pre, int32_t *bst, double *av, int *nb,
-                                                 int32_t *sh) {
+                                                 int32_t *sh, bool clip = false, int64_t cLo = 0,
+                                                 int64_t cHi = 0) {
     const int tid = threadIdx.x;
     int32_t len = 0, s = 0;
     double a = 0.0;
@@ -207,6 +211,28 @@ __device__ __forceinline__ int32_t stage_entries(const CsrDev &A, const CsrDev &
         s = B.ptr[k];
         len = B.ptr[k + 1] - s;
         if constexpr (VALS) a = A.val[eb + tid];
+        if (clip && len > 0) {
+            const int32_t *bi = B.idx + s;
+            int32_t a0 = 0, a1 = len;
+            if ((int64_t)__ldg(&bi[0]) < cLo) {
+                int32_t l = 1, h = len;
+                while (l < h) {
+                    const int32_t m = (l + h) >> 1;
+                    if ((int64_t)__ldg(&bi[m]) < cLo) l = m + 1; else h = m;
+                }
+                a0 = l;
+            }
+            if (a0 < len && (int64_t)__ldg(&bi[len - 1]) >= cHi) {
+                int32_t l = a0, h = len - 1;
+                while (l < h) {
+                    const int32_t m = (l + h) >> 1;
+                    if ((int64_t)__ldg(&bi[m]) < cHi) l = m + 1; else h = m;
+                }
+                a1 = l;
+            }
+            s += a0;
+            len = max(0, a1 - a0);
+        }
     }
     int32_t total, kept;
     const int32_t ex = block_excl_scan<THREADS>(len, &total, sh);
@@ -552,14 +578,17 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
         const int rowCap = a.rowP[row] <= cap ? cap : 0;
         const bool keep = a.wideBits && sw <= kRankWordsMax;
         int cnt = 0;
+        // Rows over several windows enumerate, per window, only the part of
+        // each B row inside it (B's rows ascending).
+        const bool clip = a.bSorted && end - base > (int64_t)winBits;
         for (int64_t c_lo = base; c_lo < end; c_lo += winBits) {
             const int words = (int)min((int64_t)winBits, end - c_lo + 31) >> 5;
             if (tid == 0) nt = rowCap ? 0 : cap + 1;
             __syncthreads();
             for (int32_t eb = e0; eb < e1; eb += THREADS) {
                 int nb;
-                const int32_t total =
-                    stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
+                const int32_t total = stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst,
+                                                                    nullptr, &nb, sh, clip, c_lo, c_lo + winBits);
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
                 if (rowCap) {
@@ -1690,15 +1719,20 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
         const int64_t obase = a.Cp[row] - a.outBase;
         const int32_t shift = col_shift(a, row);
         const int64_t end = (int64_t)a.rowHi[row] + 1;
+        const int64_t start = (int64_t)(a.rowLo[row] >> 5) << 5;
+        // Rows over several windows enumerate, per window, only the part
+        // of each B row inside it (B's rows ascending).
+        const bool clip = a.bSorted && end - start > (int64_t)WIN * 32;
         int64_t run = 0;
-        for (int64_t c_lo = (int64_t)(a.rowLo[row] >> 5) << 5; c_lo < end; c_lo += (int64_t)WIN * 32) {
+        for (int64_t c_lo = start; c_lo < end; c_lo += (int64_t)WIN * 32) {
             const int nwords = (int)min((int64_t)WIN, (end - c_lo + 31) >> 5);
             const uint32_t nbits = (uint32_t)nwords * 32u;
+            const int64_t c_hi = c_lo + nbits;
             // Pass 1: the window's bits.
             for (int32_t eb = e0; eb < e1; eb += THREADS) {
                 int nb;
-                const int32_t total =
-                    stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh);
+                const int32_t total = stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst,
+                                                                    nullptr, &nb, sh, clip, c_lo, c_hi);
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
                 warp_range_ld<4>(
@@ -1746,21 +1780,20 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
             // Pass 2: the window's products into C's row in place.
             for (int32_t eb = e0; eb < e1; eb += THREADS) {
                 int nb;
-                const int32_t total =
-                    stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh);
+                const int32_t total = stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av,
+                                                                   &nb, sh, clip, c_lo, c_hi);
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
-                // Only products inside the window read their B value (rows
-                // over several windows would read it once per window).
                 warp_range_ld<4>(
-                    pre, bst, nb, tb, te, [&](int32_t pos) { return make_int2(__ldg(&a.B.idx[pos]), pos); },
-                    [&](bool v, int2 x, int e) {
-                        const uint32_t c = v ? (uint32_t)((int64_t)x.x - c_lo) : 0u;
+                    pre, bst, nb, tb, te,
+                    [&](int32_t pos) { return ColVal{__ldg(&a.B.idx[pos]), __ldg(&a.B.val[pos])}; },
+                    [&](bool v, const ColVal &x, int e) {
+                        const uint32_t c = v ? (uint32_t)((int64_t)x.c - c_lo) : 0u;
                         if (v && c < nbits) {
                             const int w = (int)(c >> 5);
                             const int64_t r = run + (int64_t)gbase[w >> 8] + wpre[w] +
                                               __popc(bits[w] & ((1u << (c & 31)) - 1u));
-                            if (r < expect) atomicAdd(&a.Cv[obase + r], __dmul_rn(av[e], __ldg(&a.B.val[x.y])));
+                            if (r < expect) atomicAdd(&a.Cv[obase + r], __dmul_rn(av[e], x.v));
                         }
                     });
                 __syncthreads();

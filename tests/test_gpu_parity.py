@@ -251,6 +251,37 @@ def test_dense_rows_long_and_thin_b_rows(ctx, orc):
             check(res.C, A, B, orc)
 
 
+def test_dense_rows_over_several_windows(ctx, orc):
+    """Rows over 2.5M columns (three 2^20-column windows, symbolic and
+    numeric): B rows scattered over the whole range (each window takes its
+    part of them), B rows inside one window, B rows ending exactly at a
+    window edge; then the same B with its rows out of column order."""
+    rng = np.random.default_rng(12)
+    n = 2_500_000
+    rows, cols = [], []
+    for r in range(3000):
+        kind = r % 3
+        if kind == 0:
+            c = rng.choice(n, 40, replace=False)
+        elif kind == 1:
+            w0 = (r % 3) * (1 << 20)
+            c = w0 + rng.choice(min(1 << 20, n - w0), 40, replace=False)
+        else:
+            edge = (1 + r % 2) << 20
+            c = np.concatenate([np.arange(edge - 20, edge), rng.choice(n, 20, replace=False)])
+            c = np.unique(c)
+        rows.append(np.full(c.size, r))
+        cols.append(c)
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    B = gen._from_coo(3000, n, rows, cols, rng.uniform(-1, 1, rows.size))
+    A = gen.uniform_rows(24, 600, seed=9, n_cols=3000, dist="uniform")
+    res = ctx.spgemm(A, B, scope="kernel")
+    check(res.C, A, B, orc)
+    assert res.stats["rows_per_bin"][8] > 0 and res.stats["sym_rows_per_bin"][5] > 0
+    res = ctx.spgemm(A, shuffled_rows(rng, B), scope="kernel")
+    check(res.C, A, B, orc)
+
+
 def test_dense_rows_unsorted_b(ctx, orc):
     """Dense-window rows with B rows out of column order take the rescanning path."""
     rng = np.random.default_rng(5)
