@@ -735,14 +735,18 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
 
     std::vector<Chunk> chunks;
     int64_t cap_entries = nnz;
-    const int nslots_dev = 2;
+    // The kernel scope copies nothing out, so one slot takes the whole
+    // remaining budget: few, large chunks, in which the heaviest rows of a
+    // power-law matrix are a small share of a launch's work.  The copying
+    // scopes keep two slots of at most 1 GiB, so that copies overlap compute.
+    const bool copies = scope != DBD_SCOPE_KERNEL;
+    const int nslots_dev = copies ? 2 : 1;
     if (resident) {
         Chunk ch{0, m, 0, nnz};
         chunks.push_back(ch);
     } else {
-        // Output chunks: at most 1 GiB of output (so copies overlap compute)
-        // and at most a share of the remaining device budget per ring slot.
-        const double slot_bytes = std::min(std::max(0.0, dev_avail) / nslots_dev, 1.0 * kGiB);
+        const double slot_bytes =
+            std::min(std::max(0.0, dev_avail) / nslots_dev, copies ? 1.0 * kGiB : std::max(0.0, dev_avail));
         cap_entries = std::max<int64_t>((int64_t)(slot_bytes / 12.0), 1);
         std::vector<int64_t> cpBlk((size_t)c->nblocks + 1);
         // Cp at block boundaries (strided copy of one int64 per block).

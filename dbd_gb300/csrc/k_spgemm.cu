@@ -2292,7 +2292,8 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
         case NB_DENSE:
             if (a.tune.denseMethod == 0) {
                 cudaMemsetAsync(a.ctr + CTR_NUM_RANKWIN, 0, sizeof(uint32_t), s);
-                const int grid = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1));
+                const int per_sm = std::max(1, (int)((227 * 1024) / (kSmemRankWin + 1024)));
+                const int grid = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1) * per_sm);
                 k_num_rankwin<kRankWinThreads, kRankWinWords>
                     <<<(unsigned)grid, kRankWinThreads, kSmemRankWin, s>>>(a, lo, n);
             } else if (a.tune.denseMethod == 1 && a.gBits) {
