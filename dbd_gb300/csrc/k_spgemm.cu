@@ -1711,8 +1711,8 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
     for (;;) {
         if (tid == 0) next = (int32_t)atomicAdd(&a.ctr[CTR_NUM_RANKWIN], 1u);
         __syncthreads();
+        if (next >= count) break;
         const int32_t item = next;
-        if (item >= count) break;
         const int32_t row = a.list[lo + item];
         const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
         const int64_t expect = a.Cp[row + 1] - a.Cp[row];

@@ -258,6 +258,7 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     na.rowLo = ri.lo;
     na.numSms = sms;
     na.rowHi = ri.hi;
+    na.ctr = ctrs;
     for (int bin = NB_TINY; bin < NB_COUNT; ++bin)
         launch_numeric_bin(na, bin, numStart_h[bin], numStart_h[bin + 1], s, &launches);
     NA_CK(cudaMemcpyAsync(hflags, flags, sizeof(int), cudaMemcpyDeviceToHost, s));

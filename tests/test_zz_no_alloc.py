@@ -50,10 +50,22 @@ def noalloc_multiply(torch, lib, A, capacity):
     return rc, n, cp.cpu().numpy(), ci[:max(n, 0)].cpu().numpy(), cv[:max(n, 0)].cpu().numpy()
 
 
+def wide_rows(n=300_000, heavy=40, k=3000, seed=3):
+    """n x n with `heavy` rows of k columns spread over all n columns (their
+    rows of A*A land in the dense-window bin) and two columns in every other
+    row."""
+    rng = np.random.default_rng(seed)
+    rows = [np.repeat(np.arange(heavy), k), np.repeat(np.arange(heavy, n), 2)]
+    cols = [np.concatenate([rng.choice(n, k, replace=False) for _ in range(heavy)]),
+            rng.integers(0, n, 2 * (n - heavy))]
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    return gen._from_coo(n, n, rows, cols, rng.uniform(-1, 1, rows.size))
+
+
 def test_noalloc_matches_regular_entry_point_twice(orc):
     torch = pytest.importorskip("torch")
     lib = _ffi.load()
-    mats = [gen.rmat(14, 8, seed=5), gen.laplacian_2d(128)]
+    mats = [gen.rmat(14, 8, seed=5), gen.laplacian_2d(128), wide_rows()]
     with dbd.Context(cpu_gib=8, gpu_gib=8) as ctx:
         for A in mats:
             ref = ctx.spgemm(A, scope="kernel").C
