@@ -735,18 +735,22 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
 
     std::vector<Chunk> chunks;
     int64_t cap_entries = nnz;
-    // The kernel scope copies nothing out, so one slot takes the whole
-    // remaining budget: few, large chunks, in which the heaviest rows of a
-    // power-law matrix are a small share of a launch's work.  The copying
-    // scopes keep two slots of at most 1 GiB, so that copies overlap compute.
+    // Chunks are large, so that the heaviest rows of a power-law matrix are
+    // a small share of a launch's work.  The kernel scope copies nothing
+    // out: one slot takes the whole remaining budget.  The copying scopes
+    // keep two device slots (a chunk computes while the previous one is
+    // copied) and two host ring slots, each of at most 6 GiB.
     const bool copies = scope != DBD_SCOPE_KERNEL;
     const int nslots_dev = copies ? 2 : 1;
     if (resident) {
         Chunk ch{0, m, 0, nnz};
         chunks.push_back(ch);
     } else {
-        const double slot_bytes =
-            std::min(std::max(0.0, dev_avail) / nslots_dev, copies ? 1.0 * kGiB : std::max(0.0, dev_avail));
+        double slot_bytes = std::max(0.0, dev_avail) / nslots_dev;
+        if (copies) {
+            slot_bytes = std::min(slot_bytes, 6.0 * kGiB);
+            if (!(scope == DBD_SCOPE_D2H && host_fits)) slot_bytes = std::min(slot_bytes, host_budget / 2.0);
+        }
         cap_entries = std::max<int64_t>((int64_t)(slot_bytes / 12.0), 1);
         std::vector<int64_t> cpBlk((size_t)c->nblocks + 1);
         // Cp at block boundaries (strided copy of one int64 per block).
@@ -783,7 +787,7 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         CK(c, c->hCv.ensure(sizeof(double) * (size_t)std::max<int64_t>(nnz, 1)));
         c->host_full = true;
     } else if (scope != DBD_SCOPE_KERNEL) {
-        nhslots = scope == DBD_SCOPE_IO ? 3 : 2;
+        nhslots = 2;
         const double ring = (double)nhslots * 12.0 * (double)slot_entries;
         if (ring > host_budget) return set_err(c, DBD_ERR_BUDGET, "host budget smaller than the output ring");
         CK(c, c->hCi.ensure(sizeof(int32_t) * slot_entries * nhslots));
