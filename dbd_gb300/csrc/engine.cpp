@@ -739,7 +739,9 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     // a small share of a launch's work.  The kernel scope copies nothing
     // out: one slot takes the whole remaining budget.  The copying scopes
     // keep two device slots (a chunk computes while the previous one is
-    // copied) and two host ring slots, each of at most 6 GiB.
+    // copied) and two host ring slots, each a sixth of C clamped to
+    // [1, 6] GiB: at least six chunks overlap their copies with compute
+    // when C is small, and a large C keeps its chunks large.
     const bool copies = scope != DBD_SCOPE_KERNEL;
     const int nslots_dev = copies ? 2 : 1;
     if (resident) {
@@ -748,7 +750,7 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     } else {
         double slot_bytes = std::max(0.0, dev_avail) / nslots_dev;
         if (copies) {
-            slot_bytes = std::min(slot_bytes, 6.0 * kGiB);
+            slot_bytes = std::min(slot_bytes, std::min(6.0 * kGiB, std::max(1.0 * kGiB, 12.0 * (double)nnz / 6.0)));
             if (!(scope == DBD_SCOPE_D2H && host_fits)) slot_bytes = std::min(slot_bytes, host_budget / 2.0);
         }
         cap_entries = std::max<int64_t>((int64_t)(slot_bytes / 12.0), 1);

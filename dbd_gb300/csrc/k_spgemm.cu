@@ -695,42 +695,19 @@ __device__ __forceinline__ bool interval_union_count(const CsrDev &A, const CsrD
 }
 
 // Products of one row for one warp, calling f(j, av) for every product (B
-// position j, A value av) on the lane that owns it.  Row-wise (long B rows):
-// the A entries one after another, the lanes over the B row; f calls of one
-// A entry see distinct columns when B's rows are strictly ascending, and a
-// __syncwarp separates consecutive A entries.  Flattened (short B rows):
-// 32 products of up to 32 A entries per step (Chunk).
+// position j, A value av) on the lane that owns it: 32 products of up to 32
+// A entries per step (Chunk).  Callers with long B rows walk them row-wise
+// themselves.
 template <class F>
-__device__ __forceinline__ void warp_products(const CsrDev &A, const CsrDev &B, int32_t e0, int32_t e1, bool rowwise,
-                                              int lane, F &&f) {
-    if (rowwise) {
-        for (int32_t eb = e0; eb < e1; eb += 32) {
-            int32_t bs = 0, len = 0;
-            double av = 0.0;
-            if (eb + lane < e1) {
-                const int32_t k = A.idx[eb + lane];
-                bs = B.ptr[k];
-                len = B.ptr[k + 1] - bs;
-                av = A.val[eb + lane];
-            }
-            const int n = min(32, e1 - eb);
-            for (int q = 0; q < n; ++q) {
-                const int32_t bq = __shfl_sync(FULL, bs, q);
-                const int32_t lq = __shfl_sync(FULL, len, q);
-                const double aq = __shfl_sync(FULL, av, q);
-                for (int32_t i = lane; i < lq; i += 32) f(bq + i, aq);
-                __syncwarp();
-            }
-        }
-    } else {
-        for (int32_t e = e0; e < e1; e += 32) {
-            const Chunk c = load_chunk(A, B, e, e1, lane);
-            for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
-                const int32_t t = t0 + lane;
-                double av;
-                const int32_t j = chunk_pos(c, t, &av);
-                if (t < c.total) f(j, av);
-            }
+__device__ __forceinline__ void warp_products(const CsrDev &A, const CsrDev &B, int32_t e0, int32_t e1, int lane,
+                                              F &&f) {
+    for (int32_t e = e0; e < e1; e += 32) {
+        const Chunk c = load_chunk(A, B, e, e1, lane);
+        for (int32_t t0 = 0; t0 < c.total; t0 += 32) {
+            const int32_t t = t0 + lane;
+            double av;
+            const int32_t j = chunk_pos(c, t, &av);
+            if (t < c.total) f(j, av);
         }
     }
 }
@@ -810,7 +787,7 @@ __global__ void __launch_bounds__(32 * ROWS) k_sym_flagw(SymArgs a, int32_t begi
             }
         }
     } else {
-        warp_products(a.A, a.B, e0, e1, false, lane, [&](int32_t j, double) {
+        warp_products(a.A, a.B, e0, e1, lane, [&](int32_t j, double) {
             const uint32_t rel = (uint32_t)(bidx[j] - base);
             if (in_window(rel, nb, err)) fb[rel] = 1;
         });
@@ -1442,7 +1419,7 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_densew(NumArgs a, int32_t lo,
             }
         }
     } else {
-        warp_products(a.A, a.B, e0, e1, false, lane,
+        warp_products(a.A, a.B, e0, e1, lane,
                       [&](int32_t j, double av) { add((uint32_t)(bidx[j] - cbase), av, bval[j]); });
     }
     __syncwarp();
