@@ -740,8 +740,9 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     // out: one slot takes the whole remaining budget.  The copying scopes
     // keep two device slots (a chunk computes while the previous one is
     // copied) and two host ring slots, each a sixth of C clamped to
-    // [1, 6] GiB: at least six chunks overlap their copies with compute
-    // when C is small, and a large C keeps its chunks large.
+    // [1, 6] GiB (and within both budgets): at least six chunks overlap
+    // their copies with compute when C is small, and a large C keeps its
+    // chunks large (slots of 11.5 GiB copied slower than 6 GiB ones).
     const bool copies = scope != DBD_SCOPE_KERNEL;
     const int nslots_dev = copies ? 2 : 1;
     if (resident) {
