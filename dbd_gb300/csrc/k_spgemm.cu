@@ -5,26 +5,33 @@
 // merge (:296-329) and its compaction kernel collect (:331-341).  The
 // reference writes every intermediate product to HBM and re-reads it for an
 // FP32 atomic merge into a dense global row, deciding structure by value
-// (|partial sum| < 1e-4).  Here no intermediate product touches HBM:
+// (|partial sum| < 1e-4).  Here no intermediate product touches HBM; each
+// bin of rows (by products, size and column window) has its own kernels:
 //
 //   tiny rows   (P_r <= 32)     one warp per row, products held one per lane,
 //                               duplicates found with __match_any_sync and
 //                               summed in Gustavson order (bit-exact FP64)
-//   warp hash rows              one warp per row, open-addressing hash table
-//                               in shared memory (keys int32, values FP64)
-//   CTA hash rows               one CTA per row; the row's A entries and the
-//                               prefix of their B lengths are staged in shared
-//                               memory so that every thread takes consecutive
-//                               products (coalesced B loads, no idle warps);
-//                               compacted and bitonic-sorted in place
-//   wide rows   (symbolic)      shared bitmap over column windows, bits set
-//                               once per distinct word per warp step
-//   dense rows  (numeric)       shared FP64 dense window of 8192 columns
-//                               swept across the row; one warp per A entry
-//                               scans its sorted B row from a cursor, 32
-//                               products per step, the window's end found by
-//                               ballot; entries with nothing in the window are
-//                               skipped by their next column
+//   narrow rows (small window)  one warp per row over a window of flag bytes
+//                               and FP64 accumulators (symbolic: the length of
+//                               the union of the B rows' column runs when
+//                               each is one run); warp bitmap ranks
+//   short rows  (<= 256 nnz)    one warp per row: symbolic by a shared hash
+//                               table; numeric by expand-sort-compress for
+//                               rows of at most 256 products, else by the
+//                               table, compaction and a bucket sort
+//   CTA rows                    the row's A entries staged in shared memory,
+//                               warps over consecutive products with several
+//                               B loads in flight (warp_range_ld): hash
+//                               tables for narrow-span rows, bitmap + word
+//                               ranks for rows within 2^18 columns (values in
+//                               shared memory or reduced into C in place)
+//   wide rows   (symbolic)      persistent CTAs, a shared bitmap over windows
+//                               of up to 2^20 columns that stays zero between
+//                               rows, kept for the numeric rank kernels
+//   dense rows  (numeric)       persistent CTAs, bitmap ranks over 2^20-column
+//                               windows in shared memory, work per window
+//                               over its non-empty words only, products
+//                               reduced into C in place
 //
 // Structure is decided by index only (a column belongs to a row as soon as a
 // product lands on it).  GB300's FP64 pipe is narrow (about two FP64
