@@ -1225,7 +1225,7 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
     uint32_t *bits = reinterpret_cast<uint32_t *>(smem + L::bytes);
     int32_t *wpre = reinterpret_cast<int32_t *>(bits + maxWords);
     double *vals = reinterpret_cast<double *>(wpre + maxWords);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int32_t row = a.list[lo + blockIdx.x];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
@@ -1260,43 +1260,42 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
         }
     }
 
-    // Ranks: each warp takes a contiguous run of words, lanes read 32
-    // consecutive words per step.
-    const int per = ((nwords + NW - 1) / NW + 31) / 32 * 32;
-    const int wb = min(nwords, warp * per), we = min(nwords, wb + per);
-    int32_t wsum = 0;
-    for (int w = wb + lane; w < we; w += 32) wsum += __popc(bits[w]);
-#pragma unroll
-    for (int d = 16; d; d >>= 1) wsum += __shfl_xor_sync(FULL, wsum, d);
-    int32_t tot;
-    int32_t run = block_excl_scan<THREADS>(lane == 0 ? wsum : 0, &tot, sh);
-    run = __shfl_sync(FULL, run, 0);
-    for (int w0 = wb; w0 < we; w0 += 32) {
-        const int w = w0 + lane;
-        const int32_t pc = w < we ? __popc(bits[w]) : 0;
-        int32_t incl = pc;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int32_t y = __shfl_up_sync(FULL, incl, d);
-            if (lane >= d) incl += y;
+    // Ranks and C's columns, per thread over its own wpt consecutive words
+    // (wpt a power of two, THREADS * wpt >= nwords): one sweep gives the
+    // thread the mask of its non-empty words and their bit count, a block
+    // scan the rank of its first column; then only the non-empty words are
+    // ranked and their columns written, a contiguous run per thread (no
+    // lane waits on a denser word of its neighbours).  Lanes start their
+    // sweeps at different words so that a warp's loads hit 32 banks.
+    int wpt = 1;
+    while (wpt * THREADS < nwords) wpt <<= 1;
+    const int w0 = tid * wpt;
+    const int rot = (lane * wpt) >> 5;
+    uint32_t mask = 0u;
+    int32_t cnt = 0;
+    for (int k = 0; k < wpt; ++k) {
+        const int q = (k + rot) & (wpt - 1);
+        if (w0 + q < nwords) {
+            const uint32_t x = bits[w0 + q];
+            if (x) mask |= 1u << q;
+            cnt += __popc(x);
         }
-        if (w < we) wpre[w] = run + incl - pc;
-        run += __shfl_sync(FULL, incl, 31);
     }
+    int32_t tot;
+    int32_t run = block_excl_scan<THREADS>(cnt, &tot, sh);
     if (tid == 0 && tot != expect) raise(a.err, DEV_COUNT_MISMATCH);
-    __syncthreads();
-
-    // Columns of C's row.
-    for (int w = tid; w < nwords; w += THREADS) {
+    for (uint32_t m = mask; m; m &= m - 1u) {
+        const int w = w0 + __ffs(m) - 1;
         uint32_t word = bits[w];
-        int64_t p = wpre[w];
+        wpre[w] = run;
         while (word) {
             const int b = __ffs(word) - 1;
             word &= word - 1u;
-            if (p < expect) __stcs(&a.Ci[obase + p], obc + (w << 5) + b);
-            ++p;
+            if (run < expect) __stcs(&a.Ci[obase + run], obc + (w << 5) + b);
+            ++run;
         }
     }
+    __syncthreads();
 
     if constexpr (GLOBAL_ACC) {
         double *cv = a.Cv + obase;
