@@ -1010,9 +1010,11 @@ __device__ __forceinline__ void table_write_sorted(NumArgs &a, int32_t row, int3
     }
 }
 
-// Shared bytes per warp of the warp hash kernel: keys, values, the bucket
-// order's output and counters.
-constexpr size_t warp_hash_bytes(int table) { return 12 * (size_t)table + 4 * (size_t)table + 4 * (size_t)kBuckets; }
+// Shared bytes per warp of the warp hash kernel: keys, values and the bucket
+// counters.  Rows of at most kNumWarpMax products (expand-sort-compress) sort
+// into the upper half of the values, which they do not use; the table path
+// sorts its compacted keys in place (bitonic).  7 KB per warp.
+constexpr size_t warp_hash_bytes(int table) { return 12 * (size_t)table + 4 * (size_t)kBuckets; }
 
 // Warp hash rows: keys int32[TABLE] then values double[TABLE] per row.
 // A row of at most kNumWarpMax products, by one warp without a hash table
@@ -1116,12 +1118,12 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t 
     unsigned char *base_ptr = smem + (size_t)g * warp_hash_bytes(TABLE);
     int32_t *keys = reinterpret_cast<int32_t *>(base_ptr);
     double *vals = reinterpret_cast<double *>(base_ptr + 4 * (size_t)TABLE);
-    uint64_t *bbuf = reinterpret_cast<uint64_t *>(base_ptr + 12 * (size_t)TABLE);
-    int *cnts = reinterpret_cast<int *>(bbuf + TABLE / 2);
+    int *cnts = reinterpret_cast<int *>(base_ptr + 12 * (size_t)TABLE);
     const int32_t row = a.list[lo + item];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     if (a.rowP[row] <= kNumWarpMax && TABLE >= 2 * kNumWarpMax) {
-        esc_row<ROWS>(a, row, e0, e1, (int)a.rowP[row], reinterpret_cast<uint64_t *>(keys), vals, cnts, bbuf);
+        esc_row<ROWS>(a, row, e0, e1, (int)a.rowP[row], reinterpret_cast<uint64_t *>(keys), vals, cnts,
+                      reinterpret_cast<uint64_t *>(vals + kNumWarpMax));
         return;
     }
     for (int i = lane; i < TABLE; i += 32) {
@@ -1162,7 +1164,7 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t 
         }
     }
     __syncwarp();
-    table_write_sorted<32, ROWS, TABLE>(a, row, keys, vals, &gcnt[g], lane, cnts, bbuf);
+    table_write_sorted<32, ROWS, TABLE>(a, row, keys, vals, &gcnt[g], lane);
 }
 
 // CTA hash rows: one CTA per row, products spread over all threads.
