@@ -21,7 +21,7 @@ import numpy as np
 from . import _ffi
 from .csr import CSR
 
-__all__ = ["CSR", "Context", "DBDError", "read_CSR", "write_CSR", "lib_path", "SCOPES"]
+__all__ = ["CSR", "Context", "DBDError", "Writer", "read_CSR", "write_CSR", "lib_path", "SCOPES"]
 
 SCOPES = dict(_ffi.SCOPES)
 
@@ -78,6 +78,62 @@ def write_CSR(path, m, fp64=True):
     _check(lib.dbd_write_csr(os.fsencode(path), C.byref(v), 1 if fp64 else 0))
 
 
+class Writer:
+    """The +I/O output writer on the caller's chunks (dbd_writer_*): Idx.output
+    and Val.output appended in row order with aligned O_DIRECT writes (or
+    through the page cache), Ptr.output at finish().  With resume=True a
+    progress manifest makes every append durable; reopening the same product
+    (n_rows, nnz, fingerprint, layout) continues at .resume_row."""
+
+    def __init__(self, out_dir, n_rows, nnz, fingerprint=0, buffered=False, val_fp32=False, ptr32=False,
+                 resume=False, rotate_gib=0.0):
+        self._lib = _ffi.load()
+        flags = ((_ffi.WRITER_BUFFERED if buffered else 0) | (_ffi.WRITER_VAL_FP32 if val_fp32 else 0) |
+                 (_ffi.WRITER_PTR32 if ptr32 else 0) | (_ffi.WRITER_RESUME if resume else 0))
+        h = C.c_void_p()
+        row = C.c_int64()
+        _check(self._lib.dbd_writer_open(os.fsencode(out_dir), int(n_rows), int(nnz), int(fingerprint), flags,
+                                         float(rotate_gib), C.byref(h), C.byref(row)))
+        self._h = h
+        self.resume_row = row.value
+        self.direct = bool(self._lib.dbd_writer_is_direct(h))
+
+    def _check(self, rc):
+        if rc != _ffi.DBD_OK:
+            m = self._lib.dbd_writer_error(self._h)
+            raise DBDError(rc, m.decode() if m else "")
+
+    def append(self, row_end, col_idx, val):
+        ci = np.ascontiguousarray(col_idx, np.int32)
+        cv = np.ascontiguousarray(val, np.float64)
+        if ci.size != cv.size:
+            raise ValueError("col_idx and val differ in length")
+        self._check(self._lib.dbd_writer_append(self._h, int(row_end), ci.ctypes.data, cv.ctypes.data, ci.size))
+
+    def finish(self, row_ptr):
+        rp = np.ascontiguousarray(row_ptr, np.int64)
+        t = C.c_double()
+        self._check(self._lib.dbd_writer_finish(self._h, rp.ctypes.data, C.byref(t)))
+        return t.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.dbd_writer_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Result:
     """Product of one multiply: C (host CSR with int64 row_ptr) and the stats."""
 
@@ -112,7 +168,8 @@ class Context:
     """A libdbd context: device, budgets, streams, buffers (one per host thread)."""
 
     def __init__(self, cpu_gib=28.0, gpu_gib=22.0, rows_per_block=4096, device=0, out_val_fp32=False,
-                 out_ptr32=False, verbose=False, io_rotate_gib=0.0, time_kernels=False):
+                 out_ptr32=False, verbose=False, io_rotate_gib=0.0, time_kernels=False, io_buffered=False,
+                 io_resume=False):
         self._lib = _ffi.load()
         cfg = _ffi.Config()
         self._lib.dbd_config_default(C.byref(cfg))
@@ -121,10 +178,12 @@ class Context:
         cfg.rows_per_block = int(rows_per_block)
         cfg.device = int(device)
         cfg.out_val_fp32 = int(bool(out_val_fp32))
-        cfg.out_ptr32 = int(bool(out_ptr32))
+        cfg.out_ptr32 = int(out_ptr32)
         cfg.verbose = int(bool(verbose))
         cfg.time_kernels = int(bool(time_kernels))
         cfg.io_rotate_gib = float(io_rotate_gib)
+        cfg.io_buffered = int(bool(io_buffered))
+        cfg.io_resume = int(bool(io_resume))
         h = C.c_void_p()
         _check(self._lib.dbd_create(C.byref(cfg), C.byref(h)))
         self._h = h
@@ -301,6 +360,29 @@ class Context:
                 raise ValueError("A and B values must both be host or both be device arrays")
         _check(self._lib.dbd_update_values(self._h, len(a_vals), ta, tb, 1 if on_dev else 0), self._h)
         del ka, kb
+
+    # ---- output digest ----
+    def set_digest(self, device=True, host=False):
+        """Per-row digest of C on every later multiply: on the device after each
+        chunk's kernels (device) and from each chunk's pinned host copy in the
+        d2h / io scopes (host)."""
+        flags = (_ffi.DIGEST_DEVICE if device else 0) | (_ffi.DIGEST_HOST if host else 0)
+        _check(self._lib.dbd_set_digest(self._h, flags), self._h)
+
+    def digest(self, n_rows, which="device"):
+        """The last multiply's digest (C has n_rows rows): dict of per-row
+        numpy arrays count, col_hash, val_hash (uint64), sum, wsum and the
+        count of bad rows."""
+        m = int(n_rows)
+        out = {"count": np.empty(m, np.int64), "col_hash": np.empty(m, np.uint64),
+               "val_hash": np.empty(m, np.uint64), "sum": np.empty(m), "wsum": np.empty(m)}
+        bad = C.c_int64()
+        w = _ffi.DIGEST_DEVICE if which == "device" else _ffi.DIGEST_HOST
+        _check(self._lib.dbd_digest_copy(self._h, w, out["count"].ctypes.data, out["col_hash"].ctypes.data,
+                                         out["val_hash"].ctypes.data, out["sum"].ctypes.data,
+                                         out["wsum"].ctypes.data, C.byref(bad)), self._h)
+        out["bad_rows"] = int(bad.value)
+        return out
 
     def spgemm_files(self, path_a, path_b=None, scope="io", out_dir="."):
         st = _ffi.Stats()

@@ -40,7 +40,8 @@ class CsrHost(C.Structure):
 class Config(C.Structure):
     _fields_ = [("host_gib", C.c_double), ("gpu_gib", C.c_double), ("rows_per_block", C.c_int64),
                 ("device", C.c_int32), ("out_val_fp32", C.c_int32), ("out_ptr32", C.c_int32),
-                ("verbose", C.c_int32), ("time_kernels", C.c_int32), ("io_rotate_gib", C.c_double)]
+                ("verbose", C.c_int32), ("time_kernels", C.c_int32), ("io_rotate_gib", C.c_double),
+                ("io_buffered", C.c_int32), ("io_resume", C.c_int32)]
 
 
 class Tuning(C.Structure):
@@ -63,7 +64,7 @@ class Stats(C.Structure):
                 ("sym_rows_per_bin", C.c_int64 * NUM_BINS), ("bytes_d2h", C.c_int64),
                 ("bytes_written", C.c_int64), ("gpu_launches", C.c_int64), ("t_analysis_ms", C.c_double),
                 ("t_sym_bin_ms", C.c_double * NUM_BINS), ("t_scan_ms", C.c_double),
-                ("t_num_bin_ms", C.c_double * NUM_BINS)]
+                ("t_num_bin_ms", C.c_double * NUM_BINS), ("io_direct", C.c_int64), ("resumed_from_row", C.c_int64)]
 
     def as_dict(self):
         d = {}
@@ -107,7 +108,24 @@ SIGNATURES = {
     "dbd_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "dbd_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "dbd_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Tuning), C.POINTER(C.c_double)]),
+    "dbd_set_digest": (C.c_int, [C.c_void_p, C.c_int]),
+    "dbd_writer_open": (C.c_int, [C.c_char_p, C.c_int64, C.c_int64, C.c_uint64, C.c_int, C.c_double,
+                                  C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
+    "dbd_writer_append": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64]),
+    "dbd_writer_finish": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_double)]),
+    "dbd_writer_is_direct": (C.c_int, [C.c_void_p]),
+    "dbd_writer_error": (C.c_char_p, [C.c_void_p]),
+    "dbd_writer_close": (None, [C.c_void_p]),
+    "dbd_digest_copy": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.POINTER(C.c_int64)]),
 }
+
+DIGEST_DEVICE = 1
+DIGEST_HOST = 2
+WRITER_BUFFERED = 1
+WRITER_VAL_FP32 = 2
+WRITER_PTR32 = 4
+WRITER_RESUME = 8
 
 _lib = None
 

@@ -8,10 +8,16 @@
 // and the timing block of main.cpp:100-106 is printed.  The scope is fixed at
 // build time: -DDBD_CLI_SCOPE=0 (compute), 1 (d2h), 2 (SSpMM, debug).
 //
-// Differences, all deliberate: values are FP64 and Ptr.output is int64 unless
-// DBD_OUT_FP32=1 / DBD_OUT_PTR32=1 ask for the reference's float32 / int32
-// layout; DBD_ROWS_IN_BLOCK selects 4096 (for_small_datasets, default) or 512
-// (for_large_datasets) instead of two builds; DBD_JSON=1 adds one JSON line.
+// The output files keep the reference's layout by default: float32
+// Val.output (values computed in FP64, rounded on write) and int32
+// Ptr.output, which becomes int64 only when nnz(C) >= 2^31, where the
+// reference's own int32 ptrC wraps (distributeWorkload.cpp:207-212).
+// DBD_OUT_FP64=1 writes this library's FP64 values and int64 row pointers.
+// Further switches: DBD_ROWS_IN_BLOCK selects 4096 (for_small_datasets,
+// default) or 512 (for_large_datasets) instead of two builds;
+// DBD_IO_BUFFERED=1 writes through the page cache instead of O_DIRECT;
+// DBD_IO_RESUME=1 keeps a progress manifest and continues an interrupted
+// run; DBD_JSON=1 adds one JSON line.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -64,8 +70,11 @@ int main(int argc, char **argv) {
         usage_and_exit();
     }
     cfg.rows_per_block = (int64_t)env_num("DBD_ROWS_IN_BLOCK", 4096);
-    cfg.out_val_fp32 = (int)env_num("DBD_OUT_FP32", 0);
-    cfg.out_ptr32 = (int)env_num("DBD_OUT_PTR32", 0);
+    const bool fp64 = env_num("DBD_OUT_FP64", 0) != 0;
+    cfg.out_val_fp32 = fp64 ? 0 : 1;
+    cfg.out_ptr32 = fp64 ? 0 : 2;
+    cfg.io_buffered = (int)env_num("DBD_IO_BUFFERED", 0);
+    cfg.io_resume = (int)env_num("DBD_IO_RESUME", 0);
     cfg.io_rotate_gib = env_num("DBD_IO_ROTATE_GIB", 0);
     cfg.device = (int)env_num("DBD_DEVICE", 0);
     cfg.verbose = 1;

@@ -252,6 +252,25 @@ void launch_batch_gather(const BatchPair *pairs, const int64_t *rowOff, const in
 // dst[i] = src[idx[i]] for i < n.
 void launch_gather_i64(const int64_t *src, const int64_t *idx, int64_t n, int64_t *dst, cudaStream_t s);
 
+// ---- output digest (k_digest.cu) ----
+// Per-row digest arrays of C (m entries each) and the count of rows whose
+// columns are not strictly ascending or out of range.
+struct RowDigest {
+    int64_t *count = nullptr;
+    uint64_t *colHash = nullptr;
+    uint64_t *valHash = nullptr;
+    double *sum = nullptr;
+    double *wsum = nullptr;
+    int64_t *bad = nullptr;
+};
+// Digest of rows [r0, r1) whose entries sit at Cp[r] - outBase in Ci / Cv.
+void launch_row_digest(int64_t r0, int64_t r1, const int64_t *Cp, int64_t outBase, const int32_t *Ci,
+                       const double *Cv, int64_t ncols, const RowDigest &d, cudaStream_t s, int num_sms);
+
+// *acc += sum over i < n of mix64(((uint64)i << 32 | w[i]) ^ (salt * G)) (an
+// order-dependent hash of a device array of 32-bit words).
+void launch_hash_words(const uint32_t *w, int64_t n, uint64_t salt, uint64_t *acc, cudaStream_t s);
+
 // One-time kernel attribute setup (dynamic shared memory limits).
 void init_kernel_attributes();
 

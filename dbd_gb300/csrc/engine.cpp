@@ -40,6 +40,7 @@
 #include "../../include/dbd.h"
 #include "dbd_internal.h"
 #include "dbd_io.h"
+#include "writer.h"
 
 using namespace dbd;
 
@@ -115,6 +116,8 @@ struct WriteJob {
     int slot;
     int64_t n;
     cudaEvent_t ready;
+    int64_t r0, r1, c0;  // the chunk's rows and its first entry
+    int64_t lead_i, lead_v;  // its indices / values start this many bytes into their slots
 };
 
 }  // namespace
@@ -166,6 +169,18 @@ struct dbd_ctx {
     int32_t symStart_h[kMaxBins + 1] = {0};
     int32_t numStart_h[kMaxBins + 1] = {0};
     std::vector<int32_t> numTileOff_h;
+
+    // Per-row digest of C (dbd_set_digest): the device digest is taken
+    // after every chunk's numeric kernels, the host digest from every
+    // chunk's pinned copy.  *Ok: the last multiply filled them.
+    int digest = 0;
+    DevBuf dgCount, dgCol, dgVal, dgSum, dgWsum, dgBad;
+    DevBuf hashOut;  // operand hash of a resumable +I/O run
+    bool dgDevOk = false, dgHostOk = false;
+    std::vector<int64_t> hdCount;
+    std::vector<uint64_t> hdCol, hdVal;
+    std::vector<double> hdSum, hdWsum;
+    std::atomic<int64_t> hdBad{0};
 
     // host result / ring
     HostBuf hCp, hCi, hCv;
@@ -608,12 +623,13 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
     fk.join();
 }
 
-// Chunks of consecutive row blocks whose output fits cap_entries.
-int plan_chunks(dbd_ctx *c, const std::vector<int64_t> &cpBlk, int64_t cap_entries, std::vector<Chunk> &out) {
+// Chunks of consecutive row blocks from block b0 on whose output fits cap_entries.
+int plan_chunks(dbd_ctx *c, const std::vector<int64_t> &cpBlk, int64_t cap_entries, int64_t b0,
+                std::vector<Chunk> &out) {
     out.clear();
     const int64_t nb = c->nblocks;
     const int64_t rpb = c->cfg.rows_per_block;
-    int64_t b = 0;
+    int64_t b = b0;
     while (b < nb) {
         int64_t e = b + 1;
         if (cpBlk[(size_t)e] - cpBlk[(size_t)b] > cap_entries)
@@ -630,63 +646,102 @@ int plan_chunks(dbd_ctx *c, const std::vector<int64_t> &cpBlk, int64_t cap_entri
     return DBD_OK;
 }
 
-// ---- the writer thread (+I/O) -------------------------------------------
-
-struct Writer {
-    int fd_idx = -1, fd_val = -1;
-    int64_t off_idx = 0, off_val = 0;
-    int64_t wrap_idx = 0, wrap_val = 0;  // 0: no wrap
-    bool val_fp32 = false;
-    std::vector<float> f32;
-    double busy = 0.0;
-    int64_t bytes = 0;
-    std::atomic<int> error{0};
-    std::string msg;
-
-    int pwrite_all(int fd, const void *src, int64_t n, int64_t &off, int64_t wrap) {
-        const char *p = (const char *)src;
-        while (n > 0) {
-            int64_t at = off, lim = n;
-            if (wrap > 0) {
-                at = off % wrap;
-                lim = std::min<int64_t>(n, wrap - at);
-            }
-            const size_t step = (size_t)std::min<int64_t>(lim, 1 << 30);
-            const ssize_t w = ::pwrite(fd, p, step, (off_t)at);
-            if (w <= 0) {
-                if (w < 0 && errno == EINTR) continue;
-                msg = std::string("pwrite: ") + (w < 0 ? strerror(errno) : "short write");
-                return DBD_ERR_IO;
-            }
-            p += w;
-            n -= w;
-            off += w;
-            bytes += w;
-        }
-        return DBD_OK;
-    }
-
-    int write_chunk(const int32_t *ci, const double *cv, int64_t n) {
-        const auto t0 = Clock::now();
-        int rc = pwrite_all(fd_idx, ci, n * 4, off_idx, wrap_idx);
-        if (!rc) {
-            if (val_fp32) {
-                f32.resize((size_t)n);
-                for (int64_t i = 0; i < n; ++i) f32[(size_t)i] = (float)cv[i];
-                rc = pwrite_all(fd_val, f32.data(), n * 4, off_val, wrap_val);
-            } else {
-                rc = pwrite_all(fd_val, cv, n * 8, off_val, wrap_val);
-            }
-        }
-        busy += seconds_since(t0);
-        return rc;
-    }
-};
-
 std::string join_path(const char *dir, const char *name) {
     std::string d = (dir && *dir) ? dir : ".";
     if (d.back() != '/') d += '/';
     return d + name;
+}
+
+// ---- host digest of C (the same per-row summary as k_digest.cu) ----------
+
+uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+void neumaier_add(double &s, double &c, double x) {
+    const double t = s + x;
+    if (std::fabs(s) >= std::fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+}
+
+// Digest of rows [r0, r1) of a host copy whose entries sit at Cp[r] - base,
+// split over host threads by entries.
+void host_digest_rows(dbd_ctx *c, const int64_t *Cp, int64_t r0, int64_t r1, int64_t base, const int32_t *ci,
+                      const double *cv) {
+    const int64_t ncols = c->ncols;
+    auto run = [&](int64_t a, int64_t b) {
+        int64_t bad = 0;
+        for (int64_t r = a; r < b; ++r) {
+            const int64_t e0 = Cp[r] - base, e1 = Cp[r + 1] - base;
+            uint64_t h = 0, hv = 0;
+            double s = 0, sc = 0, w = 0, wc = 0;
+            bool rbad = false;
+            for (int64_t i = e0; i < e1; ++i) {
+                const int32_t col = ci[i];
+                const double v = cv[i];
+                if (col < 0 || (int64_t)col >= ncols || (i > e0 && ci[i - 1] >= col)) rbad = true;
+                uint64_t bits;
+                memcpy(&bits, &v, sizeof(bits));
+                h += mix64((uint64_t)(uint32_t)col);
+                hv += mix64(bits + 0x9E3779B97F4A7C15ull * ((uint64_t)(uint32_t)col + 1));
+                neumaier_add(s, sc, v);
+                const double wt = 0.5 + (double)(mix64((uint64_t)(uint32_t)col) >> 11) * 0x1.0p-53;
+                neumaier_add(w, wc, v * wt);
+            }
+            c->hdCount[(size_t)r] = e1 - e0;
+            c->hdCol[(size_t)r] = h;
+            c->hdVal[(size_t)r] = hv;
+            c->hdSum[(size_t)r] = s + sc;
+            c->hdWsum[(size_t)r] = w + wc;
+            bad += rbad;
+        }
+        if (bad) c->hdBad += bad;
+    };
+    const int64_t entries = Cp[r1] - Cp[r0];
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)std::thread::hardware_concurrency(), 32,
+                                                                entries / (1 << 20) + 1, r1 - r0}));
+    if (nt <= 1) {
+        run(r0, r1);
+        return;
+    }
+    std::vector<std::thread> th;
+    int64_t a = r0;
+    for (int t = 1; t <= nt; ++t) {
+        // First row whose start passes t/nt of the chunk's entries.
+        const int64_t goal = Cp[r0] + entries * t / nt;
+        int64_t b = t == nt ? r1 : (int64_t)(std::lower_bound(Cp + a, Cp + r1, goal) - Cp);
+        b = std::max(b, a);
+        if (b > a) th.emplace_back(run, a, b);
+        a = b;
+    }
+    for (auto &x : th) x.join();
+}
+
+// Identity of the product for a resumable +I/O run: the operands' sizes,
+// C's row pointers (host copy) and a device hash of the operands' arrays.
+int product_fingerprint(dbd_ctx *c, uint64_t *out) {
+    CK(c, c->hashOut.ensure(sizeof(uint64_t)));
+    CK(c, cudaMemsetAsync(c->hashOut.p, 0, sizeof(uint64_t), c->stream));
+    const CsrDev &A = c->A.dev, &B = opB(c);
+    launch_hash_words(reinterpret_cast<const uint32_t *>(A.ptr), A.m + 1, 1, c->hashOut.as<uint64_t>(), c->stream);
+    launch_hash_words(reinterpret_cast<const uint32_t *>(A.idx), A.nnz, 2, c->hashOut.as<uint64_t>(), c->stream);
+    launch_hash_words(reinterpret_cast<const uint32_t *>(A.val), 2 * A.nnz, 3, c->hashOut.as<uint64_t>(), c->stream);
+    launch_hash_words(reinterpret_cast<const uint32_t *>(B.ptr), B.m + 1, 4, c->hashOut.as<uint64_t>(), c->stream);
+    launch_hash_words(reinterpret_cast<const uint32_t *>(B.idx), B.nnz, 5, c->hashOut.as<uint64_t>(), c->stream);
+    launch_hash_words(reinterpret_cast<const uint32_t *>(B.val), 2 * B.nnz, 6, c->hashOut.as<uint64_t>(), c->stream);
+    c->launches += 6;
+    uint64_t h = 0;
+    CK(c, cudaMemcpyAsync(&h, c->hashOut.p, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    const int64_t *cp = c->hCp.as<int64_t>();
+    for (int64_t r = 0; r <= c->m; ++r) h += mix64((uint64_t)cp[r] ^ mix64((uint64_t)r));
+    for (int64_t x : {c->m, c->ncols, c->nnzC, c->products, A.nnz, B.nnz}) h = mix64(h ^ (uint64_t)x);
+    *out = h;
+    return DBD_OK;
 }
 
 // ---- stage 3: the distributor --------------------------------------------
@@ -733,6 +788,46 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     const bool resident = out_bytes <= std::max(0.0, dev_avail) && scope == DBD_SCOPE_KERNEL;
     const bool host_fits = out_bytes + 8.0 * (double)(m + 1) <= host_budget;
 
+    const bool copies = scope != DBD_SCOPE_KERNEL;
+    int64_t bytes_d2h = 0;
+    // The copying scopes bring all of C's row pointers to the host first:
+    // Ptr.output, the host digest and a resumed run's start need them.
+    if (copies) {
+        CK(c, c->hCp.ensure(sizeof(int64_t) * (size_t)(m + 1)));
+        CK(c, cudaMemcpyAsync(c->hCp.p, c->Cp.p, sizeof(int64_t) * (size_t)(m + 1), cudaMemcpyDeviceToHost,
+                              c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+        bytes_d2h += 8 * (m + 1);
+    }
+    // The +I/O writer opens before the chunks are planned: a resumed run
+    // starts after the last row its files hold durably.
+    struct WriterGuard {
+        ChunkWriter *w = nullptr;
+        ~WriterGuard() { writer_close(w); }
+    } wg;
+    int64_t resume_row = 0;
+    if (scope == DBD_SCOPE_IO) {
+        WriterOpts wo;
+        wo.direct = c->cfg.io_buffered == 0;
+        wo.val_fp32 = c->cfg.out_val_fp32 != 0;
+        wo.ptr32 = c->cfg.out_ptr32 == 1 || (c->cfg.out_ptr32 == 2 && nnz <= INT32_MAX);
+        wo.rotate_bytes = c->cfg.io_rotate_gib > 0 ? (int64_t)(c->cfg.io_rotate_gib * kGiB) : 0;
+        wo.resume = c->cfg.io_resume != 0;
+        wo.m = m;
+        wo.nnz = nnz;
+        if (wo.resume) {
+            rc = product_fingerprint(c, &wo.fingerprint);
+            if (rc) return rc;
+        }
+        std::string err;
+        rc = writer_open(out_dir ? out_dir : ".", wo, &wg.w, &resume_row, &err);
+        if (rc) return set_err(c, rc, err);
+        if (resume_row % c->cfg.rows_per_block != 0 && resume_row != m)
+            return set_err(c, DBD_ERR_INVALID, "the progress manifest does not end on a row block");
+    }
+    ChunkWriter *wr = wg.w;
+    const int64_t b0 = resume_row / c->cfg.rows_per_block;
+
     std::vector<Chunk> chunks;
     int64_t cap_entries = nnz;
     // Chunks are large, so that the heaviest rows of a power-law matrix are
@@ -743,7 +838,6 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     // [1, 6] GiB (and within both budgets): at least six chunks overlap
     // their copies with compute when C is small, and a large C keeps its
     // chunks large (slots of 11.5 GiB copied slower than 6 GiB ones).
-    const bool copies = scope != DBD_SCOPE_KERNEL;
     const int nslots_dev = copies ? 2 : 1;
     if (resident) {
         Chunk ch{0, m, 0, nnz};
@@ -756,22 +850,26 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         }
         cap_entries = std::max<int64_t>((int64_t)(slot_bytes / 12.0), 1);
         std::vector<int64_t> cpBlk((size_t)c->nblocks + 1);
-        // Cp at block boundaries (strided copy of one int64 per block).
-        if (c->nblocks > 0) {
+        // Cp at block boundaries (from the host copy, or a strided copy of
+        // one int64 per block).
+        if (copies) {
+            for (int64_t b = 0; b < c->nblocks; ++b)
+                cpBlk[(size_t)b] = c->hCp.as<int64_t>()[b * c->cfg.rows_per_block];
+        } else if (c->nblocks > 0) {
             const size_t pitch = sizeof(int64_t) * (size_t)c->cfg.rows_per_block;
             CK(c, cudaMemcpy2DAsync(cpBlk.data(), sizeof(int64_t), c->Cp.p, pitch, sizeof(int64_t),
                                     (size_t)c->nblocks, cudaMemcpyDeviceToHost, c->stream));
+            CK(c, cudaStreamSynchronize(c->stream));
         }
         cpBlk[(size_t)c->nblocks] = nnz;
-        CK(c, cudaStreamSynchronize(c->stream));
         int64_t maxblk = 0;
-        for (int64_t b = 0; b < c->nblocks; ++b) maxblk = std::max(maxblk, cpBlk[(size_t)b + 1] - cpBlk[(size_t)b]);
+        for (int64_t b = b0; b < c->nblocks; ++b) maxblk = std::max(maxblk, cpBlk[(size_t)b + 1] - cpBlk[(size_t)b]);
         if (maxblk > cap_entries) {
             if ((double)maxblk * 12.0 * nslots_dev > std::max(0.0, dev_avail))
                 return set_err(c, DBD_ERR_BUDGET, "a row block's output does not fit the GPU budget");
             cap_entries = maxblk;
         }
-        rc = plan_chunks(c, cpBlk, cap_entries, chunks);
+        rc = plan_chunks(c, cpBlk, cap_entries, b0, chunks);
         if (rc) return rc;
     }
     c->stats.n_chunks = (int32_t)chunks.size();
@@ -784,45 +882,65 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     // Host side of D2H / IO.
     c->host_full = false;
     int nhslots = 0;
+    // Ring slots leave 4 KiB of lead room on both sides of a chunk, so that
+    // an O_DIRECT writer finds every chunk at its file offset modulo 4 KiB.
+    const size_t si = (size_t)writer_slot_bytes((int64_t)slot_entries, 4);
+    const size_t sv = (size_t)writer_slot_bytes((int64_t)slot_entries, 8);
     if (scope == DBD_SCOPE_D2H && host_fits) {
-        CK(c, c->hCp.ensure(sizeof(int64_t) * (size_t)(m + 1)));
         CK(c, c->hCi.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1)));
         CK(c, c->hCv.ensure(sizeof(double) * (size_t)std::max<int64_t>(nnz, 1)));
         c->host_full = true;
     } else if (scope != DBD_SCOPE_KERNEL) {
         nhslots = 2;
-        const double ring = (double)nhslots * 12.0 * (double)slot_entries;
+        const double ring = (double)nhslots * (double)(si + sv);
         if (ring > host_budget) return set_err(c, DBD_ERR_BUDGET, "host budget smaller than the output ring");
-        CK(c, c->hCi.ensure(sizeof(int32_t) * slot_entries * nhslots));
-        CK(c, c->hCv.ensure(sizeof(double) * slot_entries * nhslots));
-        CK(c, c->hCp.ensure(sizeof(int64_t) * (size_t)(m + 1)));
+        CK(c, c->hCi.ensure(si * nhslots));
+        CK(c, c->hCv.ensure(sv * nhslots));
     }
 
-    // Writer thread state.
-    Writer wr;
+    // Digests of this multiply.
+    c->dgDevOk = c->dgHostOk = false;
+    const bool dev_dg = (c->digest & DBD_DIGEST_DEVICE) != 0;
+    const bool host_dg = (c->digest & DBD_DIGEST_HOST) != 0 && scope != DBD_SCOPE_KERNEL;
+    RowDigest rd;
+    if (dev_dg) {
+        const size_t mm = (size_t)std::max<int64_t>(m, 1);
+        CK(c, c->dgCount.ensure(sizeof(int64_t) * mm));
+        CK(c, c->dgCol.ensure(sizeof(uint64_t) * mm));
+        CK(c, c->dgVal.ensure(sizeof(uint64_t) * mm));
+        CK(c, c->dgSum.ensure(sizeof(double) * mm));
+        CK(c, c->dgWsum.ensure(sizeof(double) * mm));
+        CK(c, c->dgBad.ensure(sizeof(int64_t)));
+        CK(c, cudaMemsetAsync(c->dgBad.p, 0, sizeof(int64_t), c->stream));
+        rd.count = c->dgCount.as<int64_t>();
+        rd.colHash = c->dgCol.as<uint64_t>();
+        rd.valHash = c->dgVal.as<uint64_t>();
+        rd.sum = c->dgSum.as<double>();
+        rd.wsum = c->dgWsum.as<double>();
+        rd.bad = c->dgBad.as<int64_t>();
+    }
+    if (host_dg) {
+        c->hdCount.assign((size_t)m, 0);
+        c->hdCol.assign((size_t)m, 0);
+        c->hdVal.assign((size_t)m, 0);
+        c->hdSum.assign((size_t)m, 0.0);
+        c->hdWsum.assign((size_t)m, 0.0);
+        c->hdBad = 0;
+    }
+    // Host slots are handed to a consumer thread (file writes, host digest)
+    // unless the whole product lands in host memory.
+    const bool consume = scope == DBD_SCOPE_IO || (host_dg && !c->host_full);
+
+    // Consumer thread state.
+    std::atomic<int> werr{0};
+    std::string wmsg;
     std::mutex mu;
     std::condition_variable cv;
     std::deque<WriteJob> jobs;
     std::vector<int64_t> slot_owner((size_t)std::max(nhslots, 1), -1);  // chunk using host slot, -1 free
     bool done = false;
     std::thread th;
-    if (scope == DBD_SCOPE_IO) {
-        const std::string pi = join_path(out_dir, "Idx.output"), pv = join_path(out_dir, "Val.output");
-        unlink(join_path(out_dir, "Ptr.output").c_str());
-        wr.fd_idx = open(pi.c_str(), O_CREAT | O_TRUNC | O_WRONLY, 0644);
-        wr.fd_val = open(pv.c_str(), O_CREAT | O_TRUNC | O_WRONLY, 0644);
-        if (wr.fd_idx < 0 || wr.fd_val < 0) {
-            if (wr.fd_idx >= 0) close(wr.fd_idx);
-            if (wr.fd_val >= 0) close(wr.fd_val);
-            return set_err(c, DBD_ERR_IO, "cannot create output files in " + std::string(out_dir ? out_dir : "."));
-        }
-        wr.val_fp32 = c->cfg.out_val_fp32 != 0;
-        if (c->cfg.io_rotate_gib > 0) {
-            const int64_t rot = (int64_t)(c->cfg.io_rotate_gib * kGiB);
-            const int64_t vb = wr.val_fp32 ? 4 : 8;
-            wr.wrap_idx = std::max<int64_t>(4096, (rot * 4 / (4 + vb)) / 4096 * 4096);
-            wr.wrap_val = std::max<int64_t>(4096, (rot * vb / (4 + vb)) / 4096 * 4096);
-        }
+    if (consume) {
         th = std::thread([&]() {
             for (;;) {
                 WriteJob j;
@@ -833,14 +951,23 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
                     j = jobs.front();
                     jobs.pop_front();
                 }
-                if (cudaEventSynchronize(j.ready) != cudaSuccess && !wr.error) {
-                    wr.error = DBD_ERR_CUDA;
-                    wr.msg = "writer: copy event failed";
+                if (cudaEventSynchronize(j.ready) != cudaSuccess && !werr) {
+                    wmsg = "writer: copy event failed";
+                    werr = DBD_ERR_CUDA;
                 }
-                if (!wr.error) {
-                    const size_t so = (size_t)j.slot * slot_entries;
-                    int e = wr.write_chunk(c->hCi.as<int32_t>() + so, c->hCv.as<double>() + so, j.n);
-                    if (e) wr.error = e;
+                char *ib = c->hCi.as<char>() + (size_t)j.slot * si;
+                char *vb = c->hCv.as<char>() + (size_t)j.slot * sv;
+                if (!werr && host_dg)
+                    host_digest_rows(c, c->hCp.as<int64_t>(), j.r0, j.r1, j.c0,
+                                     reinterpret_cast<const int32_t *>(ib + j.lead_i),
+                                     reinterpret_cast<const double *>(vb + j.lead_v));
+                if (!werr && wr) {
+                    std::string err;
+                    int e = writer_append(wr, ib, vb, j.n, j.r1, &err);
+                    if (e) {
+                        wmsg = err;
+                        werr = e;
+                    }
                 }
                 {
                     std::lock_guard<std::mutex> lk(mu);
@@ -858,7 +985,6 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         cudaEventCreateWithFlags(&evCopy[i], cudaEventDisableTiming);
     }
     double t_d2h_issue = 0.0;
-    int64_t bytes_d2h = 0;
     CK(c, cudaEventRecord(c->evNumA, c->stream));
     int loop_rc = DBD_OK;
     for (size_t i = 0; i < chunks.size() && !loop_rc; ++i) {
@@ -870,27 +996,34 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         if (!resident && i >= (size_t)nslots && scope != DBD_SCOPE_KERNEL)
             cudaStreamWaitEvent(c->stream, evCopy[i - nslots], 0);
         numeric_rows(c, ch.r0, ch.r1, ch.c0, dCi, dCv);
+        if (dev_dg) {
+            launch_row_digest(ch.r0, ch.r1, c->Cp.as<int64_t>(), ch.c0, dCi, dCv, c->ncols, rd, c->stream,
+                              c->num_sms);
+            c->launches++;
+        }
         cudaEventRecord(evNum[i], c->stream);
         if (scope == DBD_SCOPE_KERNEL) continue;
         const int64_t n = ch.c1 - ch.c0;
         int32_t *hCi;
         double *hCv;
         int hs = 0;
+        const int64_t lead_i = wr ? writer_lead_for(wr, ch.c0, 0) : 0;
+        const int64_t lead_v = wr ? writer_lead_for(wr, ch.c0, 1) : 0;
         if (c->host_full) {
             hCi = c->hCi.as<int32_t>() + ch.c0;
             hCv = c->hCv.as<double>() + ch.c0;
         } else {
             hs = (int)(i % nhslots);
-            if (scope == DBD_SCOPE_IO) {
+            if (consume) {
                 std::unique_lock<std::mutex> lk(mu);
-                cv.wait(lk, [&] { return slot_owner[(size_t)hs] < 0 || wr.error; });
+                cv.wait(lk, [&] { return slot_owner[(size_t)hs] < 0 || werr; });
                 slot_owner[(size_t)hs] = (int64_t)i;
             } else if (i >= (size_t)nhslots) {
                 // d2h scope with a ring: the host slot is overwritten, as the
                 // reference's bin/d2h reuses one pinned buffer (preProc.cu:94-95).
             }
-            hCi = c->hCi.as<int32_t>() + (size_t)hs * slot_entries;
-            hCv = c->hCv.as<double>() + (size_t)hs * slot_entries;
+            hCi = reinterpret_cast<int32_t *>(c->hCi.as<char>() + (size_t)hs * si + lead_i);
+            hCv = reinterpret_cast<double *>(c->hCv.as<char>() + (size_t)hs * sv + lead_v);
         }
         const auto ti = Clock::now();
         cudaStreamWaitEvent(c->copy_stream, evNum[i], 0);
@@ -904,25 +1037,18 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         cudaEventRecord(evCopy[i], c->copy_stream);
         bytes_d2h += 12 * n;
         t_d2h_issue += seconds_since(ti);
-        if (scope == DBD_SCOPE_IO) {
+        if (consume) {
             {
                 std::lock_guard<std::mutex> lk(mu);
-                jobs.push_back(WriteJob{(int64_t)i, hs, n, evCopy[i]});
+                jobs.push_back(WriteJob{(int64_t)i, hs, n, evCopy[i], ch.r0, ch.r1, ch.c0, lead_i, lead_v});
             }
             cv.notify_all();
         }
     }
     CK(c, cudaEventRecord(c->evNumB, c->stream));
-    // Row pointer of C to the host for D2H / IO.
-    if (scope != DBD_SCOPE_KERNEL) {
-        cudaStreamWaitEvent(c->copy_stream, c->evSym, 0);
-        CK(c, cudaMemcpyAsync(c->hCp.p, c->Cp.p, sizeof(int64_t) * (size_t)(m + 1), cudaMemcpyDeviceToHost,
-                              c->copy_stream));
-        bytes_d2h += 8 * (m + 1);
-    }
     cudaError_t se = cudaStreamSynchronize(c->stream);
     cudaError_t ce = cudaStreamSynchronize(c->copy_stream);
-    if (scope == DBD_SCOPE_IO) {
+    if (consume) {
         {
             std::lock_guard<std::mutex> lk(mu);
             done = true;
@@ -937,55 +1063,20 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     if (loop_rc) return loop_rc;
     if (se != cudaSuccess) return cuda_fail(c, se, "compute stream");
     if (ce != cudaSuccess) return cuda_fail(c, ce, "copy stream");
+    if (host_dg && c->host_full && m > 0)
+        host_digest_rows(c, c->hCp.as<int64_t>(), 0, m, 0, c->hCi.as<int32_t>(), c->hCv.as<double>());
+    c->dgDevOk = dev_dg;
+    c->dgHostOk = host_dg && !werr;
     rc = check_device_err(c, "numeric");
-    if (rc) {
-        if (wr.fd_idx >= 0) close(wr.fd_idx);
-        if (wr.fd_val >= 0) close(wr.fd_val);
-        return rc;
-    }
+    if (rc) return rc;
     if (scope == DBD_SCOPE_IO) {
-        int rc2 = wr.error;
-        std::string msg = wr.msg;
-        // Ptr.output (write_Ptr, writeFile.cpp:177-196).
-        const auto tp = Clock::now();
-        if (!rc2) {
-            const std::string pp = join_path(out_dir, "Ptr.output");
-            const int fd = open(pp.c_str(), O_CREAT | O_TRUNC | O_WRONLY, 0644);
-            if (fd < 0) {
-                rc2 = DBD_ERR_IO;
-                msg = "cannot create Ptr.output";
-            } else {
-                int64_t off = 0;
-                if (c->cfg.out_ptr32) {
-                    if (nnz > INT32_MAX) {
-                        rc2 = DBD_ERR_OVERFLOW;
-                        msg = "nnz(C) does not fit a 32-bit Ptr.output";
-                    } else {
-                        std::vector<int32_t> p32((size_t)m + 1);
-                        const int64_t *p = c->hCp.as<int64_t>();
-                        for (int64_t r = 0; r <= m; ++r) p32[(size_t)r] = (int32_t)p[r];
-                        rc2 = wr.pwrite_all(fd, p32.data(), 4 * (m + 1), off, 0);
-                    }
-                } else {
-                    rc2 = wr.pwrite_all(fd, c->hCp.p, 8 * (m + 1), off, 0);
-                }
-                wr.busy += seconds_since(tp);
-                const auto tf = Clock::now();
-                if (!rc2 && (fsync(fd) != 0 || fsync(wr.fd_idx) != 0 || fsync(wr.fd_val) != 0)) {
-                    rc2 = DBD_ERR_IO;
-                    msg = std::string("fsync: ") + strerror(errno);
-                }
-                c->stats.t_fsync = seconds_since(tf);
-                if (close(fd) != 0 && !rc2) {
-                    rc2 = DBD_ERR_IO;
-                    msg = "close Ptr.output";
-                }
-            }
-        }
-        if (close(wr.fd_idx) != 0 && !rc2) rc2 = DBD_ERR_IO;
-        if (close(wr.fd_val) != 0 && !rc2) rc2 = DBD_ERR_IO;
-        c->stats.t_write_file = wr.busy;
-        c->stats.bytes_written = wr.bytes;
+        int rc2 = werr;
+        std::string msg = wmsg;
+        if (!rc2) rc2 = writer_finish(wr, c->hCp.as<int64_t>(), &c->stats.t_fsync, &msg);
+        c->stats.t_write_file = writer_busy(wr);
+        c->stats.bytes_written = writer_bytes(wr);
+        c->stats.io_direct = writer_is_direct(wr) ? 1 : 0;
+        c->stats.resumed_from_row = resume_row;
         if (rc2) return set_err(c, rc2, msg.empty() ? "output write failed" : msg);
     }
     c->stats.t_kernel_exec = seconds_since(t0);
@@ -1107,7 +1198,8 @@ void dbd_destroy(dbd_ctx *c) {
                       &c->symTileOff, &c->numTileOff, &c->symStart, &c->numStart, &c->part, &c->Cp, &c->cursor,
                       &c->err, &c->blockP, &c->flags, &c->Ci, &c->Cv, &c->wideBits, &c->wideSlot, &c->adjG,
                       &c->adjA, &c->adjB, &c->rowLo, &c->rowHi, &c->A.bmin, &c->A.bmax, &c->B.bmin, &c->B.bmax,
-                      &c->ctrs, &c->gdense})
+                      &c->ctrs, &c->gdense, &c->dgCount, &c->dgCol, &c->dgVal, &c->dgSum, &c->dgWsum,
+                      &c->dgBad, &c->hashOut})
         b->release();
     c->hCp.release();
     c->hCi.release();
@@ -1215,6 +1307,13 @@ int dbd_result(dbd_ctx *c, dbd_csr_out *o) {
 
 int dbd_result_copy(dbd_ctx *c, int64_t *row_ptr, int32_t *col_idx, double *val) {
     if (!c) return DBD_ERR_INVALID;
+    if (!col_idx && !val && row_ptr) {
+        // The row pointers stay on the device after any multiply, streamed or not.
+        if (c->m <= 0 && c->nnzC == 0 && !c->Cp.p) return set_err(c, DBD_ERR_INVALID, "no multiply yet");
+        cudaSetDevice(c->cfg.device);
+        CK(c, cudaMemcpy(row_ptr, c->Cp.p, sizeof(int64_t) * (size_t)(c->m + 1), cudaMemcpyDefault));
+        return DBD_OK;
+    }
     dbd_csr_out o;
     int rc = dbd_result(c, &o);
     if (rc) return rc;
@@ -1224,6 +1323,40 @@ int dbd_result_copy(dbd_ctx *c, int64_t *row_ptr, int32_t *col_idx, double *val)
         if (col_idx) CK(c, cudaMemcpy(col_idx, o.col_idx, sizeof(int32_t) * (size_t)o.nnz, k));
         if (val) CK(c, cudaMemcpy(val, o.val, sizeof(double) * (size_t)o.nnz, k));
     }
+    return DBD_OK;
+}
+
+int dbd_set_digest(dbd_ctx *c, int flags) {
+    if (!c || (flags & ~(DBD_DIGEST_DEVICE | DBD_DIGEST_HOST))) return DBD_ERR_INVALID;
+    c->digest = flags;
+    return DBD_OK;
+}
+
+int dbd_digest_copy(dbd_ctx *c, int which, int64_t *count, uint64_t *col_hash, uint64_t *val_hash, double *sum,
+                    double *wsum, int64_t *bad_rows) {
+    if (!c || (which != DBD_DIGEST_DEVICE && which != DBD_DIGEST_HOST)) return DBD_ERR_INVALID;
+    const size_t m = (size_t)c->m;
+    if (which == DBD_DIGEST_HOST) {
+        if (!c->dgHostOk) return set_err(c, DBD_ERR_INVALID, "the last multiply took no host digest");
+        if (count) memcpy(count, c->hdCount.data(), sizeof(int64_t) * m);
+        if (col_hash) memcpy(col_hash, c->hdCol.data(), sizeof(uint64_t) * m);
+        if (val_hash) memcpy(val_hash, c->hdVal.data(), sizeof(uint64_t) * m);
+        if (sum) memcpy(sum, c->hdSum.data(), sizeof(double) * m);
+        if (wsum) memcpy(wsum, c->hdWsum.data(), sizeof(double) * m);
+        if (bad_rows) *bad_rows = c->hdBad.load();
+        return DBD_OK;
+    }
+    if (!c->dgDevOk) return set_err(c, DBD_ERR_INVALID, "the last multiply took no device digest");
+    cudaSetDevice(c->cfg.device);
+    const cudaMemcpyKind k = cudaMemcpyDefault;
+    if (m) {
+        if (count) CK(c, cudaMemcpy(count, c->dgCount.p, sizeof(int64_t) * m, k));
+        if (col_hash) CK(c, cudaMemcpy(col_hash, c->dgCol.p, sizeof(uint64_t) * m, k));
+        if (val_hash) CK(c, cudaMemcpy(val_hash, c->dgVal.p, sizeof(uint64_t) * m, k));
+        if (sum) CK(c, cudaMemcpy(sum, c->dgSum.p, sizeof(double) * m, k));
+        if (wsum) CK(c, cudaMemcpy(wsum, c->dgWsum.p, sizeof(double) * m, k));
+    }
+    if (bad_rows) CK(c, cudaMemcpy(bad_rows, c->dgBad.p, sizeof(int64_t), cudaMemcpyDeviceToHost));
     return DBD_OK;
 }
 

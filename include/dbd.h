@@ -94,12 +94,16 @@ typedef struct {
     int64_t rows_per_block;   /* 4096 (for_small_datasets) or 512 (for_large_datasets) */
     int32_t device;           /* CUDA device ordinal */
     int32_t out_val_fp32;     /* Val.output as float32 (reference layout) instead of FP64 */
-    int32_t out_ptr32;        /* Ptr.output as int32 (reference layout; fails if nnz(C) >= 2^31) */
+    int32_t out_ptr32;        /* Ptr.output as int32 (reference layout): 1 always (fails if nnz(C) >= 2^31),
+                                 2 when nnz(C) < 2^31 and int64 otherwise */
     int32_t verbose;          /* print the reference's progress lines */
     int32_t time_kernels;     /* record CUDA events around every kernel family (dbd_stats.t_*_bin_ms);
                                  the bins then run one after another on the context's stream, so
                                  each time is that kernel's own duration (for profiling runs) */
     double io_rotate_gib;     /* > 0: +I/O output files wrap after this many GiB (disk smaller than C) */
+    int32_t io_buffered;      /* +I/O through the page cache instead of aligned O_DIRECT writes */
+    int32_t io_resume;        /* +I/O keeps a progress manifest and continues an interrupted run
+                                 (DBD_WRITER_RESUME; not with io_rotate_gib) */
 } dbd_config;
 
 /* Number of row bins the categoriser produces for the symbolic and numeric
@@ -135,6 +139,8 @@ typedef struct {
     double t_sym_bin_ms[DBD_NUM_BINS];  /* with time_kernels: symbolic kernel of each bin */
     double t_scan_ms;         /* with time_kernels: row_ptr scan + numeric binning */
     double t_num_bin_ms[DBD_NUM_BINS];  /* with time_kernels: numeric kernels of each bin, summed over chunks */
+    int64_t io_direct;        /* +I/O: 1 when the files were written with O_DIRECT */
+    int64_t resumed_from_row; /* +I/O with io_resume: the row an earlier run's manifest let this one start at */
 } dbd_stats;
 
 /* ---- lifecycle ---------------------------------------------------------- */
@@ -217,7 +223,9 @@ int dbd_result(dbd_ctx *ctx, dbd_csr_out *c);
  * caller-provided arrays, host or device memory, sized from dbd_result:
  * row_ptr n_rows+1, col_idx and val nnz entries; any of them may be NULL.
  * For FFI callers that cannot read the context's memory; the reference hands
- * results back only through Ptr/Idx/Val.output. */
+ * results back only through Ptr/Idx/Val.output.  With col_idx and val both
+ * NULL, row_ptr is copied after any multiply, including one whose C was
+ * streamed out in chunks (the row pointers stay on the device). */
 int dbd_result_copy(dbd_ctx *ctx, int64_t *row_ptr, int32_t *col_idx, double *val);
 
 int dbd_get_stats(const dbd_ctx *ctx, dbd_stats *st);
@@ -348,6 +356,73 @@ int dbd_autotune(dbd_ctx *ctx, int repeats, dbd_tuning *best, double *best_ms);
  * multiply, dbd_load_a/b or dbd_spgemm_adjoint's reload drops the graph. */
 int dbd_update_values(dbd_ctx *ctx, int64_t count, const double *const *a_val, const double *const *b_val,
                       int on_device);
+
+/* ---- output digest (no reference counterpart) ----------------------------- */
+
+/* Per-row digest of C, for checking a product that is never whole in any
+ * memory (out-of-core: the device slot and the host ring are recycled chunk
+ * by chunk; the reference checks nothing).  With DBD_DIGEST_DEVICE set, every
+ * multiply summarises each row of C on the device right after its chunk's
+ * numeric kernels; with DBD_DIGEST_HOST set, the D2H and IO scopes summarise
+ * each row again from its pinned host copy (a host thread takes every chunk
+ * before its ring slot is reused).  Per row r:
+ *   count[r]     entries
+ *   col_hash[r]  sum of mix64(col) over the row's entries, mod 2^64
+ *   val_hash[r]  sum of mix64(bits(val) + G * (col + 1)), mod 2^64,
+ *                G = 0x9E3779B97F4A7C15
+ *   sum[r]       sum of the values (compensated summation)
+ *   wsum[r]      sum of val * w(col), w(col) = 0.5 + (mix64(col) >> 11) * 2^-53
+ * where mix64 is SplitMix64's output function.  The hashes do not depend on
+ * entry order, so two digests of the same C agree bit for bit; sum and wsum
+ * equal A*(B*1) and A*(B*w) up to rounding.  *bad_rows counts rows whose
+ * columns are not strictly ascending or fall outside [0, n_cols).  Off by
+ * default; the digest costs one read of C per multiply (device) and host
+ * threads at the copy rate (host). */
+#define DBD_DIGEST_DEVICE 1
+#define DBD_DIGEST_HOST   2
+int dbd_set_digest(dbd_ctx *ctx, int flags);
+
+/* Copies the digest of the last multiply (which = DBD_DIGEST_DEVICE or
+ * DBD_DIGEST_HOST) into host arrays of n_rows entries (any may be NULL). */
+int dbd_digest_copy(dbd_ctx *ctx, int which, int64_t *count, uint64_t *col_hash, uint64_t *val_hash,
+                    double *sum, double *wsum, int64_t *bad_rows);
+
+/* ---- output writer ------------------------------------------------------- */
+
+/* The writer of the +I/O scope on the caller's own chunks: Idx.output and
+ * Val.output appended in row order, Ptr.output at the end.  Replaces
+ * write_File / flush_Buffer / write_Ptr (ZIP:dbd/src/writeFile.cpp:13-196;
+ * the coalescing variant writeFile_binding.cpp:60-160).  dbd_spgemm's IO
+ * scope drives the same writer from its pinned host ring without copies.
+ *
+ * By default every write is 4 KiB-aligned O_DIRECT (the page cache is
+ * bypassed, so the data reaches the device as it is written and the final
+ * fsync is short); filesystems that refuse O_DIRECT get page-cache writes
+ * (dbd_writer_is_direct tells which).  DBD_WRITER_RESUME keeps a progress
+ * manifest (DBD.progress in out_dir): after every append the data is
+ * fdatasync'ed and the manifest records the rows written; opening the same
+ * product again (same n_rows, nnz, fingerprint and flags, files still
+ * holding the recorded bytes) continues there, and *resume_row receives the
+ * first row still to be appended (0 otherwise).  A resumed caller appends
+ * from that row on.  rotate_gib > 0 wraps the two data files at that total
+ * size (disks smaller than C; not with DBD_WRITER_RESUME).  Errors
+ * (ENOSPC, EIO, a short write off the 4 KiB grid) return DBD_ERR_IO with the
+ * message in dbd_writer_error(). */
+typedef struct dbd_writer dbd_writer;
+#define DBD_WRITER_BUFFERED 1   /* page-cache writes instead of O_DIRECT */
+#define DBD_WRITER_VAL_FP32 2   /* Val.output as float32 (the reference layout) */
+#define DBD_WRITER_PTR32    4   /* Ptr.output as int32 (the reference layout; fails if nnz >= 2^31) */
+#define DBD_WRITER_RESUME   8   /* progress manifest; reopening continues after the last durable row */
+int dbd_writer_open(const char *out_dir, int64_t n_rows, int64_t nnz, uint64_t fingerprint, int flags,
+                    double rotate_gib, dbd_writer **w, int64_t *resume_row);
+/* Appends the n entries of the next rows, which end at row row_end. */
+int dbd_writer_append(dbd_writer *w, int64_t row_end, const int32_t *col_idx, const double *val, int64_t n);
+/* Writes Ptr.output (n_rows + 1 row pointers), makes all three files
+ * durable (*t_fsync: seconds in fsync) and removes the manifest. */
+int dbd_writer_finish(dbd_writer *w, const int64_t *row_ptr, double *t_fsync);
+int dbd_writer_is_direct(const dbd_writer *w);
+const char *dbd_writer_error(const dbd_writer *w);
+void dbd_writer_close(dbd_writer *w);
 
 /* ---- allocation-free multiply --------------------------------------------- */
 

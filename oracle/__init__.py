@@ -61,6 +61,10 @@ def lib():
         L.orc_spgemm_numeric.argtypes = [I64, I64, P, P, P, P, P, P, P, P, P, P]
         L.orc_ref_cpu_rows.argtypes = [I64, I64, I64, P, P, P, P, P, P, P, P, P, P, C.c_int]
         L.orc_adjoint.argtypes = [I64, P, P, P, P, P, P, I64, P, P, P, P, P]
+        L.orc_row_col_digest.argtypes = [I64, I64, I64, P, P, P, P, P, P]
+        L.orc_row_sums.argtypes = [I64, P, P, P, I64, P, P, P, C.c_int, P, P]
+        L.orc_col_weight.restype = C.c_double
+        L.orc_col_weight.argtypes = [C.c_int32]
         _orc = L
     return _orc
 
@@ -201,6 +205,54 @@ def adjoint(A, B, Cp, Ci, G):
     return dA[:Ai.size], dB[:Bi.size]
 
 
+def col_weights(cols):
+    """w(c) = 0.5 + (mix64(c) >> 11) * 2^-53 of the library's digest, vectorised."""
+    z = np.asarray(cols).astype(np.uint64)
+    with np.errstate(over="ignore"):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return 0.5 + (z >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+
+
+def mix64(x):
+    """SplitMix64's output function on uint64 arrays (the digest's column hash)."""
+    z = np.asarray(x).astype(np.uint64)
+    with np.errstate(over="ignore"):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def row_col_digest(A, B=None, r0=0, r1=None):
+    """(count, col_hash) of rows [r0, r1) of A*B: distinct columns per row and
+    the sum of mix64(col) over them, without forming C (O(products))."""
+    B = A if B is None else B
+    r1 = A.n_rows if r1 is None else r1
+    Ap, Ai, _ = _csr(A)
+    Bp, Bi, _ = _csr(B)
+    cnt = np.zeros(max(r1 - r0, 1), np.int64)
+    h = np.zeros(max(r1 - r0, 1), np.uint64)
+    lib().orc_row_col_digest(r0, r1, B.n_cols, Ap.ctypes.data, Ai.ctypes.data, Bp.ctypes.data, Bi.ctypes.data,
+                             cnt.ctypes.data, h.ctypes.data)
+    return cnt[:r1 - r0], h[:r1 - r0]
+
+
+def row_sums(A, B=None, weighted=False):
+    """(A*(B*w), |A|*(|B|*w)) per row by compensated sums; w = 1 or the
+    digest's column weights."""
+    B = A if B is None else B
+    Ap, Ai, Av = _csr(A)
+    Bp, Bi, Bv = _csr(B)
+    out = np.zeros(max(A.n_rows, 1))
+    out_abs = np.zeros(max(A.n_rows, 1))
+    lib().orc_row_sums(A.n_rows, Ap.ctypes.data, Ai.ctypes.data, Av.ctypes.data, B.n_rows, Bp.ctypes.data,
+                       Bi.ctypes.data, Bv.ctypes.data, 1 if weighted else 0, out.ctypes.data, out_abs.ctypes.data)
+    return out[:A.n_rows], out_abs[:A.n_rows]
+
+
 # ---- the reference's own CPU code (built only where the reference tree exists) ----
 
 def reference():
@@ -218,8 +270,42 @@ def reference():
         L.ref_divide.argtypes = [C.c_int, C.c_int, P, P, C.c_int, C.c_int, P, P, P, P]
         L.ref_criteria.restype = C.c_int
         L.ref_criteria.argtypes = [C.c_int, P, C.c_longlong]
+        L.ref_cpu_blocks.restype = C.c_int
+        L.ref_cpu_blocks.argtypes = [C.c_int, C.c_int, P, P, P, C.c_int, C.c_int, P, P, P, C.c_int, REF_BLOCK_CB,
+                                     P]
         _ref = L
     return _ref
+
+
+# Callback of ref_cpu_blocks: (r0, r1, cnt, hash, idx, n_idx, dups, user).
+REF_BLOCK_CB = C.CFUNCTYPE(None, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_uint64),
+                           C.POINTER(C.c_int32), C.c_longlong, C.c_longlong, C.c_void_p)
+
+
+def ref_cpu_blocks(A, B=None, rows_per_block=512, on_block=None):
+    """Runs the reference's compute_CPU over A*B block by block of
+    rows_per_block rows and hands each block's canonical output to
+    on_block(r0, r1, cnt, hash, idx, dups): cnt the entries of each row,
+    hash the sum of mix64(col) over each row's entries, idx the rows' columns
+    (each row sorted, duplicates kept), dups the number of repeated columns in
+    the block (0 on quirk-inert inputs).  The arrays are
+    valid only during the call.  Memory: the largest block's products, not
+    the whole product."""
+    L = reference()
+    B = A if B is None else B
+    Ap, Ai, Av = _csr(A, np.float32)
+    Bp, Bi, Bv = _csr(B, np.float32)
+
+    def cb(r0, r1, cnt, hsh, idx, n, dups, user):
+        c = np.ctypeslib.as_array(cnt, shape=(r1 - r0,)) if r1 > r0 else np.zeros(0, np.int32)
+        h = np.ctypeslib.as_array(hsh, shape=(r1 - r0,)) if r1 > r0 else np.zeros(0, np.uint64)
+        i = np.ctypeslib.as_array(idx, shape=(n,)) if n else np.zeros(0, np.int32)
+        on_block(r0, r1, c, h, i, dups)
+    fn = REF_BLOCK_CB(cb)
+    rc = L.ref_cpu_blocks(A.n_rows, A.n_cols, Ap.ctypes.data, Ai.ctypes.data, Av.ctypes.data, B.n_rows, B.n_cols,
+                          Bp.ctypes.data, Bi.ctypes.data, Bv.ctypes.data, int(rows_per_block), fn, None)
+    if rc:
+        raise RuntimeError(f"ref_cpu_blocks failed ({rc})")
 
 
 def ref_divide(A, B=None):

@@ -10,6 +10,7 @@ the shared library into oracle/_ref/.  No reference source is copied into the
 repository.  When the reference tree is absent (as on a machine that only
 receives the repository), it does nothing.
 """
+import json
 import os
 import subprocess
 import sys
@@ -17,20 +18,41 @@ import tempfile
 import zipfile
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ZIP = "/root/reference/DBD_FULL.zip"
+
+
+def reference_root():
+    """The reference checkout: $DBD_REFERENCE_DIR, else the benchmark's
+    reference_path at the repository root; None when neither names a
+    directory that exists."""
+    root = os.environ.get("DBD_REFERENCE_DIR")
+    if not root:
+        try:
+            with open(os.path.join(os.path.dirname(HERE), "BASELINE.json")) as f:
+                root = json.load(f).get("reference_path")
+        except (OSError, ValueError):
+            root = None
+    return root if root and os.path.isdir(root) else None
+
+
+def _ref_zip():
+    root = reference_root()
+    return os.path.join(root, "DBD_FULL.zip") if root else None
+
+
 MEMBERS = ["dbd/src/SSpMM.hpp", "dbd/src/main.cpp", "dbd/src/distributeWorkload.cpp",
            "dbd/src/computeCPU.cpp", "dbd/src/readInput.cpp"]
 OUT = os.path.join(HERE, "_ref", "libdbdref.so")
 
 
 def build(verbose=False):
-    if not os.path.exists(REF_ZIP):
+    ref_zip = _ref_zip()
+    if not ref_zip or not os.path.exists(ref_zip):
         if verbose:
             print("build_ref: reference tree absent; oracle/_ref not built")
         return None
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
     with tempfile.TemporaryDirectory(prefix="dbdref_") as tmp:
-        with zipfile.ZipFile(REF_ZIP) as z:
+        with zipfile.ZipFile(ref_zip) as z:
             for m in MEMBERS:
                 z.extract(m, tmp)
         src = os.path.join(tmp, "dbd", "src")

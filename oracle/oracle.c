@@ -319,3 +319,108 @@ void orc_adjoint(int64_t m,
         }
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Digest of C without forming C (checks of out-of-core products)           */
+/* ------------------------------------------------------------------------ */
+
+/* SplitMix64's output function (Steele, Lea and Flood, OOPSLA 2014): the
+ * column hash of the library's per-row digest of C. */
+static uint64_t orc_mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* Column weight w(c) = 0.5 + (mix64(c) >> 11) * 2^-53, in [0.5, 1.5). */
+double orc_col_weight(int32_t c)
+{
+    return 0.5 + (double)(orc_mix64((uint64_t)(uint32_t)c) >> 11) * 0x1.0p-53;
+}
+
+/* Per row r in [r0, r1) of A*B: cnt[r - r0] = distinct columns its products
+ * reach (nnz of C's row in the index-determined structure of
+ * orc_spgemm_symbolic) and hash[r - r0] = sum of mix64(col) over those
+ * columns, mod 2^64 -- the count and column hash of the library's digest,
+ * without forming or sorting C.  O(products) with one marker array per
+ * thread. */
+void orc_row_col_digest(int64_t r0, int64_t r1, int64_t ncols,
+                        const int32_t *Ap, const int32_t *Ai,
+                        const int32_t *Bp, const int32_t *Bi,
+                        int64_t *cnt, uint64_t *hash)
+{
+    #pragma omp parallel
+    {
+        int64_t *mark = (int64_t *)malloc(sizeof(int64_t) * (size_t)(ncols > 0 ? ncols : 1));
+        for (int64_t c = 0; c < ncols; ++c) mark[c] = -1;
+        #pragma omp for schedule(dynamic, 16)
+        for (int64_t r = r0; r < r1; ++r) {
+            int64_t nz = 0;
+            uint64_t h = 0;
+            for (int64_t e = Ap[r]; e < Ap[r + 1]; ++e) {
+                int32_t k = Ai[e];
+                for (int64_t f = Bp[k]; f < Bp[k + 1]; ++f) {
+                    int32_t c = Bi[f];
+                    if (mark[c] != r) {
+                        mark[c] = r;
+                        ++nz;
+                        h += orc_mix64((uint64_t)(uint32_t)c);
+                    }
+                }
+            }
+            cnt[r - r0] = nz;
+            hash[r - r0] = h;
+        }
+        free(mark);
+    }
+}
+
+/* Neumaier's compensated summation. */
+static void orc_neumaier(double *s, double *c, double x)
+{
+    double t = *s + x;
+    if (fabs(*s) >= fabs(x)) *c += (*s - t) + x;
+    else *c += (x - t) + *s;
+    *s = t;
+}
+
+/* Row sums of C = A*B weighted by column, without forming C:
+ *   y = B * w (w = 1 when weighted == 0, else w(c) = orc_col_weight(c)),
+ *   out[r] = (A * y)[r],  out_abs[r] = (|A| * (|B| * w))[r],
+ * each dot product by compensated summation, so its error stays within a
+ * few units of the last place of out_abs.  These are the library digest's
+ * sum (weighted == 0) and wsum (weighted == 1) up to C's own rounding. */
+void orc_row_sums(int64_t m, const int32_t *Ap, const int32_t *Ai, const double *Av,
+                  int64_t mb, const int32_t *Bp, const int32_t *Bi, const double *Bv,
+                  int weighted, double *out, double *out_abs)
+{
+    double *y = (double *)malloc(sizeof(double) * (size_t)(mb > 0 ? mb : 1));
+    double *ya = (double *)malloc(sizeof(double) * (size_t)(mb > 0 ? mb : 1));
+    #pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t k = 0; k < mb; ++k) {
+        double s = 0, c = 0, sa = 0, ca = 0;
+        for (int64_t f = Bp[k]; f < Bp[k + 1]; ++f) {
+            double w = weighted ? orc_col_weight(Bi[f]) : 1.0;
+            double p = Bv[f] * w;
+            orc_neumaier(&s, &c, p);
+            orc_neumaier(&sa, &ca, fabs(p));
+        }
+        y[k] = s + c;
+        ya[k] = sa + ca;
+    }
+    #pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t r = 0; r < m; ++r) {
+        double s = 0, c = 0, sa = 0, ca = 0;
+        for (int64_t e = Ap[r]; e < Ap[r + 1]; ++e) {
+            int32_t k = Ai[e];
+            orc_neumaier(&s, &c, Av[e] * y[k]);
+            orc_neumaier(&sa, &ca, fabs(Av[e]) * ya[k]);
+        }
+        out[r] = s + c;
+        out_abs[r] = sa + ca;
+    }
+    free(y);
+    free(ya);
+}

@@ -20,6 +20,20 @@ Fixtures written (all small):
                       value-based structure test emits a duplicate column
   lap256_ref.json     checksums of the reference's output for the 256x256-grid
                       Laplacian squared (the benchmark's CPU-runnable workload)
+  rmat18_int_ref.json the reference's output structure for R-MAT scale 18,
+                      edge factor 8, seed 0 with integer values 1..9 (the
+                      quirk-inert form of that workload): sha256 of the
+                      canonical row_ptr (int64) and col_idx (int32)
+  rmat21_int_ref.json the same for R-MAT scale 21, edge factor 16, seed 0 in
+                      blocks of 512 rows (2.65e10 entries, never held whole):
+                      sha256 of the per-row entry counts (int64) and column
+                      hashes (uint64, sum of SplitMix64's mix64 of each column)
+
+    python tests/golden/make_golden.py [--only small|rmat18|rmat21]
+
+The R-MAT records take the reference's compute_CPU about 20 s (scale 18) and
+25 min (scale 21) on 8 cores; each is also checked against the oracle's own
+structure before it is written.
 """
 import hashlib
 import json
@@ -38,7 +52,9 @@ import oracle  # noqa: E402
 from dbd_gb300 import generators as gen  # noqa: E402
 from dbd_gb300.csr import CSR  # noqa: E402
 
-CAGE4 = "/root/reference/bhsparse/cage4.mtx"
+from oracle.build_ref import reference_root  # noqa: E402
+
+CAGE4 = os.path.join(reference_root() or ".", "bhsparse", "cage4.mtx")
 MTX_FIXTURES = ["mtx_general.mtx", "mtx_symmetric.mtx", "mtx_pattern.mtx", "edges.dat"]
 
 
@@ -72,11 +88,57 @@ def digest(*arrays):
     return h.hexdigest()
 
 
+def rmat_structure(scale, edge_factor, rows_per_block, name):
+    """Streams the reference's compute_CPU output of A*A, A = rmat(scale,
+    edge_factor, seed 0, integer values), block by block and records hashes of
+    its canonical structure; asserts it equals the oracle's."""
+    import time
+    A = gen.rmat(scale, edge_factor, seed=0, int_values=True)
+    m = A.n_rows
+    cnt = np.zeros(m, np.int64)
+    chash = np.zeros(m, np.uint64)
+    h_idx = hashlib.sha256()
+    state = {"dups": 0}
+
+    def on_block(r0, r1, c, hh, idx, dups):
+        cnt[r0:r1] = c
+        chash[r0:r1] = hh
+        state["dups"] += int(dups)
+        h_idx.update(np.ascontiguousarray(idx, np.int32).tobytes())
+
+    t0 = time.time()
+    oracle.ref_cpu_blocks(A, rows_per_block=rows_per_block, on_block=on_block)
+    t_ref = time.time() - t0
+    ocnt, ohash = oracle.row_col_digest(A)
+    assert np.array_equal(ocnt, cnt), "reference row counts differ from the oracle's"
+    assert np.array_equal(ohash, chash), "reference column hashes differ from the oracle's"
+    row_ptr = np.zeros(m + 1, np.int64)
+    np.cumsum(cnt, out=row_ptr[1:])
+    rec = {"workload": f"rmat({scale}, {edge_factor}, seed=0, int_values=True) squared through the reference's "
+                       f"compute_CPU in blocks of {rows_per_block} rows, each row's columns sorted",
+           "n_rows": int(m), "nnz_a": int(A.nnz), "products": int(oracle.row_products(A, A)[1]),
+           "nnz_c": int(row_ptr[-1]), "duplicates": state["dups"],
+           "sha256_row_ptr_i64": digest(row_ptr),
+           "sha256_col_idx_i32": h_idx.hexdigest(),
+           "sha256_row_count_i64": digest(cnt),
+           "sha256_row_col_hash_u64": digest(chash),
+           "first_rows": {"count": cnt[:8].tolist(), "col_hash": [str(x) for x in chash[:8]]},
+           "reference_seconds": round(t_ref, 1)}
+    with open(os.path.join(HERE, name), "w") as f:
+        json.dump(rec, f, indent=1)
+    print(json.dumps(rec, indent=1))
+
+
 def main():
     if oracle.reference() is None:
         oracle.build()
     if oracle.reference() is None:
         sys.exit("the reference's CPU code is not built (reference tree absent)")
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only == "rmat18":
+        return rmat_structure(18, 8, 4096, "rmat18_int_ref.json")
+    if only == "rmat21":
+        return rmat_structure(21, 16, 512, "rmat21_int_ref.json")
     A, B = kat_operands()
     save_ref("kat_bhsparse.npz", A, B)
     A, B = quirk_operands()

@@ -169,3 +169,58 @@ def test_rmat_generator_matches_published_statistics():
     assert int((lens == 0).sum()) == 139756
     assert int(lens.max()) == 9628
     assert all(np.all(np.diff(A.col_idx[A.row_ptr[r]:A.row_ptr[r + 1]]) > 0) for r in range(0, A.n_rows, 997))
+
+
+def test_oracle_structure_equals_reference_output_rmat18(orc):
+    """The oracle's index-determined structure of the full R-MAT 2^18 product
+    equals the reference's own compute_CPU output (hashed by
+    tests/golden/make_golden.py on the integer-valued form of the workload)."""
+    with open(os.path.join(GOLDEN, "rmat18_int_ref.json")) as f:
+        ref = json.load(f)
+    A = gen.rmat(18, 8, seed=0)
+    cnt, h = orc.row_col_digest(A)
+    assert int(cnt.sum()) == ref["nnz_c"]
+    assert hashlib.sha256(cnt.astype(np.int64).tobytes()).hexdigest() == ref["sha256_row_count_i64"]
+    assert hashlib.sha256(h.tobytes()).hexdigest() == ref["sha256_row_col_hash_u64"]
+    row_ptr = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+    assert hashlib.sha256(row_ptr.tobytes()).hexdigest() == ref["sha256_row_ptr_i64"]
+
+
+def test_digest_oracle_against_full_product(orc):
+    """row_col_digest and row_sums (the checks of out-of-core products) agree
+    with the full oracle product they summarise."""
+    B = gen.rmat(12, 6, seed=2)
+    A = gen.uniform_rows(3000, 9, seed=4, n_cols=B.n_rows)
+    Cp, Ci, Cv = orc.spgemm(A, B)
+    rows = np.repeat(np.arange(A.n_rows), np.diff(Cp))
+    cnt, h = orc.row_col_digest(A, B)
+    hh = np.zeros(A.n_rows, np.uint64)
+    np.add.at(hh, rows, orc.mix64(Ci))
+    assert np.array_equal(cnt, np.diff(Cp)) and np.array_equal(h, hh)
+    for weighted in (False, True):
+        s, sa = orc.row_sums(A, B, weighted=weighted)
+        w = orc.col_weights(Ci) if weighted else 1.0
+        ref = np.zeros(A.n_rows)
+        np.add.at(ref, rows, Cv * w)
+        assert np.all(np.abs(s - ref) <= 1e-13 * sa + 1e-300)
+    assert orc.lib().orc_col_weight(77) == orc.col_weights(np.array([77]))[0]
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref",
+                                                    "libdbdref.so")), reason="reference CPU code not built")
+def test_reference_block_stream_matches_oracle(orc):
+    """ref_cpu_blocks (the reference's compute_CPU, block by block) gives the
+    oracle's per-row counts and column hashes on a quirk-inert R-MAT."""
+    A = gen.rmat(12, 8, seed=3, int_values=True)
+    cnt, h = orc.row_col_digest(A)
+    got_c = np.zeros(A.n_rows, np.int64)
+    got_h = np.zeros(A.n_rows, np.uint64)
+    dups = []
+
+    def on_block(r0, r1, c, hh, idx, d):
+        got_c[r0:r1] = c
+        got_h[r0:r1] = hh
+        dups.append(d)
+        assert idx.size == int(c.sum())
+    orc.ref_cpu_blocks(A, rows_per_block=512, on_block=on_block)
+    assert np.array_equal(got_c, cnt) and np.array_equal(got_h, h) and sum(dups) == 0
