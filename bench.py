@@ -1,13 +1,16 @@
 #!/usr/bin/env python3
 """SpGEMM GFLOPS (2 x intermediate products / s) of C = A*A on one GB300.
 
-Workload (default): A = R-MAT scale 18, edge factor 8, (a,b,c,d) =
-(.57,.19,.19,.05), seed 0 (n = 262,144, nnz = 2,016,992, P = 867,505,158
-products), FP64 values 1 - U[0,1), row blocks of 4096.  One step = one full
-multiply in the kernel scope (work estimate + segmentation + categorisation +
-symbolic + numeric, device-synchronised, C left in HBM), inputs resident in
-HBM, L2 flushed between steps by a 512 MiB device write outside the timed
-events.
+Workload (default, --workload rmat21): out-of-core A*A, A = R-MAT scale 21,
+edge factor 16, (a,b,c,d) = (.57,.19,.19,.05), seed 0 (n = 2,097,152, nnz =
+32,418,437, P = 55,478,194,409 products, nnz(C) = 26,485,937,763: 318 GB),
+FP64 values 1 - U[0,1), row blocks of 512, GPU budget 24 GiB, host budget
+64 GiB.  One step = one full multiply in the kernel scope (work estimate +
+segmentation + categorisation + symbolic + every chunk's numeric kernels, C
+streamed through the device slot), A resident in HBM, L2 flushed between
+steps by a 512 MiB device write outside the timed events.  --workload rmat18
+runs the in-core R-MAT scale 18 workload (n = 262,144, edge factor 8, blocks
+of 4096; C resident), laplacian256, batched512 and adjoint100k the others.
 
 Also reported: e2e = the same multiply through the C ABI (dbd_spgemm) with
 host buffers, H2D of A and D2H of the whole C inside the timed region (the
@@ -49,6 +52,8 @@ def make_workload(name):
     from dbd_gb300 import generators as gen
     if name == "rmat18":
         return gen.rmat(18, 8, seed=0)
+    if name == "rmat21":
+        return gen.rmat(21, 16, seed=0)
     if name == "laplacian256":
         return gen.laplacian_2d(256)
     if name.startswith("rmat"):
@@ -266,10 +271,11 @@ def profiled_traffic():
     return out
 
 
-def cpu_reference_port(A, threads, repeats=1):
+def cpu_reference_port(A, threads, repeats=1, rpb=4096, blocks=None):
     """The reference's CPU worker (compute_CPU, FP32) restated in oracle/,
-    block by block of 4096 rows like the reference, one reused slot buffer of
-    the largest block (h_IdxC / h_ValC)."""
+    block by block of rpb rows like the reference, one reused slot buffer of
+    the largest block (h_IdxC / h_ValC).  blocks: the row blocks to run (all
+    when None).  Returns (products of those blocks, best time)."""
     import ctypes as C
     import oracle
     L = oracle.lib()
@@ -278,23 +284,36 @@ def cpu_reference_port(A, threads, repeats=1):
     Av = np.ascontiguousarray(A.val, np.float32)
     rowP = row_products(A)
     off = np.concatenate([[0], np.cumsum(rowP)]).astype(np.int64)
-    rpb = 4096
     nb = (A.n_rows + rpb - 1) // rpb
     edges = [min(b * rpb, A.n_rows) for b in range(nb + 1)]
-    maxblk = max(int(off[edges[b + 1]] - off[edges[b]]) for b in range(nb))
+    blocks = list(range(nb)) if blocks is None else [int(b) for b in blocks]
+    maxblk = max(int(off[edges[b + 1]] - off[edges[b]]) for b in blocks)
     cnt = np.zeros(A.n_rows, np.int32)
     idx = np.zeros(max(maxblk, 1), np.int32)
     val = np.zeros(max(maxblk, 1), np.float32)
     best = None
     for _ in range(repeats):
         t0 = time.perf_counter()
-        for b in range(nb):
+        for b in blocks:
             L.orc_ref_cpu_rows(edges[b], edges[b + 1], A.n_cols, Ap.ctypes.data, Ai.ctypes.data, Av.ctypes.data,
                                Ap.ctypes.data, Ai.ctypes.data, Av.ctypes.data, off.ctypes.data, cnt.ctypes.data,
                                idx.ctypes.data, val.ctypes.data, C.c_int(threads))
         dt = time.perf_counter() - t0
         best = dt if best is None else min(best, dt)
-    return int(off[-1]), best
+    P = int(sum(int(off[edges[b + 1]] - off[edges[b]]) for b in blocks))
+    return P, best
+
+
+def cpu_sample(name, A):
+    """Row blocks the CPU legs run for a workload, and their description.
+    R-MAT 2^21: a seeded eighth of its 4096 blocks of 512 rows (~7e9
+    products, a few seconds per pass on 16 cores); otherwise every block."""
+    if name == "rmat21":
+        nb = (A.n_rows + 511) // 512
+        blocks = np.sort(np.random.default_rng(0).choice(nb, nb // 8, replace=False))
+        return 512, blocks, (f"{nb // 8} of the {nb} row blocks of 512 rows (seeded choice, numpy PCG64 seed 0), "
+                             "one pass per step")
+    return 4096, None, "the whole workload, row blocks of 4096, one pass per step"
 
 
 def run_reference_arm(args, rank, world):
@@ -303,16 +322,17 @@ def run_reference_arm(args, rank, world):
     desc, _ = WORKLOADS.get(args.workload, (args.workload, 4096))
     A = make_workload(args.workload)
     threads = os.cpu_count() or 1
-    P, _ = cpu_reference_port(A, threads, 1)
+    rpb, blocks, what = cpu_sample(args.workload, A)
+    P, _ = cpu_reference_port(A, threads, 1, rpb, blocks)
     for _ in range(args.warmup):
-        cpu_reference_port(A, threads, 1)
+        cpu_reference_port(A, threads, 1, rpb, blocks)
     times = []
     for _ in range(args.steps):
-        _, dt = cpu_reference_port(A, threads, 1)
+        _, dt = cpu_reference_port(A, threads, 1, rpb, blocks)
         times.append(dt)
     t = float(np.mean(times))
     v = 2.0 * P / t / 1e9
-    sample = f"the whole workload ({P} products), row blocks of 4096, one step = one full pass"
+    sample = f"{what} ({P} products)"
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GFLOPS", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -625,20 +645,86 @@ def run_adjoint(args, local):
     return 0
 
 
-def run_outofcore(args, local):
+def link_peak(torch, dev, gib=4):
+    """Measured host-link bandwidth (GB/s): cudaMemcpyAsync of a pinned 4 GiB
+    buffer, device-to-host and host-to-device, best of 5 by CUDA events."""
+    n = gib << 30
+    h = torch.empty(n, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(n, dtype=torch.uint8, device=dev)
+    d.fill_(1)
+    out = {}
+    for name, fn in (("d2h", lambda: h.copy_(d, non_blocking=True)), ("h2d", lambda: d.copy_(h, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 1e3
+            best = t if best is None else min(best, t)
+        out[name] = round(n / best / 1e9, 2)
+    del h, d
+    return out
+
+
+def disk_peak(directory, gib=4):
+    """Measured sequential write bandwidth of the output disk (GB/s): 64 MiB
+    aligned O_DIRECT writes of `gib` GiB, then fsync, timed together (the
+    page cache bypassed, as the +I/O writer does)."""
+    import mmap
+    path = os.path.join(directory, ".dbd_disk_probe")
+    buf = mmap.mmap(-1, 64 << 20)
+    buf.write(b"\x5a" * (64 << 20))
+    flags = os.O_CREAT | os.O_TRUNC | os.O_WRONLY | getattr(os, "O_DIRECT", 0)
+    try:
+        fd = os.open(path, flags, 0o644)
+    except OSError:
+        fd = os.open(path, os.O_CREAT | os.O_TRUNC | os.O_WRONLY, 0o644)
+    try:
+        t0 = time.perf_counter()
+        for i in range(gib * 16):
+            os.pwrite(fd, buf, i * (64 << 20))
+        os.fsync(fd)
+        t = time.perf_counter() - t0
+    finally:
+        os.close(fd)
+        os.unlink(path)
+    return round(gib * 2**30 / t / 1e9, 3)
+
+
+def run_outofcore(args, local, rank=0, world=1):
     """Out-of-core A*A, A = R-MAT scale 21, edge factor 16, blocks of 512 rows,
-    GPU budget 24 GiB and host budget 64 GiB: C (billions of entries) streams
-    through the device output ring (kernel scope), pinned D2H (+D2H scope)
-    and the writer thread (+I/O scope, files wrapping when the disk is
-    smaller than C)."""
+    GPU budget 24 GiB and host budget 64 GiB: C (2.65e10 entries, 318 GB)
+    streams through the device slot (kernel scope), pinned D2H through the
+    host ring (+D2H scope) and the O_DIRECT writer (+I/O scope, a file set
+    that wraps at a fraction of the free disk, which is smaller than C).
+
+    value: kernel scope, CUDA events on the library's stream around each
+    dbd_spgemm call (operand checks, work estimate, symbolic, every chunk's
+    numeric kernels), inputs resident in HBM (400 MB, above L2), L2 flushed
+    between steps.  e2e: +D2H with A in host memory.  roofline: the dominant
+    kernel family by a second context that times every family (bins
+    serialised), plus the +D2H rate against the measured host link and the
+    +I/O rate against the measured disk write rate.
+
+    With N ranks (torchrun), every rank multiplies its own replica; the
+    kernel-scope time is the maximum over ranks and value counts the N
+    products.  The copying scopes and the CPU baseline run on rank 0."""
     import torch
     import dbd_gb300 as dbd
-    from dbd_gb300 import generators as gen
+    from dbd_gb300 import replicas
     from dbd_gb300.csr import CSR
     dev = torch.device("cuda", local)
     torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
     t0 = time.perf_counter()
-    A = gen.rmat(21, 16, seed=0)
+    A = make_workload("rmat21")
     t_gen = time.perf_counter() - t0
     rowP = row_products(A)
     P = int(rowP.sum())
@@ -647,56 +733,134 @@ def run_outofcore(args, local):
     free = shutil.disk_usage(ROOT).free
     rotate = max(1.0, min(16.0, free / 4 / 2**30))
     ctx = dbd.Context(cpu_gib=64, gpu_gib=24, rows_per_block=512, device=local, io_rotate_gib=rotate)
-    out = {}
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    for _ in range(args.warmup):
+        ctx.spgemm(D, scope="kernel", fetch=False)
+        flush.zero_()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
     with Clocks(local) as clk:
-        for _ in range(args.warmup):
-            ctx.spgemm(D, scope="kernel", fetch=False)
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            stats.append(ctx.spgemm(D, scope="kernel", fetch=False).stats)
+            evs[i][1].record(stream)
             flush.zero_()
-        ts = []
-        for _ in range(args.steps):
-            torch.cuda.synchronize()
-            a = time.perf_counter()
-            r = ctx.spgemm(D, scope="kernel", fetch=False)
-            torch.cuda.synchronize()
-            ts.append(time.perf_counter() - a)
-            flush.zero_()
-        out["kernel"] = (float(np.mean(ts)), r.stats)
-        ctx.spgemm(A, scope="d2h", fetch=False)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_kernel = replicas.max_over_ranks(float(np.mean([a.elapsed_time(b) for a, b in evs])) / 1e3, dist, dev)
+    if rank != 0:
+        ctx.close()
+        dist.destroy_process_group()
+        return 0
+    st = stats[-1]
+    nnzC = int(st["nnz_c"])
+    launches = int(sum(x["gpu_launches"] for x in stats))
+    Cp = np.empty(A.n_rows + 1, np.int64)
+    dbd._check(ctx._lib.dbd_result_copy(ctx.handle, Cp.ctypes.data, None, None), ctx.handle)
+    nnz_r = np.diff(Cp)
+
+    # Per-kernel times: one more multiply on a context that times every
+    # kernel family with the bins one after another.
+    pctx = dbd.Context(cpu_gib=64, gpu_gib=24, rows_per_block=512, device=local, time_kernels=True)
+    pctx.set_stream(stream.cuda_stream)
+    pctx.spgemm(D, scope="kernel", fetch=False)
+    flush.zero_()
+    ps = pctx.spgemm(D, scope="kernel", fetch=False).stats
+    torch.cuda.synchronize()
+    pctx.close()
+    sym, num = bins(A, rowP, nnz_r, span_words(A), ctx.tuning)
+    bins_match = bool(np.array_equal(np.bincount(num, minlength=12)[:12], np.array(st["rows_per_bin"])))
+    kb = kernel_bytes(A, rowP, nnz_r, sym, num)
+    ktime = {("num", b): ps["t_num_bin_ms"][b] for b in NUM_NAMES}
+    ktime.update({("sym", b): ps["t_sym_bin_ms"][b] for b in SYM_NAMES})
+    roof = roofline(ktime, kb, fp64_flops(rowP, num), torch, dev)
+    roof["traffic"] = profiled_traffic().get(("rmat21", roof["kernel"]))
+    roof["bins_match_library"] = bins_match
+    peak = roof["hbm"]["peak"]
+    c_bytes = 12 * nnzC + 8 * (A.n_rows + 1)
+    bytes_alg = 12 * P + 12 * A.nnz + 4 * (A.n_rows + 1) + c_bytes
+    roof["pipeline"] = {"bytes_alg": bytes_alg, "achieved": round(bytes_alg / t_kernel / 1e9, 2),
+                        "frac": round(bytes_alg / t_kernel / 1e9 / peak, 4),
+                        "fp64_frac": round(2 * P / t_kernel / 1e12 / roof["fp64"]["peak"], 4)}
+
+    # +D2H: host A, C through the pinned ring, each step a full multiply.
+    ctx.set_stream(None)
+    td = []
+    for i in range(max(1, args.e2e_steps) + 1):
         a = time.perf_counter()
         r = ctx.spgemm(A, scope="d2h", fetch=False)
-        out["d2h"] = (time.perf_counter() - a, r.stats)
+        if i:
+            td.append(time.perf_counter() - a)
+    t_d2h = float(np.mean(td))
+    d2h_stats = r.stats
+    link = link_peak(torch, dev)
+    # +I/O: one run through the O_DIRECT writer into a wrapping file set.
     tmp = tempfile.mkdtemp(prefix="dbd_io_", dir=ROOT)
     try:
+        disk = disk_peak(tmp)
         a = time.perf_counter()
         r = ctx.spgemm(A, scope="io", out_dir=tmp, fetch=False)
-        out["io"] = (time.perf_counter() - a, r.stats)
+        t_io = time.perf_counter() - a
+        io_stats = r.stats
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     ctx.close()
-    st = out["kernel"][1]
-    nnzC = int(st["nnz_c"])
+    d2h_gbs = c_bytes / t_d2h / 1e9
+    io_gbs = io_stats["bytes_written"] / t_io / 1e9
+    roof["d2h_frac"] = round(d2h_gbs / link["d2h"], 4)
+    roof["io_frac"] = round(io_gbs / disk, 4)
+    roof["d2h"] = {"achieved": round(d2h_gbs, 2), "peak": link["d2h"], "unit": "GB/s",
+                   "frac": roof["d2h_frac"], "bytes": c_bytes,
+                   "peak_kind": "measured in this run: pinned 4 GiB cudaMemcpyAsync D2H, best of 5",
+                   "what": "C's bytes over the +D2H scope's whole time (compute overlapped)"}
+    roof["io"] = {"achieved": round(io_gbs, 3), "peak": disk, "unit": "GB/s", "frac": roof["io_frac"],
+                  "bytes": int(io_stats["bytes_written"]), "direct": bool(io_stats["io_direct"]),
+                  "peak_kind": "measured in this run: 4 GiB of 64 MiB O_DIRECT writes + fsync to the output disk",
+                  "what": "bytes written over the +I/O scope's whole time"}
+
     g = lambda x: round(2.0 * P / x / 1e9, 4)
-    line = {"metric": METRIC, "value": g(out["kernel"][0]), "unit": "GFLOPS", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(out["kernel"][0] * 1e3, 3), "higher_is_better": True,
+    line = {"metric": METRIC, "value": round(replicas.job_rate(2.0 * P, t_kernel, world) / 1e9, 4),
+            "unit": "GFLOPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t_kernel * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded R-MAT, numpy PCG64)",
             "config": {"workload": WORKLOADS["rmat21"][0], "n": A.n_rows, "nnz": A.nnz, "products": P,
-                       "nnz_c": nnzC, "c_bytes": 12 * nnzC + 8 * (A.n_rows + 1), "gpu_gib": 24, "host_gib": 64,
-                       "rows_per_block": 512, "n_chunks": int(st["n_chunks"]), "io_rotate_gib": round(rotate, 2),
+                       "nnz_c": nnzC, "c_bytes": c_bytes, "gpu_gib": 24, "host_gib": 64,
+                       "rows_per_block": 512, "n_chunks": int(st["n_chunks"]),
+                       "n_chunks_d2h": int(d2h_stats["n_chunks"]), "io_rotate_gib": round(rotate, 2),
                        "generate_s": round(t_gen, 1),
-                       "scope": "kernel: C streamed through the device ring (no D2H), inputs resident in HBM"},
-            "gpu_launches": int(st["gpu_launches"]),
-            "scopes": {"kernel_gflops": g(out["kernel"][0]), "kernel_s": round(out["kernel"][0], 3),
-                       "d2h_gflops": g(out["d2h"][0]), "d2h_s": round(out["d2h"][0], 3),
-                       "d2h_bytes": int(out["d2h"][1]["bytes_d2h"]),
-                       "io_gflops": g(out["io"][0]), "io_s": round(out["io"][0], 3),
-                       "io_bytes": int(out["io"][1]["bytes_written"]),
-                       "io_fsync_s": round(out["io"][1]["t_fsync"], 3)},
-            "e2e": {"value": g(out["d2h"][0]), "unit": "GFLOPS", "h2d_bytes_per_step": 12 * A.nnz + 4 * (A.n_rows + 1),
-                    "d2h_bytes_per_step": int(out["d2h"][1]["bytes_d2h"]),
-                    "scope": "+D2H through dbd_spgemm with host A; C through the 64 GiB pinned host ring"},
+                       "scope": "kernel: operand checks + work estimate + symbolic + every chunk's numeric kernels, "
+                                "C streamed through the device slot (no D2H), A resident in HBM",
+                       "l2": "inputs larger than L2 (A: 400 MB) and a 512 MiB device write between steps",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "scopes": {"kernel_gflops": g(t_kernel), "kernel_s": round(t_kernel, 4),
+                       "d2h_gflops": g(t_d2h), "d2h_s": round(t_d2h, 3), "d2h_bytes": int(d2h_stats["bytes_d2h"]),
+                       "io_gflops": g(t_io), "io_s": round(t_io, 3), "io_bytes": int(io_stats["bytes_written"]),
+                       "io_fsync_s": round(io_stats["t_fsync"], 3), "io_direct": bool(io_stats["io_direct"]),
+                       "link_gbs": link, "disk_write_gbs": disk},
+            "e2e": {"value": g(t_d2h), "unit": "GFLOPS", "h2d_bytes_per_step": 12 * A.nnz + 4 * (A.n_rows + 1),
+                    "d2h_bytes_per_step": int(d2h_stats["bytes_d2h"]), "ms_per_step": round(t_d2h * 1e3, 2),
+                    "scope": "+D2H through dbd_spgemm with host (pageable) A; all of C through the pinned host ring"},
             "clocks": clk.summary()}
+    if world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rpb, blocks, what = cpu_sample("rmat21", A)
+        Pc, tc = cpu_reference_port(A, threads, 1, rpb, blocks)
+        line["cpu_baseline"] = {"value": round(2.0 * Pc / tc / 1e9, 4), "unit": "GFLOPS", "cores": threads,
+                                "kind": "port", "sample": f"{what} ({Pc} products); FP32 restatement of the "
+                                                          "reference's compute_CPU"}
     print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
     return 0
 
 
@@ -706,7 +870,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="dbd", choices=["dbd", "reference"])
-    ap.add_argument("--workload", default="rmat18")
+    ap.add_argument("--workload", default="rmat21")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-io", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -726,9 +890,7 @@ def main():
             return 0
         return run_batched(args, local)
     if args.workload == "rmat21":
-        if rank != 0:
-            return 0
-        return run_outofcore(args, local)
+        return run_outofcore(args, local, rank, world)
     if args.workload == "adjoint100k":
         if rank != 0:
             return 0
@@ -886,11 +1048,11 @@ def main():
         line["scopes"] = scopes
         if world == 1 and not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
-            Pc, tc = cpu_reference_port(A, threads, 1)
+            rpb_c, blocks_c, what = cpu_sample(args.workload, A)
+            Pc, tc = cpu_reference_port(A, threads, 1, rpb_c, blocks_c)
             line["cpu_baseline"] = {"value": round(2.0 * Pc / tc / 1e9, 4), "unit": "GFLOPS", "cores": threads,
-                                    "kind": "port",
-                                    "sample": "the whole workload, FP32 restatement of the reference's "
-                                              "compute_CPU, row blocks of 4096, one pass"}
+                                    "kind": "port", "sample": f"{what}; FP32 restatement of the reference's "
+                                                              "compute_CPU"}
     ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
