@@ -733,6 +733,8 @@ def run_outofcore(args, local, rank=0, world=1):
     free = shutil.disk_usage(ROOT).free
     rotate = max(1.0, min(16.0, free / 4 / 2**30))
     ctx = dbd.Context(cpu_gib=64, gpu_gib=24, rows_per_block=512, device=local, io_rotate_gib=rotate)
+    if args.tune:
+        ctx.set_tuning(**{k: int(v) for k, v in (kv.split("=") for kv in args.tune.split(","))})
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
@@ -770,6 +772,7 @@ def run_outofcore(args, local, rank=0, world=1):
     # Per-kernel times: one more multiply on a context that times every
     # kernel family with the bins one after another.
     pctx = dbd.Context(cpu_gib=64, gpu_gib=24, rows_per_block=512, device=local, time_kernels=True)
+    pctx.set_tuning(**ctx.tuning)
     pctx.set_stream(stream.cuda_stream)
     pctx.spgemm(D, scope="kernel", fetch=False)
     flush.zero_()
@@ -792,6 +795,7 @@ def run_outofcore(args, local, rank=0, world=1):
                         "fp64_frac": round(2 * P / t_kernel / 1e12 / roof["fp64"]["peak"], 4)}
 
     # +D2H: host A, C through the pinned ring, each step a full multiply.
+    ctx_tuning = ctx.tuning
     ctx.set_stream(None)
     td = []
     for i in range(max(1, args.e2e_steps) + 1):
@@ -839,7 +843,7 @@ def run_outofcore(args, local, rank=0, world=1):
                        "scope": "kernel: operand checks + work estimate + symbolic + every chunk's numeric kernels, "
                                 "C streamed through the device slot (no D2H), A resident in HBM",
                        "l2": "inputs larger than L2 (A: 400 MB) and a 512 MiB device write between steps",
-                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU", "tuning": ctx_tuning},
             "gpu_launches": launches,
             "roofline": roof,
             "scopes": {"kernel_gflops": g(t_kernel), "kernel_s": round(t_kernel, 4),

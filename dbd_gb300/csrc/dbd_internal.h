@@ -68,7 +68,8 @@ struct Tuning {
     int32_t denseWarpWords = kDenseWarpWords; // numeric rows on one warp's dense window
     int32_t midSpanWords = 0;                 // numeric rows on one warp's rank window (off: the
                                               // bucket-sorted warp hash measures faster)
-    int32_t denseMethod = 0;                  // dense bin: 0 rank windows, 1 global slots, 2 FP64 windows
+    int32_t denseMethod = 0;                  // dense bin: 0 rank windows, 1 global slots, 2 FP64 windows,
+                                              // 3 one pass into FP64 scratch rows
 };
 
 __host__ __device__ __forceinline__ uint8_t sym_bin_of(int64_t P, int32_t nA, int sw, const Tuning &t) {
@@ -105,7 +106,7 @@ inline Tuning clamp_tuning(Tuning t) {
     t.symHashSpanWords = cl(t.symHashSpanWords, 0, 1 << 26);
     t.denseWarpWords = cl(t.denseWarpWords, 0, kDenseWarpWords);
     t.midSpanWords = cl(t.midSpanWords, 0, kMidSpanWords);
-    t.denseMethod = cl(t.denseMethod, 0, 2);
+    t.denseMethod = cl(t.denseMethod, 0, 3);
     return t;
 }
 
@@ -121,7 +122,8 @@ enum DevErr : int { DEV_OK = 0, DEV_TABLE_FULL = 1, DEV_COUNT_MISMATCH = 2, DEV_
 
 // Counter slots for dynamically scheduled kernels (zeroed per multiply).
 enum CounterSlot : int {
-    CTR_SYM_TINY = 0, CTR_SYM_HWARP, CTR_SYM_HCTA, CTR_SYM_WIDE, CTR_NUM_GDENSE, CTR_NUM_RANKWIN, CTR_COUNT = 16
+    CTR_SYM_TINY = 0, CTR_SYM_HWARP, CTR_SYM_HCTA, CTR_SYM_WIDE, CTR_NUM_GDENSE, CTR_NUM_RANKWIN, CTR_NUM_DSCR,
+    CTR_COUNT = 16
 };
 
 struct Binning {
@@ -206,6 +208,11 @@ struct NumArgs {
     int64_t gStride = 0;   // multiple of 1024
     int gSlots = 0;
     uint32_t *ctr = nullptr;  // row counters of the persistent dense-row kernels (zeroed per launch)
+    // FP64 scratch rows of the one-pass dense kernel (dense_method 3): one of
+    // scrStride doubles per CTA (scrSlots of them), zero between rows.
+    double *scr = nullptr;
+    int64_t scrStride = 0;
+    int scrSlots = 0;
 };
 // Bytes of one global dense slot of `stride` columns.
 inline size_t gdense_slot_bytes(int64_t stride) { return (size_t)stride / 4; }

@@ -139,6 +139,9 @@ struct dbd_ctx {
     DevBuf gdense;           // global dense slots of the dense bin
     int gSlots = 0;
     int64_t gStride = 0;
+    DevBuf dscr;             // FP64 scratch rows of the one-pass dense kernel
+    int scrSlots = 0;
+    int64_t scrStride = 0;
     DevBuf wideBits, wideSlot;  // column bitmaps of wide rows kept for the numeric pass
     bool wideKept = false;      // the symbolic pass of this multiply kept them
     DevBuf rowLo, rowHi;        // column window of every row of C
@@ -599,6 +602,11 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
         na.gSlots = c->gSlots;
         (void)slot;
     }
+    if (c->scrSlots > 0) {
+        na.scr = c->dscr.as<double>();
+        na.scrStride = c->scrStride;
+        na.scrSlots = c->scrSlots;
+    }
     if (c->wideKept) {
         na.wideBits = c->wideBits.as<uint32_t>();
         na.wideSlot = c->wideSlot.as<int32_t>();
@@ -772,6 +780,20 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
             c->gStride = stride;
         }
     }
+    // FP64 scratch rows of the one-pass dense kernel: one per SM, as wide as
+    // a window (2^20 columns) or C, within an eighth of the GPU budget;
+    // zeroed here, and the kernel leaves them zero behind every row.
+    c->scrSlots = 0;
+    if (c->tune.denseMethod == 3 && c->numStart_h[NB_DENSE + 1] > c->numStart_h[NB_DENSE]) {
+        const int64_t stride = std::min<int64_t>((int64_t)1 << 20, (c->ncols + 31) / 32 * 32);
+        const size_t bytes = sizeof(double) * (size_t)stride * (size_t)c->num_sms;
+        if ((double)bytes <= c->cfg.gpu_gib * kGiB / 8) {
+            CK(c, c->dscr.ensure(bytes));
+            CK(c, cudaMemsetAsync(c->dscr.p, 0, bytes, c->stream));
+            c->scrSlots = c->num_sms;
+            c->scrStride = stride;
+        }
+    }
     const int64_t m = c->m, nnz = c->nnzC;
     const double gpu_budget = c->cfg.gpu_gib * kGiB;
     const double host_budget = c->cfg.host_gib * kGiB;
@@ -782,7 +804,8 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
                                  c->B.val.cap + c->rowP.cap + c->symBin.cap + c->numBin.cap + c->rowNnz.cap +
                                  c->symList.cap + c->numList.cap + c->hist.cap + c->symTileOff.cap +
                                  c->numTileOff.cap + c->part.cap + c->Cp.cap + c->cursor.cap +
-                                 (c->gSlots ? c->gdense.cap : 0) + c->wideBits.cap);
+                                 (c->gSlots ? c->gdense.cap : 0) + (c->scrSlots ? c->dscr.cap : 0) +
+                                 c->wideBits.cap);
     const double dev_avail = std::min(gpu_budget - used, (double)free_b - 512.0 * 1024 * 1024);
     const double out_bytes = 12.0 * (double)nnz;
     const bool resident = out_bytes <= std::max(0.0, dev_avail) && scope == DBD_SCOPE_KERNEL;
@@ -1199,7 +1222,7 @@ void dbd_destroy(dbd_ctx *c) {
                       &c->err, &c->blockP, &c->flags, &c->Ci, &c->Cv, &c->wideBits, &c->wideSlot, &c->adjG,
                       &c->adjA, &c->adjB, &c->rowLo, &c->rowHi, &c->A.bmin, &c->A.bmax, &c->B.bmin, &c->B.bmax,
                       &c->ctrs, &c->gdense, &c->dgCount, &c->dgCol, &c->dgVal, &c->dgSum, &c->dgWsum,
-                      &c->dgBad, &c->hashOut})
+                      &c->dgBad, &c->hashOut, &c->dscr})
         b->release();
     c->hCp.release();
     c->hCi.release();
@@ -1680,7 +1703,7 @@ int dbd_autotune(dbd_ctx *c, int repeats, dbd_tuning *best, double *best_ms) {
         {&Tuning::symHashSpanWords, {512, 2048, 8192}},
         {&Tuning::denseWarpWords, {0, 4, 8, 16}},
         {&Tuning::midSpanWords, {0, 256, 1024, 2048}},
-        {&Tuning::denseMethod, {0, 1, 2}},
+        {&Tuning::denseMethod, {0, 1, 2, 3}},
     };
     const Tuning start = c->tune;
     Tuning cur = start;

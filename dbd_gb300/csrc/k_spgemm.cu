@@ -1793,6 +1793,114 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
     }
 }
 
+// Dense rows in one product pass: persistent CTAs (one per SM) take rows
+// from a counter; per window of WIN words of the row's span (2^20 columns)
+// one pass over the row's products sets each product's column bit in a
+// shared bitmap and adds the product into the CTA's FP64 scratch row in
+// global memory, indexed by column (an L2 reduction whose result is not
+// read back).  Then each warp compacts its 1024 words of the window, word
+// by word in column order: the 32 lanes are the word's 32 columns, so C's
+// columns and values go out as contiguous runs (coalesced), the values read
+// from the scratch row at the same 32 consecutive columns, which the warp
+// zeroes behind it, leaving the scratch row and the bitmap zero for the next
+// window.  Compared with the rank method this enumerates every product once
+// instead of twice and writes C once, coalesced, instead of zeroing it and
+// reducing into it in place.
+template <int THREADS, int WIN>
+__global__ void __launch_bounds__(THREADS) k_num_dscr(NumArgs a, int32_t lo, int32_t count) {
+    static_assert(WIN == 32 * THREADS, "one 32-word group per thread");
+    extern __shared__ __align__(16) unsigned char smem[];
+    using L = StageLayout<THREADS>;
+    constexpr int NW = THREADS / 32;
+    __shared__ int32_t sh[NW];
+    __shared__ int32_t next;
+    int32_t *pre = reinterpret_cast<int32_t *>(smem + L::pre);
+    int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
+    double *av = reinterpret_cast<double *>(smem + L::av);
+    uint32_t *bits = reinterpret_cast<uint32_t *>(smem + L::bytes);
+    double *scr = a.scr + (size_t)blockIdx.x * (size_t)a.scrStride;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (int i = tid; i < WIN; i += THREADS) bits[i] = 0u;
+    for (;;) {
+        if (tid == 0) next = (int32_t)atomicAdd(&a.ctr[CTR_NUM_DSCR], 1u);
+        __syncthreads();
+        if (next >= count) break;
+        const int32_t item = next;
+        const int32_t row = a.list[lo + item];
+        const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
+        const int64_t expect = a.Cp[row + 1] - a.Cp[row];
+        const int64_t obase = a.Cp[row] - a.outBase;
+        const int32_t shift = col_shift(a, row);
+        const int64_t end = (int64_t)a.rowHi[row] + 1;
+        const int64_t start = (int64_t)(a.rowLo[row] >> 5) << 5;
+        const bool clip = a.bSorted && end - start > (int64_t)WIN * 32;
+        int64_t run = 0;
+        for (int64_t c_lo = start; c_lo < end; c_lo += (int64_t)WIN * 32) {
+            const int nwords = (int)min((int64_t)WIN, (end - c_lo + 31) >> 5);
+            const uint32_t nbits = min((uint32_t)nwords * 32u, (uint32_t)a.scrStride);
+            const int64_t c_hi = c_lo + nbits;
+            // The pass: bits in shared memory, products into the scratch row.
+            for (int32_t eb = e0; eb < e1; eb += THREADS) {
+                int nb;
+                const int32_t total = stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av,
+                                                                   &nb, sh, clip, c_lo, c_hi);
+                int32_t tb, te;
+                warp_share<THREADS>(total, &tb, &te);
+                warp_range_ld<4>(
+                    pre, bst, nb, tb, te,
+                    [&](int32_t pos) { return ColVal{__ldg(&a.B.idx[pos]), __ldg(&a.B.val[pos])}; },
+                    [&](bool v, const ColVal &x, int e) {
+                        const uint32_t rel = v ? (uint32_t)((int64_t)x.c - c_lo) : 0u;
+                        const bool in = v && rel < nbits;
+                        or_bits_runs(bits, in, rel);
+                        if (in) atomicAdd(&scr[rel], __dmul_rn(av[e], x.v));
+                    });
+                __syncthreads();
+            }
+            // Word counts: thread t holds words [32 t, 32 t + 32).
+            uint32_t mask = 0;
+            int32_t cnt = 0;
+#pragma unroll 8
+            for (int k = 0; k < 32; ++k) {
+                const int q = (k + lane) & 31;
+                const uint32_t x = bits[32 * tid + q];
+                if (x) mask |= 1u << q;
+                cnt += __popc(x);
+            }
+            int32_t tot;
+            const int32_t base = block_excl_scan<THREADS>(cnt, &tot, sh);
+            // Compaction: the warp walks its lanes' non-empty words in column
+            // order; lane b takes column 32 w + b of word w.
+            for (int src = 0; src < 32; ++src) {
+                uint32_t m = __shfl_sync(FULL, mask, src);
+                int64_t p = run + __shfl_sync(FULL, base, src);
+                while (m) {
+                    const int w = 32 * (32 * (tid >> 5) + src) + __ffs(m) - 1;
+                    m &= m - 1u;
+                    const uint32_t word = bits[w];
+                    const int64_t q = p + __popc(word & lt);
+                    if ((word >> lane) & 1u) {
+                        double *s = &scr[32 * w + lane];
+                        if (q < expect) {
+                            __stcs(&a.Ci[obase + q], (int32_t)(c_lo + 32 * w + lane - shift));
+                            __stcs(&a.Cv[obase + q], __ldcg(s));
+                        }
+                        __stcg(s, 0.0);
+                    }
+                    p += __popc(word);
+                }
+            }
+            __syncthreads();  // every warp has read its words before they clear
+            for (uint32_t m = mask; m; m &= m - 1u) bits[32 * tid + __ffs(m) - 1] = 0u;
+            __syncthreads();
+            run += tot;
+        }
+        if (tid == 0 && run != expect) raise(a.err, DEV_COUNT_MISMATCH);
+        __syncthreads();  // every thread has read `next` before it changes
+    }
+}
+
 // Dense rows with a global slot: persistent CTAs, one slot each, take rows
 // from a counter; the rank method over the whole row, its bitmap and word
 // ranks in the slot (two bits per column of C, so the slots of all CTAs stay
@@ -2138,6 +2246,7 @@ constexpr int kRankWinWords = 32768;  // 2^20 columns per window
 constexpr size_t kSmemRankWin = StageLayout<kRankWinThreads>::bytes + 6 * (size_t)kRankWinWords +
                                 4 * (size_t)(kRankWinWords / 256);
 constexpr size_t kSmemGdenseBase = StageLayout<kGdenseThreads>::bytes;
+constexpr size_t kSmemDscr = StageLayout<kRankWinThreads>::bytes + 4 * (size_t)kRankWinWords;
 constexpr int kRankmRows = 5;  // 14.6 KiB per warp: three CTAs (15 warps) per SM
 constexpr size_t kSmemRankm =
     (size_t)kRankmRows * (6 * (size_t)kMidSpanWords + 4 * (size_t)(kMidSpanWords / 32) + 8 * (size_t)kNumWarpMax);
@@ -2170,6 +2279,8 @@ void init_kernel_attributes() {
     cudaFuncSetAttribute(k_num_rankm<kRankmRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemRankm);
     cudaFuncSetAttribute(k_num_rankwin<kRankWinThreads, kRankWinWords>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kSmemRankWin);
+    cudaFuncSetAttribute(k_num_dscr<kRankWinThreads, kRankWinWords>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemDscr);
     cudaFuncSetAttribute(k_num_gdense<kGdenseThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(kSmemGdenseBase + 4 * (size_t)kGdenseSumMax));
 }
@@ -2281,6 +2392,10 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
                 const int grid = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1) * per_sm);
                 k_num_rankwin<kRankWinThreads, kRankWinWords>
                     <<<(unsigned)grid, kRankWinThreads, kSmemRankWin, s>>>(a, lo, n);
+            } else if (a.tune.denseMethod == 3 && a.scr) {
+                cudaMemsetAsync(a.ctr + CTR_NUM_DSCR, 0, sizeof(uint32_t), s);
+                const int grid = (int)std::min<int64_t>(n, a.scrSlots);
+                k_num_dscr<kRankWinThreads, kRankWinWords><<<(unsigned)grid, kRankWinThreads, kSmemDscr, s>>>(a, lo, n);
             } else if (a.tune.denseMethod == 1 && a.gBits) {
                 cudaMemsetAsync(a.ctr + CTR_NUM_GDENSE, 0, sizeof(uint32_t), s);
                 const int grid = (int)std::min<int64_t>(n, a.gSlots);

@@ -312,7 +312,8 @@ int dbd_spgemm_batched(dbd_ctx *ctx, int64_t count, const dbd_csr_view *a, const
  *                          rank window instead of a hash table (0..2048)
  *   dense_method           rows of the dense bin: 0 rank windows of 2^20 columns in
  *                          shared memory, 1 rank over the whole row in global slots,
- *                          2 FP64 windows of 8192 columns swept by cursors */
+ *                          2 FP64 windows of 8192 columns swept by cursors, 3 one pass
+ *                          per 2^20-column window into an FP64 scratch row per SM */
 typedef struct {
     int32_t warp_span_words;
     int32_t warp_max_nnz;

@@ -235,20 +235,23 @@ def test_dense_rows_long_and_thin_b_rows(ctx, orc):
     A_long = gen.uniform_rows(48, 60, seed=4, n_cols=k, dist="uniform")
     B_thin = gen.uniform_rows(4000, 5, seed=3, n_cols=n, dist="uniform")
     A_thin = gen.uniform_rows(48, 1000, seed=5, n_cols=4000, dist="uniform")
-    # Every method of the dense bin: rank windows, global slots, FP64 windows.
-    for method in (0, 1, 2):
+    # Every method of the dense bin: rank windows, global slots, FP64 windows,
+    # one pass into scratch rows.
+    for method in (0, 1, 2, 3):
         with dbd.Context(cpu_gib=8, gpu_gib=16) as c:
             c.set_tuning(dense_method=method)
             for A, B in ((A_long, B_long), (A_thin, B_thin)):
                 res = c.spgemm(A, B, scope="kernel")
                 check(res.C, A, B, orc)
                 assert res.stats["rows_per_bin"][8] > 0  # the dense bin
-    # Global slots without room for them (a small budget): FP64 windows.
-    with dbd.Context(cpu_gib=4, gpu_gib=0.5) as small:
-        small.set_tuning(dense_method=1)
-        for A, B in ((A_long, B_long), (A_thin, B_thin)):
-            res = small.spgemm(A, B, scope="kernel")
-            check(res.C, A, B, orc)
+    # Global slots or scratch rows without room for them (a small budget):
+    # FP64 windows.
+    for method in (1, 3):
+        with dbd.Context(cpu_gib=4, gpu_gib=0.5) as small:
+            small.set_tuning(dense_method=method)
+            for A, B in ((A_long, B_long), (A_thin, B_thin)):
+                res = small.spgemm(A, B, scope="kernel")
+                check(res.C, A, B, orc)
 
 
 def test_dense_rows_over_several_windows(ctx, orc):
@@ -275,11 +278,15 @@ def test_dense_rows_over_several_windows(ctx, orc):
     rows, cols = np.concatenate(rows), np.concatenate(cols)
     B = gen._from_coo(3000, n, rows, cols, rng.uniform(-1, 1, rows.size))
     A = gen.uniform_rows(24, 600, seed=9, n_cols=3000, dist="uniform")
-    res = ctx.spgemm(A, B, scope="kernel")
-    check(res.C, A, B, orc)
-    assert res.stats["rows_per_bin"][8] > 0 and res.stats["sym_rows_per_bin"][5] > 0
-    res = ctx.spgemm(A, shuffled_rows(rng, B), scope="kernel")
-    check(res.C, A, B, orc)
+    Bu = shuffled_rows(rng, B)
+    for method in (0, 3):  # rank windows, one pass into scratch rows
+        with dbd.Context(cpu_gib=8, gpu_gib=32) as c:
+            c.set_tuning(dense_method=method)
+            res = c.spgemm(A, B, scope="kernel")
+            check(res.C, A, B, orc)
+            assert res.stats["rows_per_bin"][8] > 0 and res.stats["sym_rows_per_bin"][5] > 0
+            res = c.spgemm(A, Bu, scope="kernel")
+            check(res.C, A, B, orc)
 
 
 def test_dense_rows_unsorted_b(ctx, orc):
@@ -294,9 +301,12 @@ def test_dense_rows_unsorted_b(ctx, orc):
         perm_idx[s:e] = B.col_idx[s:e][p]
         B.val[s:e] = B.val[s:e][p]
     B = CSR(B.n_rows, B.n_cols, B.row_ptr, perm_idx, B.val)
-    res = ctx.spgemm(A, B, scope="kernel")
-    check(res.C, A, B, orc)
-    assert res.stats["rows_per_bin"][8] > 0  # dense windows
+    for method in (0, 3):
+        with dbd.Context(cpu_gib=8, gpu_gib=16) as c:
+            c.set_tuning(dense_method=method)
+            res = c.spgemm(A, B, scope="kernel")
+            check(res.C, A, B, orc)
+            assert res.stats["rows_per_bin"][8] > 0  # dense windows
 
 
 def test_edge_cases(ctx, orc):

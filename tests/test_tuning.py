@@ -18,6 +18,9 @@ EXTREMES = [
     dict(warp_span_words=8, warp_max_nnz=64, sym_warp_max_products=128, rank_words_max=1024,
          rank_shared_max_nnz=512, sym_hash_span_words=512, dense_warp_span_words=4, mid_span_words=100,
          dense_method=0),
+    dict(warp_span_words=32, warp_max_nnz=128, sym_warp_max_products=256, rank_words_max=2048,
+         rank_shared_max_nnz=1024, sym_hash_span_words=2048, dense_warp_span_words=8, mid_span_words=0,
+         dense_method=3),
 ]
 
 
@@ -38,7 +41,7 @@ def test_out_of_range_tuning_refused(ctx):
     before = ctx.tuning
     for k, v in [("warp_span_words", 65), ("warp_max_nnz", 0), ("sym_warp_max_products", 513),
                  ("rank_words_max", 8193), ("rank_shared_max_nnz", 4097), ("sym_hash_span_words", -1),
-                 ("dense_warp_span_words", 17), ("mid_span_words", 2049), ("dense_method", 3)]:
+                 ("dense_warp_span_words", 17), ("mid_span_words", 2049), ("dense_method", 4)]:
         with pytest.raises(dbd.DBDError):
             ctx.set_tuning(**{k: v})
     assert ctx.tuning == before
