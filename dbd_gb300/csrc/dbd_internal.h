@@ -280,5 +280,9 @@ void launch_hash_words(const uint32_t *w, int64_t n, uint64_t salt, uint64_t *ac
 
 // One-time kernel attribute setup (dynamic shared memory limits).
 void init_kernel_attributes();
+// Load the kernels of k_analysis.cu / k_spgemm.cu now instead of at their
+// first launch (cudaFuncGetAttributes on each); the first error is returned.
+cudaError_t preload_analysis_kernels();
+cudaError_t preload_spgemm_kernels();
 
 }  // namespace dbd

@@ -438,4 +438,21 @@ void launch_validate_idx(const int32_t *idx, int64_t nnz, int64_t ncols, int *fl
     k_validate_idx<<<(unsigned)std::min<int64_t>(ceil_div(nnz, 256), 4096), 256, 0, s>>>(idx, nnz, ncols, flag);
 }
 
+// Loads every kernel of this file now (CUDA loads kernels lazily, on first
+// launch, by default).  Returns the first error.
+cudaError_t preload_analysis_kernels() {
+    const void *fns[] = {
+        (const void *)k_row_minmax, (const void *)k_row_products<256>, (const void *)k_block_products,
+        (const void *)k_num_bins, (const void *)k_bin_hist, (const void *)k_bin_scan, (const void *)k_bin_scatter,
+        (const void *)k_scan_reduce, (const void *)k_scan_parts, (const void *)k_scan_final,
+        (const void *)k_f32_to_f64, (const void *)k_validate_ptr, (const void *)k_validate_idx,
+    };
+    for (const void *f : fns) {
+        cudaFuncAttributes fa;
+        const cudaError_t e = cudaFuncGetAttributes(&fa, f);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 }  // namespace dbd

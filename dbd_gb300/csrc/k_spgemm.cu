@@ -2285,6 +2285,41 @@ void init_kernel_attributes() {
                          (int)(kSmemGdenseBase + 4 * (size_t)kGdenseSumMax));
 }
 
+// Loads every symbolic and numeric kernel of this file now.  CUDA loads
+// kernels lazily (on first launch) by default; a caller that must not have
+// the driver allocate during a later call (the allocation-free entry point)
+// has them loaded at its set-up instead.  Returns the first error.
+cudaError_t preload_spgemm_kernels() {
+    const void *fns[] = {
+        (const void *)k_sym_tiny,
+        (const void *)k_sym_flagw<kBitwRows>,
+        (const void *)k_sym_hash_warp<kSymWarpRows, kSymWarpTable>,
+        (const void *)k_sym_hash_cta<kSymCtaThreads, kSymCtaTable>,
+        (const void *)k_sym_wide<kWideThreads>,
+        (const void *)k_sym_wide<kWideThreadsBig>,
+        (const void *)k_num_tiny,
+        (const void *)k_num_hash_warp<kNumWarpRows, kNumWarpTable>,
+        (const void *)k_num_densew<kDensewRows>,
+        (const void *)k_num_rankm<kRankmRows>,
+        (const void *)k_num_rankw<kRankwRows>,
+        (const void *)k_num_rank<kRankSThreads, false>,
+        (const void *)k_num_rank<kRankLThreads, true>,
+        (const void *)k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>,
+        (const void *)k_num_hash_cta<kNumCtaLThreads, kNumCtaLTable>,
+        (const void *)k_num_rankwin<kRankWinThreads, kRankWinWords>,
+        (const void *)k_num_dscr<kRankWinThreads, kRankWinWords>,
+        (const void *)k_num_gdense<kGdenseThreads>,
+        (const void *)k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, true>,
+        (const void *)k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, false>,
+    };
+    for (const void *f : fns) {
+        cudaFuncAttributes fa;
+        const cudaError_t e = cudaFuncGetAttributes(&fa, f);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 // Dynamic shared memory of the rank kernel: staging, bitmap and word ranks of
 // maxWords words, vcap shared values.
 static size_t smem_rank(int threads, int maxWords, int vcap) {

@@ -51,6 +51,14 @@ int device_scratch(int dev, unsigned char **out) {
     std::lock_guard<std::mutex> lk(g_setup_mu);
     if (!g_setup_done[dev]) {
         init_kernel_attributes();
+        // Every kernel the pipeline launches is loaded here, so that no later
+        // call has the driver load a module (and allocate) on first launch.
+        cudaError_t le = preload_analysis_kernels();
+        if (le == cudaSuccess) le = preload_spgemm_kernels();
+        if (le != cudaSuccess) {
+            snprintf(g_msg, sizeof(g_msg), "loading the kernels: %s", cudaGetErrorString(le));
+            return report(DBD_ERR_CUDA);
+        }
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) {

@@ -448,11 +448,13 @@ void dbd_writer_close(dbd_writer *w);
  * Every temporary array lives in one file-scope device array of
  * DBD_NOALLOC_SCRATCH_BYTES (32 MiB), which each GPU that loads the library
  * holds until the process exits.  Inputs whose scratch would exceed it --
- * about 31 bytes per row of A, 8 per row of B and 8 per entry of A, e.g.
- * ~700k rows at 2 entries per row of a square A -- are rejected with
- * DBD_ERR_BUDGET.  The first call on a
- * device sets that device up (its kernel attributes and the array's device
- * address), so make the first call on each device before any stream capture.
+ * about 31 bytes per row of A, 8 per row of B and 8 per entry of A, so a
+ * square A with 2 entries per row fits up to about 610k rows (31 + 8 + 16 =
+ * 55 bytes per row) -- are rejected with DBD_ERR_BUDGET.  The first call on a
+ * device sets that device up (its kernel attributes, the loading of every
+ * kernel the pipeline launches, and the array's device address), so make the
+ * first call on each device before any stream capture and before reserving
+ * the device's memory.
  * All calls share the array: calls that overlap on the GPU (other threads or
  * streams) race and must be serialised by the caller.  On failure the
  * message is printed to stderr. */

@@ -7,7 +7,9 @@ every temporary array in one file-scope device array of fixed size.  This file
 checks, through the C ABI, that two calls in a row (different matrices, so the
 second call starts from the first call's leftovers in that array) give the
 same product as the regular entry point dbd_spgemm, within the tolerance of
-the other parity tests, and that an input too large for the array is refused.
+the other parity tests, that an input too large for the array is refused, and
+that after its first call on the device (the set-up) further calls whose rows
+land in different kernel bins leave the device's free memory unchanged.
 It is collected last so that a failure here stops a -x run only after every
 other test ran; it also passes on its own in a fresh process.
 """
@@ -93,3 +95,34 @@ def test_noalloc_reports_short_capacity_and_size_limit():
     rc = lib.dbd_spgemm_noalloc(C.byref(vb), None, C.c_void_p(cp.data_ptr()), None, None, 0, C.byref(nnz),
                                 None)
     assert rc == -4
+
+
+def test_noalloc_allocates_nothing_after_setup():
+    """After the first call (which sets the device up), calls on inputs that
+    reach different kernels leave cudaMemGetInfo's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    lib = _ffi.load()
+    mats = [gen.laplacian_2d(128), gen.rmat(13, 8, seed=9), wide_rows(n=200_000, heavy=20)]
+    prepared = []
+    for A in mats:
+        va, keep = device_view(torch, A)
+        cap = int(np.diff(A.row_ptr).astype(np.int64)[A.col_idx].sum()) + 16  # products bound nnz(C)
+        out = (torch.empty(A.n_rows + 1, dtype=torch.int64, device="cuda"),
+               torch.empty(cap, dtype=torch.int32, device="cuda"),
+               torch.empty(cap, dtype=torch.float64, device="cuda"))
+        prepared.append((va, keep, out, cap))
+    stream = torch.cuda.current_stream().cuda_stream
+    nnz = C.c_int64(0)
+
+    def call(i):
+        va, _, (cp, ci, cv), cap = prepared[i]
+        rc = lib.dbd_spgemm_noalloc(C.byref(va), None, C.c_void_p(cp.data_ptr()), C.c_void_p(ci.data_ptr()),
+                                    C.c_void_p(cv.data_ptr()), cap, C.byref(nnz), C.c_void_p(stream))
+        torch.cuda.synchronize()
+        return rc
+
+    assert call(0) == 0  # set-up (and the first call)
+    free0 = torch.cuda.mem_get_info()[0]
+    for i in (1, 2, 0, 2):
+        assert call(i) == 0
+    assert torch.cuda.mem_get_info()[0] == free0
