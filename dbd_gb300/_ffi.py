@@ -64,7 +64,8 @@ class Stats(C.Structure):
                 ("sym_rows_per_bin", C.c_int64 * NUM_BINS), ("bytes_d2h", C.c_int64),
                 ("bytes_written", C.c_int64), ("gpu_launches", C.c_int64), ("t_analysis_ms", C.c_double),
                 ("t_sym_bin_ms", C.c_double * NUM_BINS), ("t_scan_ms", C.c_double),
-                ("t_num_bin_ms", C.c_double * NUM_BINS), ("io_direct", C.c_int64), ("resumed_from_row", C.c_int64)]
+                ("t_num_bin_ms", C.c_double * NUM_BINS), ("io_direct", C.c_int64), ("resumed_from_row", C.c_int64),
+                ("heavy_rows", C.c_int64)]
 
     def as_dict(self):
         d = {}

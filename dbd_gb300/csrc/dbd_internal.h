@@ -48,6 +48,17 @@ constexpr int kMidSpanWords = 2048;          // warp rank rows over their own wi
 constexpr int kRankWordsMax = 8192;          // CTA rank rows: span <= 2^18 columns
 constexpr int kWideHashSpanWords = 2048;     // symbolic: P <= kSymCtaMax rows hash above this span
 constexpr int kWideTouchMax = 8192;          // words a wide-row window clears one by one
+// Heavy rows of the dense bin are cut into pieces by column.  The symbolic
+// pass records, for rows with at least kHeavyP products, the entries of C's
+// row in every slab of 2^kSlabShift columns (from the row's first word);
+// the numeric pass cuts dense rows of more than kPieceNnz entries at slab
+// boundaries into pieces of about kPieceNnz entries and at most
+// kPieceSlabs slabs (one 2^20-column window), each an independent work item.
+constexpr int kSlabShift = 16;
+constexpr int kMaxSlabs = 64;                // rows spanning up to 2^22 columns
+constexpr int64_t kHeavyP = 65536;
+constexpr int kPieceNnz = 65536;
+constexpr int kPieceSlabs = 16;
 
 __host__ __device__ __forceinline__ int span_words(int32_t lo, int32_t hi) {
     return hi >= lo ? (hi >> 5) - (lo >> 5) + 1 : 0;
@@ -123,7 +134,7 @@ enum DevErr : int { DEV_OK = 0, DEV_TABLE_FULL = 1, DEV_COUNT_MISMATCH = 2, DEV_
 // Counter slots for dynamically scheduled kernels (zeroed per multiply).
 enum CounterSlot : int {
     CTR_SYM_TINY = 0, CTR_SYM_HWARP, CTR_SYM_HCTA, CTR_SYM_WIDE, CTR_NUM_GDENSE, CTR_NUM_RANKWIN, CTR_NUM_DSCR,
-    CTR_COUNT = 16
+    CTR_HEAVY, CTR_ITEMS, CTR_COUNT = 16
 };
 
 struct Binning {
@@ -170,12 +181,28 @@ struct SymArgs {
     Tuning tune;
     int numSms = 0;  // persistent kernels size their grid by it; ctr holds their zeroed row counters
     int bSorted = 0; // B's rows have strictly ascending columns
+    // Slab counts of heavy rows (null: not recorded): heavySlot[row] = -1 or
+    // the row's slot (taken from ctr[CTR_HEAVY], below heavyCap); slabCnt
+    // holds kMaxSlabs counts per slot.
+    int32_t *heavySlot = nullptr;
+    int32_t *slabCnt = nullptr;
+    int heavyCap = 0;
 };
 // Launches the symbolic kernel of bin `bin` over list[begin, begin + n).
 void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cudaStream_t s, int *launches);
 void launch_f32_to_f64(const float *src, double *dst, int64_t n, cudaStream_t s);
 void launch_validate_ptr(const int32_t *ptr, int64_t m, int64_t nnz, int *flag, cudaStream_t s);
 void launch_validate_idx(const int32_t *idx, int64_t nnz, int64_t ncols, int *flag, cudaStream_t s);
+
+// One work item of the dense bin: row, or the piece of it over the column
+// slabs [s0, s1) whose entries start `off` entries into C's row (s0 < 0:
+// the whole row).
+struct DenseItem {
+    int32_t row;
+    int16_t s0, s1;
+    int32_t cnt;   // entries of the piece
+    int64_t off;
+};
 
 struct NumArgs {
     CsrDev A, B;
@@ -213,7 +240,15 @@ struct NumArgs {
     double *scr = nullptr;
     int64_t scrStride = 0;
     int scrSlots = 0;
+    // Work items of the dense bin (null: one item per row).  Built on the
+    // device per launch from the bin's rows: a heavy row with slab counts
+    // becomes several pieces; the count is ctr[CTR_ITEMS].
+    const int32_t *heavySlot = nullptr;
+    const int32_t *slabCnt = nullptr;
+    DenseItem *items = nullptr;
+    int itemCap = 0;
 };
+
 // Bytes of one global dense slot of `stride` columns.
 inline size_t gdense_slot_bytes(int64_t stride) { return (size_t)stride / 4; }
 constexpr int kGdenseSumMax = 8192;  // summary words in shared memory: C up to 2^23 columns

@@ -139,6 +139,10 @@ struct dbd_ctx {
     DevBuf gdense;           // global dense slots of the dense bin
     int gSlots = 0;
     int64_t gStride = 0;
+    DevBuf heavySlot, slabCnt;  // slab counts of heavy rows (symbolic -> dense-bin pieces)
+    DevBuf items;               // dense-bin work items
+    int heavyCap = 0, itemCap = 0;
+    bool pieces = false;        // the dense bin cuts heavy rows into pieces in this multiply
     DevBuf dscr;             // FP64 scratch rows of the one-pass dense kernel
     int scrSlots = 0;
     int64_t scrStride = 0;
@@ -523,6 +527,20 @@ int symbolic(dbd_ctx *c) {
     sa.rowP = c->rowP.as<int64_t>();
     sa.rowHi = c->rowHi.as<int32_t>();
     sa.tune = c->tune;
+    // Slab counts of heavy rows for the dense bin's pieces (rank windows,
+    // B's rows ascending): at most one slot per kHeavyP products.
+    c->heavyCap = 0;
+    c->pieces = false;
+    if (c->tune.denseMethod == 0 && opB_sorted(c) && c->products >= kHeavyP) {
+        const int64_t cap = std::min<int64_t>({m, c->products / kHeavyP, 262144});
+        CK(c, c->heavySlot.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1)));
+        CK(c, c->slabCnt.ensure(sizeof(int32_t) * (size_t)kMaxSlabs * (size_t)cap));
+        CK(c, cudaMemsetAsync(c->heavySlot.p, 0xff, sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1), c->stream));
+        sa.heavySlot = c->heavySlot.as<int32_t>();
+        sa.slabCnt = c->slabCnt.as<int32_t>();
+        sa.heavyCap = (int)cap;
+        c->heavyCap = (int)cap;
+    }
     // Keep the wide rows' column bitmaps (one slot of kRankWordsMax words per
     // wide row) for the numeric rank kernels when the store stays within an
     // eighth of the GPU budget.
@@ -562,6 +580,10 @@ int symbolic(dbd_ctx *c) {
     CK(c, cudaGetLastError());
     CK(c, cudaMemcpyAsync(&c->nnzC, c->Cp.as<int64_t>() + m, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaMemcpyAsync(c->numStart_h, c->numStart.p, sizeof(c->numStart_h), cudaMemcpyDeviceToHost, c->stream));
+    uint32_t heavy = 0;
+    if (c->heavyCap > 0)
+        CK(c, cudaMemcpyAsync(&heavy, c->ctrs.as<uint32_t>() + CTR_HEAVY, sizeof(heavy), cudaMemcpyDeviceToHost,
+                              c->stream));
     c->numTileOff_h.assign((size_t)kMaxBins * (size_t)(c->ntiles + 1), 0);
     CK(c, cudaMemcpyAsync(c->numTileOff_h.data(), c->numTileOff.p, sizeof(int32_t) * c->numTileOff_h.size(),
                           cudaMemcpyDeviceToHost, c->stream));
@@ -570,6 +592,19 @@ int symbolic(dbd_ctx *c) {
     if (rc) return rc;
     for (int q = 0; q < NB_COUNT; ++q) c->stats.rows_per_bin[q] = c->numStart_h[q + 1] - c->numStart_h[q];
     c->stats.nnz_c = c->nnzC;
+    // Dense-bin work items: one per row plus the extra pieces of heavy rows
+    // (at most kMaxSlabs per recorded row).
+    const int64_t nDense = c->numStart_h[NB_DENSE + 1] - c->numStart_h[NB_DENSE];
+    const int64_t nHeavy = std::min<int64_t>((int64_t)heavy, c->heavyCap);
+    c->stats.heavy_rows = nHeavy;
+    if (c->heavyCap > 0 && nHeavy > 0 && nDense > 0) {
+        const int64_t icap = nDense + nHeavy * (kMaxSlabs - 1);
+        if (icap < INT32_MAX) {
+            CK(c, c->items.ensure(sizeof(DenseItem) * (size_t)icap));
+            c->itemCap = (int)icap;
+            c->pieces = true;
+        }
+    }
     if (c->nnzC > INT64_MAX / 16) return set_err(c, DBD_ERR_OVERFLOW, "nnz(C) too large");
     return DBD_OK;
 }
@@ -601,6 +636,12 @@ void numeric_rows(dbd_ctx *c, int64_t r0, int64_t r1, int64_t outBase, int32_t *
         na.gStride = c->gStride;
         na.gSlots = c->gSlots;
         (void)slot;
+    }
+    if (c->pieces) {
+        na.heavySlot = c->heavySlot.as<int32_t>();
+        na.slabCnt = c->slabCnt.as<int32_t>();
+        na.items = c->items.as<DenseItem>();
+        na.itemCap = c->itemCap;
     }
     if (c->scrSlots > 0) {
         na.scr = c->dscr.as<double>();
@@ -805,7 +846,7 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
                                  c->symList.cap + c->numList.cap + c->hist.cap + c->symTileOff.cap +
                                  c->numTileOff.cap + c->part.cap + c->Cp.cap + c->cursor.cap +
                                  (c->gSlots ? c->gdense.cap : 0) + (c->scrSlots ? c->dscr.cap : 0) +
-                                 c->wideBits.cap);
+                                 c->wideBits.cap + c->heavySlot.cap + c->slabCnt.cap + c->items.cap);
     const double dev_avail = std::min(gpu_budget - used, (double)free_b - 512.0 * 1024 * 1024);
     const double out_bytes = 12.0 * (double)nnz;
     const bool resident = out_bytes <= std::max(0.0, dev_avail) && scope == DBD_SCOPE_KERNEL;
@@ -1222,7 +1263,8 @@ void dbd_destroy(dbd_ctx *c) {
                       &c->err, &c->blockP, &c->flags, &c->Ci, &c->Cv, &c->wideBits, &c->wideSlot, &c->adjG,
                       &c->adjA, &c->adjB, &c->rowLo, &c->rowHi, &c->A.bmin, &c->A.bmax, &c->B.bmin, &c->B.bmax,
                       &c->ctrs, &c->gdense, &c->dgCount, &c->dgCol, &c->dgVal, &c->dgSum, &c->dgWsum,
-                      &c->dgBad, &c->hashOut, &c->dscr})
+                      &c->dgBad, &c->hashOut, &c->dscr, &c->heavySlot, &c->slabCnt,
+                      &c->items})
         b->release();
     c->hCp.release();
     c->hCi.release();

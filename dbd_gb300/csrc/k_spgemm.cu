@@ -559,6 +559,8 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
     __shared__ int32_t sh[THREADS / 32];
     __shared__ int nt;
     __shared__ int32_t next;
+    __shared__ int32_t slot;
+    __shared__ int32_t slabSh[kWideWindowBitsMax >> kSlabShift];
     int32_t *pre = reinterpret_cast<int32_t *>(smem + L::pre);
     int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
     uint32_t *bm = reinterpret_cast<uint32_t *>(smem + L::bytes);
@@ -584,6 +586,19 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
         // sweep over its words.
         const int rowCap = a.rowP[row] <= cap ? cap : 0;
         const bool keep = a.wideBits && sw <= kRankWordsMax;
+        // Heavy rows record their entries per slab of 2^kSlabShift columns
+        // (from `base`), for the numeric pass to cut them into pieces.
+        if (tid == 0) {
+            int32_t sl = -1;
+            const int64_t nslabs = ((end - base) + (1 << kSlabShift) - 1) >> kSlabShift;
+            if (a.slabCnt && !rowCap && a.rowP[row] >= kHeavyP && winBits >= (1 << kSlabShift) &&
+                nslabs <= kMaxSlabs) {
+                sl = (int32_t)atomicAdd(&a.ctr[CTR_HEAVY], 1u);
+                if (sl >= a.heavyCap) sl = -1;
+            }
+            slot = sl;
+            if (a.heavySlot) a.heavySlot[row] = sl;
+        }
         int cnt = 0;
         // Rows over several windows enumerate, per window, only the part of
         // each B row inside it (B's rows ascending).
@@ -591,6 +606,7 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
         for (int64_t c_lo = base; c_lo < end; c_lo += winBits) {
             const int words = (int)min((int64_t)winBits, end - c_lo + 31) >> 5;
             if (tid == 0) nt = rowCap ? 0 : cap + 1;
+            if (tid < (kWideWindowBitsMax >> kSlabShift)) slabSh[tid] = 0;
             __syncthreads();
             for (int32_t eb = e0; eb < e1; eb += THREADS) {
                 int nb;
@@ -618,11 +634,37 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
             }
             if (!rowCap) {
                 uint32_t *dst = keep ? a.wideBits + (size_t)item * kRankWordsMax : nullptr;
-                for (int i = tid; i < words; i += THREADS) {
-                    const uint32_t x = bm[i];
-                    cnt += __popc(x);
-                    if (dst) __stcs(&dst[i], x);
-                    bm[i] = 0u;
+                const int32_t sl = slot;
+                if (sl < 0) {
+                    for (int i = tid; i < words; i += THREADS) {
+                        const uint32_t x = bm[i];
+                        cnt += __popc(x);
+                        if (dst) __stcs(&dst[i], x);
+                        bm[i] = 0u;
+                    }
+                } else {
+                    // Groups of 32 consecutive words per thread (a slab is 64
+                    // groups); lanes start at different words of their group
+                    // so that a warp's loads hit 32 banks.
+                    const int lane = tid & 31;
+                    for (int g = tid; 32 * g < words; g += THREADS) {
+                        int c = 0;
+                        for (int k = 0; k < 32; ++k) {
+                            const int i = 32 * g + ((k + lane) & 31);
+                            if (i < words) {
+                                const uint32_t x = bm[i];
+                                c += __popc(x);
+                                if (dst) __stcs(&dst[i], x);
+                                bm[i] = 0u;
+                            }
+                        }
+                        cnt += c;
+                        if (c) atomicAdd(&slabSh[(32 * g) >> (kSlabShift - 5)], c);
+                    }
+                    __syncthreads();
+                    const int s0 = (int)((c_lo - base) >> kSlabShift);
+                    const int ns = (words + (1 << (kSlabShift - 5)) - 1) >> (kSlabShift - 5);
+                    for (int t = tid; t < ns; t += THREADS) a.slabCnt[(size_t)sl * kMaxSlabs + s0 + t] = slabSh[t];
                 }
                 if (keep && tid == 0) a.wideSlot[row] = item;
                 __syncthreads();
@@ -1664,6 +1706,48 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_rankm(NumArgs a, int32_t lo, 
     }
 }
 
+// Work items of the dense bin for list[lo, lo + n): one per row, except that
+// a row of more than kPieceNnz entries whose slab counts the symbolic pass
+// recorded (B's rows ascending) is cut at slab boundaries into pieces of
+// about kPieceNnz entries and at most kPieceSlabs slabs.  Every item is
+// independent: it knows its columns and where its entries start in C's row.
+__global__ void __launch_bounds__(256) k_dense_items(NumArgs a, int32_t lo, int32_t n) {
+    const int32_t i = (int32_t)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) return;
+    const int32_t row = a.list[lo + i];
+    const int64_t nnz = a.Cp[row + 1] - a.Cp[row];
+    const int32_t sl = a.heavySlot[row];
+    auto put = [&](int s0, int s1, int32_t cnt, int64_t off) {
+        const uint32_t k = atomicAdd(&a.ctr[CTR_ITEMS], 1u);
+        if (k >= (uint32_t)a.itemCap) {
+            raise(a.err, DEV_TABLE_FULL);
+            return;
+        }
+        a.items[k] = DenseItem{row, (int16_t)s0, (int16_t)s1, cnt, off};
+    };
+    if (sl < 0 || !a.bSorted || nnz <= kPieceNnz) {
+        put(-1, -1, (int32_t)min(nnz, (int64_t)INT32_MAX), 0);
+        return;
+    }
+    const int64_t base = (int64_t)(a.rowLo[row] >> 5) << 5;
+    const int ns = (int)((((int64_t)a.rowHi[row] + 1 - base) + (1 << kSlabShift) - 1) >> kSlabShift);
+    const int32_t *sc = a.slabCnt + (size_t)sl * kMaxSlabs;
+    int s0 = 0;
+    int32_t acc = 0;
+    int64_t off = 0;
+    for (int s = 0; s < ns; ++s) {
+        const int32_t c = sc[s];
+        if (s > s0 && (acc + c > kPieceNnz || s - s0 == kPieceSlabs)) {
+            put(s0, s, acc, off);
+            off += acc;
+            acc = 0;
+            s0 = s;
+        }
+        acc += c;
+    }
+    put(s0, ns, acc, off);
+}
+
 // Dense rows (windows wider than the CTA rank kernel's): persistent CTAs,
 // one per SM, take rows from a counter and apply the rank method over
 // windows of WIN words of the row's span (2^20 columns in shared memory).
@@ -1693,22 +1777,36 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
     int32_t *gbase = reinterpret_cast<int32_t *>(wpre + WIN);
     const int tid = threadIdx.x, lane = tid & 31;
     for (int i = tid; i < WIN; i += THREADS) bits[i] = 0u;
+    // With work items (heavy rows cut into pieces), the items the builder
+    // wrote before this launch; otherwise the bin's rows.
+    const int32_t nitems = a.items ? (int32_t)min(*(volatile uint32_t *)&a.ctr[CTR_ITEMS], (uint32_t)a.itemCap)
+                                   : count;
     for (;;) {
         if (tid == 0) next = (int32_t)atomicAdd(&a.ctr[CTR_NUM_RANKWIN], 1u);
         __syncthreads();
-        if (next >= count) break;
+        if (next >= nitems) break;
         const int32_t item = next;
-        const int32_t row = a.list[lo + item];
+        DenseItem it{0, -1, -1, 0, 0};
+        if (a.items) it = a.items[item];
+        const int32_t row = a.items ? it.row : a.list[lo + item];
         const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
         const int64_t expect = a.Cp[row + 1] - a.Cp[row];
         const int64_t obase = a.Cp[row] - a.outBase;
         const int32_t shift = col_shift(a, row);
-        const int64_t end = (int64_t)a.rowHi[row] + 1;
-        const int64_t start = (int64_t)(a.rowLo[row] >> 5) << 5;
-        // Rows over several windows enumerate, per window, only the part
-        // of each B row inside it (B's rows ascending).
-        const bool clip = a.bSorted && end - start > (int64_t)WIN * 32;
-        int64_t run = 0;
+        int64_t end = (int64_t)a.rowHi[row] + 1;
+        int64_t start = (int64_t)(a.rowLo[row] >> 5) << 5;
+        int64_t run = 0, expectEnd = expect;
+        if (it.s0 >= 0) {
+            // A piece: the row's columns [start + s0 slabs, start + s1 slabs).
+            const int64_t b = start;
+            start = b + ((int64_t)it.s0 << kSlabShift);
+            end = min(end, b + ((int64_t)it.s1 << kSlabShift));
+            run = it.off;
+            expectEnd = it.off + it.cnt;
+        }
+        // Rows over several windows and pieces enumerate, per window, only
+        // the part of each B row inside it (B's rows ascending).
+        const bool clip = a.bSorted && (it.s0 >= 0 || end - start > (int64_t)WIN * 32);
         for (int64_t c_lo = start; c_lo < end; c_lo += (int64_t)WIN * 32) {
             const int nwords = (int)min((int64_t)WIN, (end - c_lo + 31) >> 5);
             const uint32_t nbits = (uint32_t)nwords * 32u;
@@ -1788,7 +1886,7 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
             __syncthreads();
             run += tot;
         }
-        if (tid == 0 && run != expect) raise(a.err, DEV_COUNT_MISMATCH);
+        if (tid == 0 && run != expectEnd) raise(a.err, DEV_COUNT_MISMATCH);
         __syncthreads();  // every thread has read `next` before it changes
     }
 }
@@ -2307,6 +2405,7 @@ cudaError_t preload_spgemm_kernels() {
         (const void *)k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>,
         (const void *)k_num_hash_cta<kNumCtaLThreads, kNumCtaLTable>,
         (const void *)k_num_rankwin<kRankWinThreads, kRankWinWords>,
+        (const void *)k_dense_items,
         (const void *)k_num_dscr<kRankWinThreads, kRankWinWords>,
         (const void *)k_num_gdense<kGdenseThreads>,
         (const void *)k_num_dense<kDenseThreads, kDenseWindow, kDenseStage, true>,
@@ -2424,7 +2523,16 @@ void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaS
             if (a.tune.denseMethod == 0) {
                 cudaMemsetAsync(a.ctr + CTR_NUM_RANKWIN, 0, sizeof(uint32_t), s);
                 const int per_sm = std::max(1, (int)((227 * 1024) / (kSmemRankWin + 1024)));
-                const int grid = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1) * per_sm);
+                int64_t work = n;
+                if (a.items) {
+                    // Heavy rows cut into pieces: the items are built on the
+                    // device, so the grid is the persistent one.
+                    cudaMemsetAsync(a.ctr + CTR_ITEMS, 0, sizeof(uint32_t), s);
+                    k_dense_items<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(a, lo, n);
+                    ++*launches;
+                    work = (int64_t)a.itemCap;
+                }
+                const int grid = (int)std::min<int64_t>(work, (int64_t)std::max(a.numSms, 1) * per_sm);
                 k_num_rankwin<kRankWinThreads, kRankWinWords>
                     <<<(unsigned)grid, kRankWinThreads, kSmemRankWin, s>>>(a, lo, n);
             } else if (a.tune.denseMethod == 3 && a.scr) {

@@ -141,6 +141,8 @@ typedef struct {
     double t_num_bin_ms[DBD_NUM_BINS];  /* with time_kernels: numeric kernels of each bin, summed over chunks */
     int64_t io_direct;        /* +I/O: 1 when the files were written with O_DIRECT */
     int64_t resumed_from_row; /* +I/O with io_resume: the row an earlier run's manifest let this one start at */
+    int64_t heavy_rows;       /* rows whose per-slab counts the symbolic pass kept, so that the dense bin
+                                 could cut them into column pieces */
 } dbd_stats;
 
 /* ---- lifecycle ---------------------------------------------------------- */

@@ -289,6 +289,34 @@ def test_dense_rows_over_several_windows(ctx, orc):
             check(res.C, A, B, orc)
 
 
+def test_dense_rows_cut_into_pieces(ctx, orc):
+    """Dense-bin rows of more than 2^16 entries over 2.5M columns: the
+    symbolic pass keeps their per-slab counts and the numeric pass cuts them
+    into column pieces of about 2^16 entries, each its own work item; B rows
+    mix scattered columns with runs that cross slab and window edges."""
+    rng = np.random.default_rng(44)
+    n = 2_500_000
+    rows, cols = [], []
+    for r in range(3000):
+        c = rng.choice(n, 50, replace=False)
+        if r % 5 == 0:  # a run across a slab edge (2^16) or a window edge (2^20)
+            edge = ((1 + r % 7) << 16) if r % 2 else ((1 + r % 2) << 20)
+            c = np.unique(np.concatenate([c, np.arange(edge - 30, edge + 30)]))
+        rows.append(np.full(c.size, r))
+        cols.append(c)
+    rows, cols = np.concatenate(rows), np.concatenate(cols)
+    B = gen._from_coo(3000, n, rows, cols, rng.uniform(-1, 1, rows.size))
+    A = gen.uniform_rows(12, 2600, seed=13, n_cols=3000, dist="uniform")
+    res = ctx.spgemm(A, B, scope="kernel")
+    check(res.C, A, B, orc)
+    assert res.stats["rows_per_bin"][8] == A.n_rows and res.stats["heavy_rows"] == A.n_rows
+    assert np.diff(res.C.row_ptr).min() > 65536  # every row is cut into pieces
+    # B's rows out of column order: no pieces (each row one item).
+    res = ctx.spgemm(A, shuffled_rows(rng, B), scope="kernel")
+    check(res.C, A, B, orc)
+    assert res.stats["heavy_rows"] == 0
+
+
 def test_dense_rows_unsorted_b(ctx, orc):
     """Dense-window rows with B rows out of column order take the rescanning path."""
     rng = np.random.default_rng(5)
