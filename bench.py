@@ -10,7 +10,8 @@ segmentation + categorisation + symbolic + every chunk's numeric kernels, C
 streamed through the device slot), A resident in HBM, L2 flushed between
 steps by a 512 MiB device write outside the timed events.  --workload rmat18
 runs the in-core R-MAT scale 18 workload (n = 262,144, edge factor 8, blocks
-of 4096; C resident), laplacian256, batched512 and adjoint100k the others.
+of 4096; C resident), laplacian256, batched512 and adjoint100k the others;
+rmat21rows is a profiling case (a slice of the 2^21 rows times the whole matrix).
 
 Also reported: e2e = the same multiply through the C ABI (dbd_spgemm) with
 host buffers, H2D of A and D2H of the whole C inside the timed region (the
@@ -868,6 +869,67 @@ def run_outofcore(args, local, rank=0, world=1):
     return 0
 
 
+def run_slice(args, local):
+    """Rows [200704, 210944) of the out-of-core R-MAT 2^21 workload times its
+    whole A, C resident (214M entries, 2.6 GB): a middle chunk's mix of
+    dense-bin rows in a multiply small enough for a full ncu capture of its
+    kernels (`ncu -k regex:k_num_rankwin ...`).  Kernel scope, CUDA events;
+    per-kernel times from a second context with the bins serialised."""
+    import torch
+    import dbd_gb300 as dbd
+    from dbd_gb300.csr import CSR
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(local)
+    A = make_workload("rmat21")
+    r0, r1 = 200704, 210944
+    e0, e1 = int(A.row_ptr[r0]), int(A.row_ptr[r1])
+    S = CSR(r1 - r0, A.n_cols, (A.row_ptr[r0:r1 + 1] - e0).astype(np.int32), A.col_idx[e0:e1], A.val[e0:e1])
+    lens = np.diff(A.row_ptr).astype(np.int64)
+    P = int(lens[S.col_idx].sum())
+    keep = []
+
+    def up(M):
+        t = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (M.row_ptr, M.col_idx, M.val)]
+        keep.append(t)
+        return CSR.from_device(M.n_rows, M.n_cols, M.nnz, *[x.data_ptr() for x in t])
+    dS, dA = up(S), up(A)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ms, st = [], None
+    with dbd.Context(cpu_gib=16, gpu_gib=16, rows_per_block=512, device=local) as ctx:
+        ctx.set_stream(stream.cuda_stream)
+        for _ in range(args.warmup):
+            ctx.spgemm(dS, dA, scope="kernel", fetch=False)
+            flush.zero_()
+        torch.cuda.synchronize()
+        with Clocks(local) as clk:
+            for _ in range(args.steps):
+                e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0_.record(stream)
+                st = ctx.spgemm(dS, dA, scope="kernel", fetch=False).stats
+                e1_.record(stream)
+                flush.zero_()
+                torch.cuda.synchronize()
+                ms.append(e0_.elapsed_time(e1_))
+    with dbd.Context(cpu_gib=16, gpu_gib=16, rows_per_block=512, device=local, time_kernels=True) as pctx:
+        pctx.set_stream(stream.cuda_stream)
+        pctx.spgemm(dS, dA, scope="kernel", fetch=False)
+        ps = pctx.spgemm(dS, dA, scope="kernel", fetch=False).stats
+    t = float(np.mean(ms)) / 1e3
+    kms = {NUM_NAMES[b]: round(ps["t_num_bin_ms"][b], 4) for b in NUM_NAMES if ps["t_num_bin_ms"][b]}
+    kms.update({SYM_NAMES[b]: round(ps["t_sym_bin_ms"][b], 4) for b in SYM_NAMES if ps["t_sym_bin_ms"][b]})
+    line = {"metric": METRIC, "value": round(2.0 * P / t / 1e9, 4), "unit": "GFLOPS", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded R-MAT, numpy PCG64)",
+            "config": {"workload": "rows [200704, 210944) of R-MAT scale 21, edge factor 16, seed 0, times the whole "
+                                   "matrix (a profiling case: one middle chunk's dense-bin rows, C resident)",
+                       "rows": r1 - r0, "products": P, "nnz_c": int(st["nnz_c"]), "heavy_rows": int(st["heavy_rows"]),
+                       "scope": "kernel", "l2": "512 MiB device write between steps"},
+            "gpu_launches": int(st["gpu_launches"]), "kernel_ms_per_step": kms, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -893,6 +955,8 @@ def main():
         if rank != 0:
             return 0
         return run_batched(args, local)
+    if args.workload == "rmat21rows":
+        return 0 if rank != 0 else run_slice(args, local)
     if args.workload == "rmat21":
         return run_outofcore(args, local, rank, world)
     if args.workload == "adjoint100k":
