@@ -795,9 +795,13 @@ def run_outofcore(args, local, rank=0, world=1):
                         "frac": round(bytes_alg / t_kernel / 1e9 / peak, 4),
                         "fp64_frac": round(2 * P / t_kernel / 1e12 / roof["fp64"]["peak"], 4)}
 
-    # +D2H: host A, C through the pinned ring, each step a full multiply.
+    # +D2H: host A, C through the pinned ring, each step a full multiply, on
+    # a context of its own, as a caller that copies C out would hold (the
+    # kernel-scope context's one large device slot is released first).
     ctx_tuning = ctx.tuning
-    ctx.set_stream(None)
+    ctx.close()
+    ctx = dbd.Context(cpu_gib=64, gpu_gib=24, rows_per_block=512, device=local, io_rotate_gib=rotate)
+    ctx.set_tuning(**ctx_tuning)
     td = []
     for i in range(max(1, args.e2e_steps) + 1):
         a = time.perf_counter()
