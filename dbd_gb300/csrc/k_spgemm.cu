@@ -1811,11 +1811,20 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
             const int nwords = (int)min((int64_t)WIN, (end - c_lo + 31) >> 5);
             const uint32_t nbits = (uint32_t)nwords * 32u;
             const int64_t c_hi = c_lo + nbits;
-            // Pass 1: the window's bits.
+            // Pass 1: the window's bits.  A row (or piece) of at most THREADS
+            // entries is staged once, with its A values, and pass 2 reuses
+            // the staging (no second round of loads and clipping searches).
+            const bool once = e1 - e0 <= THREADS;
+            int nb1 = 0;
+            int32_t total1 = 0;
             for (int32_t eb = e0; eb < e1; eb += THREADS) {
                 int nb;
-                const int32_t total = stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst,
-                                                                    nullptr, &nb, sh, clip, c_lo, c_hi);
+                const int32_t total =
+                    once ? stage_entries<THREADS, true>(a.A, a.B, eb, e1 - eb, pre, bst, av, &nb, sh, clip, c_lo, c_hi)
+                         : stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb,
+                                                         sh, clip, c_lo, c_hi);
+                nb1 = nb;
+                total1 = total;
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
                 warp_range_ld<4>(
@@ -1862,9 +1871,11 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
             __syncthreads();
             // Pass 2: the window's products into C's row in place.
             for (int32_t eb = e0; eb < e1; eb += THREADS) {
-                int nb;
-                const int32_t total = stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av,
-                                                                   &nb, sh, clip, c_lo, c_hi);
+                int nb = nb1;
+                const int32_t total =
+                    once ? total1
+                         : stage_entries<THREADS, true>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, av, &nb, sh,
+                                                        clip, c_lo, c_hi);
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
                 warp_range_ld<4>(
