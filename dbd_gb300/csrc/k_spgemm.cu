@@ -352,6 +352,57 @@ __device__ __forceinline__ void or_bits_runs(uint32_t *bm, bool v, uint32_t rel)
     if (v && (lane == 0 || pw != w)) atomicOr(&bm[w], acc);
 }
 
+// Writes the columns of a ranked bitmap with the work balanced by output
+// position: thread t emits output ranks [t tot / T, (t + 1) tot / T), a
+// contiguous run.  The bitmap is cut into THREADS groups of G consecutive
+// words; tbase[g] is the rank of group g's first column and tmask[g] the
+// mask of its non-empty words (both in shared memory).  A thread finds the
+// group holding its first rank by binary search, then walks words and bits
+// in order.  When the columns are written by the thread that owns their
+// words instead, a thread over a dense stretch of the row writes up to 32 G
+// columns while its neighbours write few, and the CTA waits for it.
+// emit(rank, word, bit) is called once per column.
+template <int THREADS, int G, class EMIT>
+__device__ __forceinline__ void write_columns_balanced(const uint32_t *bits, const int32_t *tbase,
+                                                       const uint32_t *tmask, int32_t tot, EMIT &&emit) {
+    static_assert(G >= 1 && G <= 32, "a group's words fit one mask");
+    const int tid = threadIdx.x;
+    const int32_t r0 = (int32_t)((int64_t)tot * tid / THREADS);
+    const int32_t r1 = (int32_t)((int64_t)tot * (tid + 1) / THREADS);
+    if (r0 >= r1) return;
+    // The last group whose first rank is at most r0 holds rank r0 (the
+    // next group starts above it, so this one is not empty).
+    int lo = 0, hi = THREADS - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tbase[mid] <= r0) lo = mid;
+        else hi = mid - 1;
+    }
+    int g = lo;
+    uint32_t m = tmask[g];
+    int32_t p = tbase[g];
+    int w = G * g + __ffs(m) - 1;
+    uint32_t word = bits[w];
+    while (p + __popc(word) <= r0) {
+        p += __popc(word);
+        m &= m - 1u;
+        w = G * g + __ffs(m) - 1;
+        word = bits[w];
+    }
+    for (; p < r0; ++p) word &= word - 1u;  // drop the bits before rank r0
+    for (; p < r1; ++p) {
+        while (!word) {
+            m &= m - 1u;
+            while (!m) m = tmask[++g];
+            w = G * g + __ffs(m) - 1;
+            word = bits[w];
+        }
+        const int b = __ffs(word) - 1;
+        word &= word - 1u;
+        emit(p, w, b);
+    }
+}
+
 // Contiguous share of [0, total) for this warp, in multiples of 32 products.
 template <int THREADS>
 __device__ __forceinline__ void warp_share(int32_t total, int32_t *tb, int32_t *te) {
@@ -1775,6 +1826,8 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
     uint32_t *bits = reinterpret_cast<uint32_t *>(smem + L::bytes);
     uint16_t *wpre = reinterpret_cast<uint16_t *>(bits + WIN);
     int32_t *gbase = reinterpret_cast<int32_t *>(wpre + WIN);
+    int32_t *tbase = gbase + WIN / 256;                          // per thread: rank of its first column
+    uint32_t *tmask = reinterpret_cast<uint32_t *>(tbase + THREADS);  // per thread: its non-empty words
     const int tid = threadIdx.x, lane = tid & 31;
     for (int i = tid; i < WIN; i += THREADS) bits[i] = 0u;
     // With work items (heavy rows cut into pieces), the items the builder
@@ -1857,16 +1910,17 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
                 int32_t p = base;
                 for (uint32_t m = mask; m; m &= m - 1u) {
                     const int w = 32 * tid + __ffs(m) - 1;
-                    uint32_t word = bits[w];
                     wpre[w] = (uint16_t)(p - gb);
-                    while (word) {
-                        const int b = __ffs(word) - 1;
-                        word &= word - 1u;
-                        if (run + p < expect) __stcs(&a.Ci[obase + run + p], (int32_t)(c_lo + (w << 5) + b - shift));
-                        ++p;
-                    }
+                    p += __popc(bits[w]);
                 }
+                tbase[tid] = base;
+                tmask[tid] = mask;
             }
+            __syncthreads();
+            // C's columns, balanced over the threads by output position.
+            write_columns_balanced<THREADS, 32>(bits, tbase, tmask, tot, [&](int32_t p, int w, int b) {
+                if (run + p < expect) __stcs(&a.Ci[obase + run + p], (int32_t)(c_lo + (w << 5) + b - shift));
+            });
             for (int64_t i = tid; i < tot && run + i < expect; i += THREADS) a.Cv[obase + run + i] = 0.0;
             __syncthreads();
             // Pass 2: the window's products into C's row in place.
@@ -2353,7 +2407,7 @@ constexpr int kGdenseThreads = 512;
 constexpr int kRankWinThreads = 1024;  // one CTA per SM: all its warps
 constexpr int kRankWinWords = 32768;  // 2^20 columns per window
 constexpr size_t kSmemRankWin = StageLayout<kRankWinThreads>::bytes + 6 * (size_t)kRankWinWords +
-                                4 * (size_t)(kRankWinWords / 256);
+                                4 * (size_t)(kRankWinWords / 256) + 8 * (size_t)kRankWinThreads;
 constexpr size_t kSmemGdenseBase = StageLayout<kGdenseThreads>::bytes;
 constexpr size_t kSmemDscr = StageLayout<kRankWinThreads>::bytes + 4 * (size_t)kRankWinWords;
 constexpr int kRankmRows = 5;  // 14.6 KiB per warp: three CTAs (15 warps) per SM
