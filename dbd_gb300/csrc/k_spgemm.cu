@@ -355,17 +355,16 @@ __device__ __forceinline__ void or_bits_runs(uint32_t *bm, bool v, uint32_t rel)
 // Writes the columns of a ranked bitmap with the work balanced by output
 // position: thread t emits output ranks [t tot / T, (t + 1) tot / T), a
 // contiguous run.  The bitmap is cut into THREADS groups of G consecutive
-// words; tbase[g] is the rank of group g's first column and tmask[g] the
-// mask of its non-empty words (both in shared memory).  A thread finds the
+// words (G <= 32); tbase[g] is the rank of group g's first column and
+// tmask[g] the mask of its non-empty words (both in shared memory).  A thread finds the
 // group holding its first rank by binary search, then walks words and bits
 // in order.  When the columns are written by the thread that owns their
 // words instead, a thread over a dense stretch of the row writes up to 32 G
 // columns while its neighbours write few, and the CTA waits for it.
 // emit(rank, word, bit) is called once per column.
-template <int THREADS, int G, class EMIT>
+template <int THREADS, class EMIT>
 __device__ __forceinline__ void write_columns_balanced(const uint32_t *bits, const int32_t *tbase,
-                                                       const uint32_t *tmask, int32_t tot, EMIT &&emit) {
-    static_assert(G >= 1 && G <= 32, "a group's words fit one mask");
+                                                       const uint32_t *tmask, int G, int32_t tot, EMIT &&emit) {
     const int tid = threadIdx.x;
     const int32_t r0 = (int32_t)((int64_t)tot * tid / THREADS);
     const int32_t r1 = (int32_t)((int64_t)tot * (tid + 1) / THREADS);
@@ -1320,6 +1319,11 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
     uint32_t *bits = reinterpret_cast<uint32_t *>(smem + L::bytes);
     int32_t *wpre = reinterpret_cast<int32_t *>(bits + maxWords);
     double *vals = reinterpret_cast<double *>(wpre + maxWords);
+    // Per thread, the rank of its first column and its non-empty words, kept
+    // in the staging area (idle between the passes).
+    static_assert(8 * THREADS <= L::bytes && kRankWordsMax <= 32 * THREADS, "rank groups");
+    int32_t *tbase = pre;
+    uint32_t *tmask = reinterpret_cast<uint32_t *>(pre + THREADS);
     const int tid = threadIdx.x, lane = tid & 31;
     const int32_t row = a.list[lo + blockIdx.x];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
@@ -1355,13 +1359,12 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
         }
     }
 
-    // Ranks and C's columns, per thread over its own wpt consecutive words
-    // (wpt a power of two, THREADS * wpt >= nwords): one sweep gives the
-    // thread the mask of its non-empty words and their bit count, a block
-    // scan the rank of its first column; then only the non-empty words are
-    // ranked and their columns written, a contiguous run per thread (no
-    // lane waits on a denser word of its neighbours).  Lanes start their
-    // sweeps at different words so that a warp's loads hit 32 banks.
+    // Ranks, per thread over its own wpt consecutive words (wpt a power of
+    // two, THREADS * wpt >= nwords): one sweep gives the thread the mask of
+    // its non-empty words and their bit count, a block scan the rank of its
+    // first column; then only the non-empty words are ranked.  Lanes start
+    // their sweeps at different words so that a warp's loads hit 32 banks.
+    // C's columns are then written balanced by output position.
     int wpt = 1;
     while (wpt * THREADS < nwords) wpt <<= 1;
     const int w0 = tid * wpt;
@@ -1377,19 +1380,22 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
         }
     }
     int32_t tot;
-    int32_t run = block_excl_scan<THREADS>(cnt, &tot, sh);
+    const int32_t base = block_excl_scan<THREADS>(cnt, &tot, sh);
     if (tid == 0 && tot != expect) raise(a.err, DEV_COUNT_MISMATCH);
-    for (uint32_t m = mask; m; m &= m - 1u) {
-        const int w = w0 + __ffs(m) - 1;
-        uint32_t word = bits[w];
-        wpre[w] = run;
-        while (word) {
-            const int b = __ffs(word) - 1;
-            word &= word - 1u;
-            if (run < expect) __stcs(&a.Ci[obase + run], obc + (w << 5) + b);
-            ++run;
+    {
+        int32_t p = base;
+        for (uint32_t m = mask; m; m &= m - 1u) {
+            const int w = w0 + __ffs(m) - 1;
+            wpre[w] = p;
+            p += __popc(bits[w]);
         }
+        tbase[tid] = base;
+        tmask[tid] = mask;
     }
+    __syncthreads();
+    write_columns_balanced<THREADS>(bits, tbase, tmask, wpt, tot, [&](int32_t p, int w, int b) {
+        if (p < expect) __stcs(&a.Ci[obase + p], obc + (w << 5) + b);
+    });
     __syncthreads();
 
     if constexpr (GLOBAL_ACC) {
@@ -1918,7 +1924,7 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
             }
             __syncthreads();
             // C's columns, balanced over the threads by output position.
-            write_columns_balanced<THREADS, 32>(bits, tbase, tmask, tot, [&](int32_t p, int w, int b) {
+            write_columns_balanced<THREADS>(bits, tbase, tmask, 32, tot, [&](int32_t p, int w, int b) {
                 if (run + p < expect) __stcs(&a.Ci[obase + run + p], (int32_t)(c_lo + (w << 5) + b - shift));
             });
             for (int64_t i = tid; i < tot && run + i < expect; i += THREADS) a.Cv[obase + run + i] = 0.0;
