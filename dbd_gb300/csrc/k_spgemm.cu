@@ -28,7 +28,7 @@
 //   wide rows   (symbolic)      persistent CTAs, a shared bitmap over windows
 //                               of up to 2^20 columns that stays zero between
 //                               rows, kept for the numeric rank kernels
-//   dense rows  (numeric)       persistent CTAs, bitmap ranks over 2^20-column
+//   dense rows  (numeric)       persistent CTAs, bitmap ranks over 2^19-column
 //                               windows in shared memory, work per window
 //                               over its non-empty words only, products
 //                               reduced into C in place
@@ -197,48 +197,110 @@ __device__ __forceinline__ int block_sum_i(int v, int *sh) {
     return r;
 }
 
+// Lower bound of target in the ascending bi (the first index whose column
+// is >= target), known to lie in [l, h], found by the group of m aligned
+// lanes this lane belongs to (m a power of two, lg = log2 m): each step the
+// m lanes probe the midpoints of m equal slices of [l, h) at once and the
+// range shrinks about m times.  m = 1 is a binary search.  Every lane of
+// the warp calls; lanes with l == h wait for their warp.
+__device__ __forceinline__ int32_t group_lower_bound(const int32_t *bi, int32_t l, int32_t h, int64_t target,
+                                                    int lg) {
+    const int lane = threadIdx.x & 31;
+    const int m = 1 << lg;
+    const int j = lane & (m - 1);
+    const int base = lane & ~(m - 1);
+    const uint32_t gm = m == 32 ? FULL : (1u << m) - 1u;
+    while (__any_sync(FULL, l < h)) {
+        const int64_t n = h - l;
+        const bool act = l < h;
+        const int32_t p = l + (int32_t)((n * (2 * j + 1)) >> (lg + 1));
+        const bool below = act && (int64_t)__ldg(&bi[p]) < target;
+        const int c = __popc((__ballot_sync(FULL, below) >> base) & gm);
+        if (act) {
+            // The group's first c probes are below target (bi ascends).
+            const int32_t nl = c > 0 ? l + (int32_t)((n * (2 * c - 1)) >> (lg + 1)) + 1 : l;
+            const int32_t nh = c < m ? l + (int32_t)((n * (2 * c + 1)) >> (lg + 1)) : h;
+            l = nl;
+            h = nh;
+        }
+    }
+    return l;
+}
+
 // A batch of up to THREADS entries of one A row staged in shared memory,
 // keeping only entries whose B row is non-empty: pre[i] = exclusive prefix
 // of |B_k| (pre[*nb] = the batch's products), bst[i] = first position of B_k,
 // av[i] = A value.  Every staged entry has at least one product, so 32
 // consecutive products span at most 32 entries.  Returns the products.
 // With clip (B's rows ascending), each entry keeps only the part of its B
-// row inside the column window [cLo, cHi) (two binary searches at most), so
-// a row walked window by window enumerates each product once.
+// row inside the column window [cLo, cHi), so a row walked window by window
+// enumerates each product once.  The two ends of each part are lower-bound
+// searches over the B row, which are dependent L2 loads: an entry gets
+// as many lanes as the batch leaves free (up to 32), half searching each
+// end, so that the CTA waits a few probes instead of two binary searches.
+// With cur (a row walked through consecutive windows with the same batch),
+// cur[i] carries where entry i's part of the previous window ended, which
+// is where this window's starts (carry), and all the entry's lanes search
+// the other end.
 template <int THREADS, bool VALS>
 __device__ __forceinline__ int32_t stage_entries(const CsrDev &A, const CsrDev &B, int32_t eb, int n_in,
                                                  int32_t *pre, int32_t *bst, double *av, int *nb,
                                                  int32_t *sh, bool clip = false, int64_t cLo = 0,
-                                                 int64_t cHi = 0) {
+                                                 int64_t cHi = 0, int32_t *cur = nullptr, bool carry = false) {
     const int tid = threadIdx.x;
     int32_t len = 0, s = 0;
     double a = 0.0;
-    if (tid < n_in) {
-        const int32_t k = A.idx[eb + tid];
-        s = B.ptr[k];
-        len = B.ptr[k + 1] - s;
-        if constexpr (VALS) a = A.val[eb + tid];
-        if (clip && len > 0) {
-            const int32_t *bi = B.idx + s;
-            int32_t a0 = 0, a1 = len;
-            if ((int64_t)__ldg(&bi[0]) < cLo) {
-                int32_t l = 1, h = len;
-                while (l < h) {
-                    const int32_t m = (l + h) >> 1;
-                    if ((int64_t)__ldg(&bi[m]) < cLo) l = m + 1; else h = m;
-                }
-                a0 = l;
-            }
-            if (a0 < len && (int64_t)__ldg(&bi[len - 1]) >= cHi) {
-                int32_t l = a0, h = len - 1;
-                while (l < h) {
-                    const int32_t m = (l + h) >> 1;
-                    if ((int64_t)__ldg(&bi[m]) < cHi) l = m + 1; else h = m;
-                }
-                a1 = l;
-            }
-            s += a0;
-            len = max(0, a1 - a0);
+    if (!clip) {
+        if (tid < n_in) {
+            const int32_t k = A.idx[eb + tid];
+            s = B.ptr[k];
+            len = B.ptr[k + 1] - s;
+            if constexpr (VALS) a = A.val[eb + tid];
+        }
+    } else {
+        // Lanes per entry: L = 2^lgL, the largest with n_in L <= THREADS.
+        int lgL = 0;
+        while (lgL < 5 && n_in * (2 << lgL) <= THREADS) ++lgL;
+        const int L = 1 << lgL;
+        const int ent = tid >> lgL, sub = tid & (L - 1);
+        int32_t rs = 0, rl = 0;
+        if (ent < n_in) {
+            const int32_t k = A.idx[eb + ent];
+            rs = B.ptr[k];
+            rl = B.ptr[k + 1] - rs;
+        }
+        const int32_t *bi = B.idx + rs;
+        bool needLo = false, needHi = false;
+        int32_t a0 = 0;
+        if (rl > 0) {
+            if (carry) a0 = cur[ent] - rs;
+            else needLo = (int64_t)__ldg(&bi[0]) < cLo;
+            needHi = (int64_t)__ldg(&bi[rl - 1]) >= cHi;
+        }
+        int32_t lo, hi;
+        if (carry || L == 1) {
+            // One search per group of L lanes (L == 1: both ends in turn);
+            // the lanes of a group reach the same bounds.
+            int32_t r0 = a0;
+            if (!carry) r0 = group_lower_bound(bi, needLo ? 1 : 0, needLo ? rl : 0, cLo, 0);
+            lo = r0;
+            hi = group_lower_bound(bi, needHi ? r0 : rl, needHi ? rl - 1 : rl, cHi, lgL);
+        } else {
+            // Lanes [0, L/2) of the group find the start, [L/2, L) the end
+            // (one call site: the searches hold warp votes).
+            const bool upper = sub >= L / 2;
+            const int32_t l0 = upper ? (needHi ? 0 : rl) : (needLo ? 1 : 0);
+            const int32_t h0 = upper ? (needHi ? rl - 1 : rl) : (needLo ? rl : 0);
+            const int32_t r = group_lower_bound(bi, l0, h0, upper ? cHi : cLo, lgL - 1);
+            const int g0 = (tid & 31) & ~(L - 1);
+            lo = __shfl_sync(FULL, r, g0);
+            hi = __shfl_sync(FULL, r, g0 + L / 2);
+        }
+        if (ent < n_in && sub == 0) {
+            s = rs + lo;
+            len = max(0, hi - lo);
+            if (cur) cur[ent] = rs + max(hi, lo);
+            if constexpr (VALS) a = A.val[eb + ent];
         }
     }
     int32_t total, kept;
@@ -326,48 +388,34 @@ struct ColVal {
     double v;
 };
 
-// Sets one bit per lane in a shared bitmap with one atomicOr per run of
-// lanes that share a word.  Lanes whose products come from the same sorted B
-// row hold ascending columns, so equal words sit in adjacent lanes; a
-// segmented OR over such runs leaves each run's bits in its first lane.
-// Bits of equal words in non-adjacent lanes are ORed more than once, which
-// is harmless.  When no two adjacent lanes share a word (sparse rows, the
-// common case of power-law matrices) every lane ORs its own bit directly.
-// All lanes call; `v` marks lanes with a bit.
-__device__ __forceinline__ void or_bits_runs(uint32_t *bm, bool v, uint32_t rel) {
-    const int lane = threadIdx.x & 31;
-    const int32_t w = v ? (int32_t)(rel >> 5) : -1 - lane;
-    uint32_t acc = v ? 1u << (rel & 31) : 0u;
-    if (!__any_sync(FULL, __shfl_up_sync(FULL, w, 1) == w && lane > 0)) {
-        if (v) atomicOr(&bm[w], acc);
-        return;
-    }
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int32_t ow = __shfl_down_sync(FULL, w, d);
-        const uint32_t ob = __shfl_down_sync(FULL, acc, d);
-        if (lane + d < 32 && ow == w) acc |= ob;
-    }
-    const int32_t pw = __shfl_up_sync(FULL, w, 1);
-    if (v && (lane == 0 || pw != w)) atomicOr(&bm[w], acc);
+// Sets bit rel of a shared bitmap on lanes with v, one atomicOr per lane.
+// Lanes that share a word serialise on it; a segmented OR over runs of such
+// lanes (one atomic per run) costs more instructions than that saves, on
+// sparse and dense power-law windows alike.
+__device__ __forceinline__ void or_bit(uint32_t *bm, bool v, uint32_t rel) {
+    if (v) atomicOr(&bm[rel >> 5], 1u << (rel & 31));
 }
 
 // Writes the columns of a ranked bitmap with the work balanced by output
-// position: thread t emits output ranks [t tot / T, (t + 1) tot / T), a
-// contiguous run.  The bitmap is cut into THREADS groups of G consecutive
-// words (G <= 32); tbase[g] is the rank of group g's first column and
-// tmask[g] the mask of its non-empty words (both in shared memory).  A thread finds the
-// group holding its first rank by binary search, then walks words and bits
-// in order.  When the columns are written by the thread that owns their
-// words instead, a thread over a dense stretch of the row writes up to 32 G
-// columns while its neighbours write few, and the CTA waits for it.
-// emit(rank, word, bit) is called once per column.
-template <int THREADS, class EMIT>
+// position: thread t writes out[r] = colbase + 32 w + b for the output ranks
+// r in [t tot / T, (t + 1) tot / T) below lim, a contiguous run.  The bitmap
+// is cut into THREADS groups of G consecutive words (G <= 32); tbase[g] is
+// the rank of group g's first column and tmask[g] the mask of its non-empty
+// words (both in shared memory).  A thread finds the group holding its
+// first rank by binary search, then walks words and bits in order.  (When
+// the columns are written by the thread that owns their words instead, a
+// thread over a dense stretch of the row writes up to 32 G columns while
+// its neighbours write few, and the CTA waits for it.)  The run goes out in
+// aligned 16-byte stores, its ragged ends one column at a time: each lane
+// of a warp writes its own run, so per-column stores would cost a memory
+// transaction per column.
+template <int THREADS>
 __device__ __forceinline__ void write_columns_balanced(const uint32_t *bits, const int32_t *tbase,
-                                                       const uint32_t *tmask, int G, int32_t tot, EMIT &&emit) {
+                                                       const uint32_t *tmask, int G, int32_t tot, int32_t *out,
+                                                       int64_t lim, int64_t colbase) {
     const int tid = threadIdx.x;
     const int32_t r0 = (int32_t)((int64_t)tot * tid / THREADS);
-    const int32_t r1 = (int32_t)((int64_t)tot * (tid + 1) / THREADS);
+    const int32_t r1 = (int32_t)min((int64_t)tot * (tid + 1) / THREADS, lim);
     if (r0 >= r1) return;
     // The last group whose first rank is at most r0 holds rank r0 (the
     // next group starts above it, so this one is not empty).
@@ -389,6 +437,9 @@ __device__ __forceinline__ void write_columns_balanced(const uint32_t *bits, con
         word = bits[w];
     }
     for (; p < r0; ++p) word &= word - 1u;  // drop the bits before rank r0
+    // out + r is 16-byte aligned when (k0 + r) % 4 == 0.
+    const uint32_t k0 = (uint32_t)(reinterpret_cast<uintptr_t>(out) >> 2) & 3u;
+    int32_t q0 = 0, q1 = 0, q2 = 0, q3 = 0;
     for (; p < r1; ++p) {
         while (!word) {
             m &= m - 1u;
@@ -398,7 +449,23 @@ __device__ __forceinline__ void write_columns_balanced(const uint32_t *bits, con
         }
         const int b = __ffs(word) - 1;
         word &= word - 1u;
-        emit(p, w, b);
+        const int32_t c = (int32_t)(colbase + (w << 5) + b);
+        const uint32_t k = (k0 + (uint32_t)p) & 3u;
+        if (k == 0) q0 = c;
+        else if (k == 1) q1 = c;
+        else if (k == 2) q2 = c;
+        else q3 = c;
+        if (k == 3 || p + 1 == r1) {
+            const int32_t first = p - (int32_t)k;  // the quad's first rank
+            if (k == 3 && first >= r0) {
+                __stcs(reinterpret_cast<int4 *>(out + first), make_int4(q0, q1, q2, q3));
+            } else {
+                for (int32_t t = max(first, r0); t <= p; ++t) {
+                    const uint32_t kt = (k0 + (uint32_t)t) & 3u;
+                    __stcs(out + t, kt == 0 ? q0 : (kt == 1 ? q1 : (kt == 2 ? q2 : q3)));
+                }
+            }
+        }
     }
 }
 
@@ -561,33 +628,22 @@ __global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t beg
     if (tid == 0) a.rowNnz[row] = cnt;
 }
 
-// or_bits_runs that also counts and records: returns the number of bits this
-// lane newly set (popc of its OR against the word's old value), and appends
+// or_bit that also counts and records: returns the number of bits this
+// lane newly set (its bit, if the word's old value lacked it), and appends
 // every word it finds zero to touched[] (through *nt; entries past cap are
-// dropped, *nt still counts them).  All lanes call.
+// dropped, *nt still counts them).  Lanes that share a bit or a word
+// serialise on its atomic, so exactly one of them counts the bit and one
+// records the word.
 __device__ __forceinline__ int or_bits_count(uint32_t *bm, bool v, uint32_t rel, int32_t *touched, int *nt,
                                              int cap) {
-    const int lane = threadIdx.x & 31;
-    const int32_t w = v ? (int32_t)(rel >> 5) : -1 - lane;
-    uint32_t acc = v ? 1u << (rel & 31) : 0u;
-    bool head = v;
-    if (__any_sync(FULL, __shfl_up_sync(FULL, w, 1) == w && lane > 0)) {
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int32_t ow = __shfl_down_sync(FULL, w, d);
-            const uint32_t ob = __shfl_down_sync(FULL, acc, d);
-            if (lane + d < 32 && ow == w) acc |= ob;
-        }
-        const int32_t pw = __shfl_up_sync(FULL, w, 1);
-        head = v && (lane == 0 || pw != w);
-    }
-    if (!head) return 0;
-    const uint32_t old = atomicOr(&bm[w], acc);
+    if (!v) return 0;
+    const uint32_t bit = 1u << (rel & 31);
+    const uint32_t old = atomicOr(&bm[rel >> 5], bit);
     if (cap > 0 && old == 0u) {
         const int k = atomicAdd(nt, 1);
-        if (k < cap) touched[k] = w;
+        if (k < cap) touched[k] = (int32_t)(rel >> 5);
     }
-    return __popc(acc & ~old);
+    return (old & bit) ? 0 : 1;
 }
 
 // Words a wide-row window clears one by one: past a quarter of the window a
@@ -616,6 +672,7 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
     uint32_t *bm = reinterpret_cast<uint32_t *>(smem + L::bytes);
     int32_t *touched = reinterpret_cast<int32_t *>(bm + (winBits >> 5));
     const int cap = wide_touch_cap(winBits);
+    int32_t *cur = touched + cap;  // per staged entry: its B cursor across windows
     const int tid = threadIdx.x;
     for (int i = tid; i < (winBits >> 5); i += THREADS) bm[i] = 0u;
     for (;;) {
@@ -653,6 +710,7 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
         // Rows over several windows enumerate, per window, only the part of
         // each B row inside it (B's rows ascending).
         const bool clip = a.bSorted && end - base > (int64_t)winBits;
+        const bool once = e1 - e0 <= THREADS;  // one batch: its cursors carry over the windows
         for (int64_t c_lo = base; c_lo < end; c_lo += winBits) {
             const int words = (int)min((int64_t)winBits, end - c_lo + 31) >> 5;
             if (tid == 0) nt = rowCap ? 0 : cap + 1;
@@ -660,8 +718,9 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
             __syncthreads();
             for (int32_t eb = e0; eb < e1; eb += THREADS) {
                 int nb;
-                const int32_t total = stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst,
-                                                                    nullptr, &nb, sh, clip, c_lo, c_lo + winBits);
+                const int32_t total =
+                    stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb, sh, clip,
+                                                  c_lo, c_lo + winBits, once ? cur : nullptr, once && c_lo != base);
                 int32_t tb, te;
                 warp_share<THREADS>(total, &tb, &te);
                 if (rowCap) {
@@ -1353,7 +1412,7 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
                 pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
                 [&](bool v, int32_t col, int) {
                     const uint32_t rel = v ? (uint32_t)(col - cbase) : 0u;
-                    or_bits_runs(bits, v && in_window(rel, (uint32_t)nwords * 32u, a.err), rel);
+                    or_bit(bits, v && in_window(rel, (uint32_t)nwords * 32u, a.err), rel);
                 });
             __syncthreads();
         }
@@ -1393,9 +1452,7 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
         tmask[tid] = mask;
     }
     __syncthreads();
-    write_columns_balanced<THREADS>(bits, tbase, tmask, wpt, tot, [&](int32_t p, int w, int b) {
-        if (p < expect) __stcs(&a.Ci[obase + p], obc + (w << 5) + b);
-    });
+    write_columns_balanced<THREADS>(bits, tbase, tmask, wpt, tot, a.Ci + obase, expect, obc);
     __syncthreads();
 
     if constexpr (GLOBAL_ACC) {
@@ -1593,7 +1650,7 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_rankw(NumArgs a, int32_t lo, 
             const int32_t j = chunk_pos(c, t, nullptr);
             const uint32_t rel = t < c.total ? (uint32_t)(a.B.idx[j] - cbase) : 0u;
             const bool v = t < c.total && in_window(rel, kWarpSpanWords * 32, a.err);
-            or_bits_runs(bm, v, rel);
+            or_bit(bm, v, rel);
         }
     }
     __syncwarp();
@@ -1642,7 +1699,7 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_rankw(NumArgs a, int32_t lo, 
     for (int64_t i = lane; i < nout; i += 32) a.Cv[obase + i] = vals[i];
 }
 
-// or_bits_runs that also marks, in a summary bitmap (one bit per word),
+// A segmented OR over runs of lanes that share a word that also marks, in a summary bitmap (one bit per word),
 // every word it finds zero.  All lanes call.
 __device__ __forceinline__ void or_bits_mark(uint32_t *bm, uint32_t *sum, bool v, uint32_t rel) {
     const int lane = threadIdx.x & 31;
@@ -1806,8 +1863,8 @@ __global__ void __launch_bounds__(256) k_dense_items(NumArgs a, int32_t lo, int3
 }
 
 // Dense rows (windows wider than the CTA rank kernel's): persistent CTAs,
-// one per SM, take rows from a counter and apply the rank method over
-// windows of WIN words of the row's span (2^20 columns in shared memory).
+// two per SM, take rows from a counter and apply the rank method over
+// windows of WIN words of the row's span (2^19 columns in shared memory).
 // Per window: a pass over the row's products sets the bits inside the
 // window; a sweep gives each thread the non-empty-word mask and bit count
 // of its 32 words (one summary word), and a scan of the counts gives every
@@ -1819,7 +1876,7 @@ __global__ void __launch_bounds__(256) k_dense_items(NumArgs a, int32_t lo, int3
 // rank (FP64 L2 reductions).  Power-law rows spread thinly over millions of
 // columns pay for their entries, not for their span, past the one sweep.
 template <int THREADS, int WIN>
-__global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, int32_t count) {
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_num_rankwin(NumArgs a, int32_t lo, int32_t count) {
     static_assert(WIN == 32 * THREADS, "one summary word of 32 bitmap words per thread");
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
@@ -1834,6 +1891,7 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
     int32_t *gbase = reinterpret_cast<int32_t *>(wpre + WIN);
     int32_t *tbase = gbase + WIN / 256;                          // per thread: rank of its first column
     uint32_t *tmask = reinterpret_cast<uint32_t *>(tbase + THREADS);  // per thread: its non-empty words
+    int32_t *cur = reinterpret_cast<int32_t *>(tmask + THREADS);      // per staged entry: its B cursor
     const int tid = threadIdx.x, lane = tid & 31;
     for (int i = tid; i < WIN; i += THREADS) bits[i] = 0u;
     // With work items (heavy rows cut into pieces), the items the builder
@@ -1879,7 +1937,8 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
             for (int32_t eb = e0; eb < e1; eb += THREADS) {
                 int nb;
                 const int32_t total =
-                    once ? stage_entries<THREADS, true>(a.A, a.B, eb, e1 - eb, pre, bst, av, &nb, sh, clip, c_lo, c_hi)
+                    once ? stage_entries<THREADS, true>(a.A, a.B, eb, e1 - eb, pre, bst, av, &nb, sh, clip, c_lo, c_hi,
+                                                        cur, c_lo != start)
                          : stage_entries<THREADS, false>(a.A, a.B, eb, min(THREADS, e1 - eb), pre, bst, nullptr, &nb,
                                                          sh, clip, c_lo, c_hi);
                 nb1 = nb;
@@ -1890,7 +1949,7 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
                     pre, bst, nb, tb, te, [&](int32_t pos) { return __ldg(&a.B.idx[pos]); },
                     [&](bool v, int32_t col, int) {
                         const uint32_t rel = v ? (uint32_t)((int64_t)col - c_lo) : 0u;
-                        or_bits_runs(bits, v && rel < nbits, rel);
+                        or_bit(bits, v && rel < nbits, rel);
                     });
                 __syncthreads();
             }
@@ -1924,9 +1983,8 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
             }
             __syncthreads();
             // C's columns, balanced over the threads by output position.
-            write_columns_balanced<THREADS>(bits, tbase, tmask, 32, tot, [&](int32_t p, int w, int b) {
-                if (run + p < expect) __stcs(&a.Ci[obase + run + p], (int32_t)(c_lo + (w << 5) + b - shift));
-            });
+            write_columns_balanced<THREADS>(bits, tbase, tmask, 32, tot, a.Ci + obase + run, expect - run,
+                                            c_lo - shift);
             for (int64_t i = tid; i < tot && run + i < expect; i += THREADS) a.Cv[obase + run + i] = 0.0;
             __syncthreads();
             // Pass 2: the window's products into C's row in place.
@@ -1962,8 +2020,8 @@ __global__ void __launch_bounds__(THREADS) k_num_rankwin(NumArgs a, int32_t lo, 
     }
 }
 
-// Dense rows in one product pass: persistent CTAs (one per SM) take rows
-// from a counter; per window of WIN words of the row's span (2^20 columns)
+// Dense rows in one product pass: persistent CTAs (one per scratch row) take
+// rows from a counter; per window of WIN words of the row's span (2^19 columns)
 // one pass over the row's products sets each product's column bit in a
 // shared bitmap and adds the product into the CTA's FP64 scratch row in
 // global memory, indexed by column (an L2 reduction whose result is not
@@ -2022,7 +2080,7 @@ __global__ void __launch_bounds__(THREADS) k_num_dscr(NumArgs a, int32_t lo, int
                     [&](bool v, const ColVal &x, int e) {
                         const uint32_t rel = v ? (uint32_t)((int64_t)x.c - c_lo) : 0u;
                         const bool in = v && rel < nbits;
-                        or_bits_runs(bits, in, rel);
+                        or_bit(bits, in, rel);
                         if (in) atomicAdd(&scr[rel], __dmul_rn(av[e], x.v));
                     });
                 __syncthreads();
@@ -2270,7 +2328,7 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
                         // inside shared memory all the same
                         const int rel = v ? max(c - c_lo, 0) : 0;
                         if (v) atomic_fma(&dense[rel], av, a.B.val[p]);
-                        or_bits_runs(bits, v, (uint32_t)rel);
+                        or_bit(bits, v, (uint32_t)rel);
                         const int n = __popc(m);
                         cur += n;
                         if (n < 32) {
@@ -2285,7 +2343,7 @@ __global__ void __launch_bounds__(THREADS) k_num_dense(NumArgs a, int32_t lo) {
                         const bool v = c >= c_lo && c < c_hi;
                         const int rel = v ? c - c_lo : 0;
                         if (v) atomic_fma(&dense[rel], av, a.B.val[p]);
-                        or_bits_runs(bits, v, (uint32_t)rel);
+                        or_bit(bits, v, (uint32_t)rel);
                         if (!v && c >= c_hi) nxt = min(nxt, c);
                     }
 #pragma unroll
@@ -2410,10 +2468,10 @@ constexpr int kBitwRows = 8;
 constexpr int kRankwRows = 8;
 constexpr int kDensewRows = 8;
 constexpr int kGdenseThreads = 512;
-constexpr int kRankWinThreads = 1024;  // one CTA per SM: all its warps
-constexpr int kRankWinWords = 32768;  // 2^20 columns per window
+constexpr int kRankWinThreads = 512;  // two CTAs per SM: one works while the other waits at a barrier
+constexpr int kRankWinWords = 16384;  // 2^19 columns per window
 constexpr size_t kSmemRankWin = StageLayout<kRankWinThreads>::bytes + 6 * (size_t)kRankWinWords +
-                                4 * (size_t)(kRankWinWords / 256) + 8 * (size_t)kRankWinThreads;
+                                4 * (size_t)(kRankWinWords / 256) + 12 * (size_t)kRankWinThreads;
 constexpr size_t kSmemGdenseBase = StageLayout<kGdenseThreads>::bytes;
 constexpr size_t kSmemDscr = StageLayout<kRankWinThreads>::bytes + 4 * (size_t)kRankWinWords;
 constexpr int kRankmRows = 5;  // 14.6 KiB per warp: three CTAs (15 warps) per SM
@@ -2428,9 +2486,10 @@ void init_kernel_attributes() {
     cudaFuncSetAttribute(k_sym_hash_cta<kSymCtaThreads, kSymCtaTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemSymCta);
     cudaFuncSetAttribute(k_sym_wide<kWideThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(kSmemWideBase + kWideWindowBitsMax / 8 + 4 * (size_t)kWideTouchMax));
+                         (int)(kSmemWideBase + kWideWindowBitsMax / 8 + 4 * (size_t)kWideTouchMax + 4 * kWideThreads));
     cudaFuncSetAttribute(k_sym_wide<kWideThreadsBig>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(StageLayout<kWideThreadsBig>::bytes + kWideWindowBitsMax / 8 + 4 * (size_t)kWideTouchMax));
+                         (int)(StageLayout<kWideThreadsBig>::bytes + kWideWindowBitsMax / 8 + 4 * (size_t)kWideTouchMax +
+                               4 * kWideThreadsBig));
     cudaFuncSetAttribute(k_num_hash_warp<kNumWarpRows, kNumWarpTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumWarp);
     cudaFuncSetAttribute(k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>,
@@ -2525,11 +2584,12 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
             // Persistent: as many CTAs as fit on the GPU at once (the bitmap
             // and touch list keep one per SM), rows taken from a counter.
             const int wb = wide_window_bits(a.B.n);
-            const size_t smem = kSmemWideBase + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb);
+            const size_t smem = kSmemWideBase + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb) + 4 * kWideThreads;
             if (smem > 110 * 1024) {
                 // Only one CTA fits on an SM: give it all the SM's warps.
                 const size_t smemBig =
-                    StageLayout<kWideThreadsBig>::bytes + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb);
+                    StageLayout<kWideThreadsBig>::bytes + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb) +
+                    4 * kWideThreadsBig;
                 const int gridBig = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1));
                 k_sym_wide<kWideThreadsBig><<<(unsigned)gridBig, kWideThreadsBig, smemBig, s>>>(a, begin, n, wb);
                 break;
