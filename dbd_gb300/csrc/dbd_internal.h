@@ -41,7 +41,7 @@ constexpr int kNumWarpTable = 512, kNumWarpMax = 256;
 constexpr int kNumCtaSTable = 2048, kNumCtaSMax = 1024;
 constexpr int kNumCtaLTable = 8192, kNumCtaLMax = 4096;
 constexpr int kDenseWindow = 8192;           // FP64 columns per dense window (64 KiB)
-constexpr int kWideWindowBitsMax = 1 << 20;  // symbolic bitmap window (128 KiB)
+constexpr int kWideWindowBitsMax = 1 << 19;  // symbolic bitmap window (64 KiB: two CTAs per SM)
 constexpr int kWarpSpanWords = 64;           // warp-level bitmap rows: span <= 2048 columns
 constexpr int kDenseWarpWords = 16;          // warp dense-window rows: span <= 512 columns
 constexpr int kMidSpanWords = 2048;          // warp rank rows over their own window: span <= 2^16 columns

@@ -26,7 +26,7 @@
 //                               ranks for rows within 2^18 columns (values in
 //                               shared memory or reduced into C in place)
 //   wide rows   (symbolic)      persistent CTAs, a shared bitmap over windows
-//                               of up to 2^20 columns that stays zero between
+//                               of up to 2^19 columns that stays zero between
 //                               rows, kept for the numeric rank kernels
 //   dense rows  (numeric)       persistent CTAs, bitmap ranks over 2^19-column
 //                               windows in shared memory, work per window
@@ -2451,8 +2451,7 @@ constexpr int kNumCtaSThreads = 256;
 constexpr int kNumCtaLThreads = 512;
 constexpr int kDenseThreads = 512;
 constexpr int kDenseStage = 1024;  // entries whose cursors stay in shared memory
-constexpr int kWideThreads = 512;       // several CTAs per SM (windows up to 2^18 columns)
-constexpr int kWideThreadsBig = 1024;   // one CTA per SM (a 2^20-column window fills shared memory)
+constexpr int kWideThreads = 512;       // two or more CTAs per SM
 constexpr size_t kSmemSymWarp = (size_t)kSymWarpRows * kSymWarpTable * 4;
 constexpr size_t kSmemSymCta = StageLayout<kSymCtaThreads>::bytes + (size_t)kSymCtaTable * 4;
 constexpr size_t kSmemNumWarp = (size_t)kNumWarpRows * warp_hash_bytes(kNumWarpTable);
@@ -2487,9 +2486,6 @@ void init_kernel_attributes() {
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemSymCta);
     cudaFuncSetAttribute(k_sym_wide<kWideThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(kSmemWideBase + kWideWindowBitsMax / 8 + 4 * (size_t)kWideTouchMax + 4 * kWideThreads));
-    cudaFuncSetAttribute(k_sym_wide<kWideThreadsBig>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(StageLayout<kWideThreadsBig>::bytes + kWideWindowBitsMax / 8 + 4 * (size_t)kWideTouchMax +
-                               4 * kWideThreadsBig));
     cudaFuncSetAttribute(k_num_hash_warp<kNumWarpRows, kNumWarpTable>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemNumWarp);
     cudaFuncSetAttribute(k_num_hash_cta<kNumCtaSThreads, kNumCtaSTable>,
@@ -2524,7 +2520,6 @@ cudaError_t preload_spgemm_kernels() {
         (const void *)k_sym_hash_warp<kSymWarpRows, kSymWarpTable>,
         (const void *)k_sym_hash_cta<kSymCtaThreads, kSymCtaTable>,
         (const void *)k_sym_wide<kWideThreads>,
-        (const void *)k_sym_wide<kWideThreadsBig>,
         (const void *)k_num_tiny,
         (const void *)k_num_hash_warp<kNumWarpRows, kNumWarpTable>,
         (const void *)k_num_densew<kDensewRows>,
@@ -2581,19 +2576,10 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
             k_sym_hash_cta<kSymCtaThreads, kSymCtaTable><<<(unsigned)n, kSymCtaThreads, kSmemSymCta, s>>>(a, begin);
             break;
         case SB_WIDE: {
-            // Persistent: as many CTAs as fit on the GPU at once (the bitmap
-            // and touch list keep one per SM), rows taken from a counter.
+            // Persistent: as many CTAs as fit on the GPU at once (two per SM
+            // with the widest window), rows taken from a counter.
             const int wb = wide_window_bits(a.B.n);
             const size_t smem = kSmemWideBase + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb) + 4 * kWideThreads;
-            if (smem > 110 * 1024) {
-                // Only one CTA fits on an SM: give it all the SM's warps.
-                const size_t smemBig =
-                    StageLayout<kWideThreadsBig>::bytes + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb) +
-                    4 * kWideThreadsBig;
-                const int gridBig = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1));
-                k_sym_wide<kWideThreadsBig><<<(unsigned)gridBig, kWideThreadsBig, smemBig, s>>>(a, begin, n, wb);
-                break;
-            }
             const int per_sm = std::max(1, std::min(2048 / kWideThreads, (int)((227 * 1024) / (smem + 1024))));
             const int grid = (int)std::min<int64_t>(n, (int64_t)std::max(a.numSms, 1) * per_sm);
             k_sym_wide<kWideThreads><<<(unsigned)grid, kWideThreads, smem, s>>>(a, begin, n, wb);
