@@ -798,18 +798,26 @@ def run_outofcore(args, local, rank=0, world=1):
     # +D2H: host A, C through the pinned ring, each step a full multiply, on
     # a context of its own, as a caller that copies C out would hold (the
     # kernel-scope context's one large device slot is released first).
+    # C in the reference's output layout (float32 values rounded once on the
+    # device after FP64 accumulation: 8 bytes per entry over the link), and
+    # once more with FP64 values (12 bytes per entry) for comparison.
     ctx_tuning = ctx.tuning
     ctx.close()
-    ctx = dbd.Context(cpu_gib=64, gpu_gib=24, rows_per_block=512, device=local, io_rotate_gib=rotate)
-    ctx.set_tuning(**ctx_tuning)
-    td = []
-    for i in range(max(1, args.e2e_steps) + 1):
-        a = time.perf_counter()
-        r = ctx.spgemm(A, scope="d2h", fetch=False)
-        if i:
-            td.append(time.perf_counter() - a)
-    t_d2h = float(np.mean(td))
-    d2h_stats = r.stats
+
+    def d2h_run(fp32, steps):
+        c = dbd.Context(cpu_gib=64, gpu_gib=24, rows_per_block=512, device=local, io_rotate_gib=rotate,
+                        out_val_fp32=fp32)
+        c.set_tuning(**ctx_tuning)
+        ts = []
+        for i in range(steps + 1):
+            a = time.perf_counter()
+            r = c.spgemm(A, scope="d2h", fetch=False)
+            if i:
+                ts.append(time.perf_counter() - a)
+        return c, float(np.mean(ts)), r.stats
+    ctx, t_d2h64, d2h64_stats = d2h_run(False, 1)
+    ctx.close()
+    ctx, t_d2h, d2h_stats = d2h_run(True, max(1, args.e2e_steps))
     link = link_peak(torch, dev)
     # +I/O: one run through the O_DIRECT writer into a wrapping file set.
     tmp = tempfile.mkdtemp(prefix="dbd_io_", dir=ROOT)
@@ -822,12 +830,13 @@ def run_outofcore(args, local, rank=0, world=1):
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
     ctx.close()
-    d2h_gbs = c_bytes / t_d2h / 1e9
+    c_bytes32 = int(d2h_stats["bytes_d2h"])
+    d2h_gbs = c_bytes32 / t_d2h / 1e9
     io_gbs = io_stats["bytes_written"] / t_io / 1e9
     roof["d2h_frac"] = round(d2h_gbs / link["d2h"], 4)
     roof["io_frac"] = round(io_gbs / disk, 4)
     roof["d2h"] = {"achieved": round(d2h_gbs, 2), "peak": link["d2h"], "unit": "GB/s",
-                   "frac": roof["d2h_frac"], "bytes": c_bytes,
+                   "frac": roof["d2h_frac"], "bytes": c_bytes32,
                    "peak_kind": "measured in this run: pinned 4 GiB cudaMemcpyAsync D2H, best of 5",
                    "what": "C's bytes over the +D2H scope's whole time (compute overlapped)"}
     roof["io"] = {"achieved": round(io_gbs, 3), "peak": disk, "unit": "GB/s", "frac": roof["io_frac"],
@@ -853,12 +862,19 @@ def run_outofcore(args, local, rank=0, world=1):
             "roofline": roof,
             "scopes": {"kernel_gflops": g(t_kernel), "kernel_s": round(t_kernel, 4),
                        "d2h_gflops": g(t_d2h), "d2h_s": round(t_d2h, 3), "d2h_bytes": int(d2h_stats["bytes_d2h"]),
+                       "d2h_device_ms": round(d2h_stats["t_device_ms"], 1),
+                       "d2h_chunks_ms": round(d2h_stats["t_chunks_ms"], 1), "d2h_copy_ms": round(d2h_stats["t_copy_ms"], 1),
+                       "d2h_fp64_gflops": g(t_d2h64), "d2h_fp64_s": round(t_d2h64, 3),
+                       "d2h_fp64_bytes": int(d2h64_stats["bytes_d2h"]),
+                       "d2h_fp64_copy_ms": round(d2h64_stats["t_copy_ms"], 1),
                        "io_gflops": g(t_io), "io_s": round(t_io, 3), "io_bytes": int(io_stats["bytes_written"]),
                        "io_fsync_s": round(io_stats["t_fsync"], 3), "io_direct": bool(io_stats["io_direct"]),
                        "link_gbs": link, "disk_write_gbs": disk},
             "e2e": {"value": g(t_d2h), "unit": "GFLOPS", "h2d_bytes_per_step": 12 * A.nnz + 4 * (A.n_rows + 1),
                     "d2h_bytes_per_step": int(d2h_stats["bytes_d2h"]), "ms_per_step": round(t_d2h * 1e3, 2),
-                    "scope": "+D2H through dbd_spgemm with host (pageable) A; all of C through the pinned host ring"},
+                    "scope": "+D2H through dbd_spgemm with host (pageable) A; all of C through the pinned host ring "
+                             "in the reference's layout (float32 values rounded once on the device after FP64 "
+                             "accumulation, int32 columns, int64 row pointers)"},
             "clocks": clk.summary()}
     if world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -1089,27 +1105,39 @@ def main():
     line["clocks"] = clk.summary()
 
     if rank == 0 or world == 1:
-        # e2e: the public API with host buffers (H2D of A, D2H of all of C).
+        # e2e: the public API with host buffers (H2D of A, D2H of all of C),
+        # C in the reference's output layout (float32 values rounded on the
+        # device after FP64 accumulation, int32 columns, int64 row pointers);
+        # the same with FP64 values is reported beside it.
+        def d2h_time(c, steps):
+            c.spgemm(A, scope="d2h", fetch=False)
+            ts = []
+            for _ in range(steps):
+                t0 = time.perf_counter()
+                r = c.spgemm(A, scope="d2h", fetch=False)
+                ts.append(time.perf_counter() - t0)
+            return float(np.mean(ts)), r.stats
         ctx.set_stream(None)
-        res = ctx.spgemm(A, scope="d2h", fetch=False)
-        e2e_t = []
-        for _ in range(args.e2e_steps):
-            t0 = time.perf_counter()
-            res = ctx.spgemm(A, scope="d2h", fetch=False)
-            e2e_t.append(time.perf_counter() - t0)
-        te = float(np.mean(e2e_t))
+        te64, st64 = d2h_time(ctx, max(1, args.e2e_steps))
+        ctx32 = dbd.Context(cpu_gib=96, gpu_gib=args.gpu_gib, rows_per_block=rpb, device=local,
+                            out_val_fp32=True)
+        ctx32.set_tuning(**ctx.tuning)
+        te, st32 = d2h_time(ctx32, max(1, args.e2e_steps))
         h2d = 4 * (A.n_rows + 1) + 12 * A.nnz
-        d2h = 12 * nnzC + 8 * (A.n_rows + 1)
+        d2h = int(st32["bytes_d2h"])
         line["e2e"] = {"value": round(world * 2.0 * P / te / 1e9, 4), "unit": "GFLOPS", "h2d_bytes_per_step": h2d,
                        "d2h_bytes_per_step": d2h, "ms_per_step": round(te * 1e3, 3),
-                       "scope": "+D2H through dbd_spgemm with host (pageable) A and pinned host C"}
-        scopes = {"kernel_gflops": round(2.0 * P / t_step / 1e9, 4), "d2h_gflops": round(2.0 * P / te / 1e9, 4)}
+                       "scope": "+D2H through dbd_spgemm with host (pageable) A and pinned host C in the reference's "
+                                "layout (float32 values rounded once on the device after FP64 accumulation)"}
+        scopes = {"kernel_gflops": round(2.0 * P / t_step / 1e9, 4), "d2h_gflops": round(2.0 * P / te / 1e9, 4),
+                  "d2h_fp64_gflops": round(2.0 * P / te64 / 1e9, 4), "d2h_fp64_ms": round(te64 * 1e3, 3),
+                  "d2h_fp64_bytes": int(st64["bytes_d2h"])}
         if not args.no_io:
             tmp = tempfile.mkdtemp(prefix="dbd_io_", dir=ROOT)
             try:
-                ctx.spgemm(A, scope="io", out_dir=tmp, fetch=False)
+                ctx32.spgemm(A, scope="io", out_dir=tmp, fetch=False)
                 t0 = time.perf_counter()
-                r = ctx.spgemm(A, scope="io", out_dir=tmp, fetch=False)
+                r = ctx32.spgemm(A, scope="io", out_dir=tmp, fetch=False)
                 tio = time.perf_counter() - t0
                 scopes["io_gflops"] = round(2.0 * P / tio / 1e9, 4)
                 scopes["io_s"] = round(tio, 3)
@@ -1117,6 +1145,7 @@ def main():
                 scopes["io_bytes"] = int(r.stats["bytes_written"])
             finally:
                 shutil.rmtree(tmp, ignore_errors=True)
+        ctx32.close()
         line["scopes"] = scopes
         if world == 1 and not args.no_cpu_baseline:
             threads = os.cpu_count() or 1

@@ -251,8 +251,15 @@ class Context:
         _check(self._lib.dbd_result(self._h, C.byref(o)), self._h)
         ptr = np.empty(o.n_rows + 1, np.int64)
         idx = np.empty(o.nnz, np.int32)
-        val = np.empty(o.nnz, np.float64)
-        _check(self._lib.dbd_result_copy(self._h, ptr.ctypes.data, idx.ctypes.data, val.ctypes.data), self._h)
+        if o.val_fp32:
+            # float32 values (out_val_fp32 in a copying scope), in host memory
+            val = np.empty(o.nnz, np.float32)
+            if o.nnz:
+                C.memmove(val.ctypes.data, o.val, 4 * o.nnz)
+            _check(self._lib.dbd_result_copy(self._h, ptr.ctypes.data, idx.ctypes.data, None), self._h)
+        else:
+            val = np.empty(o.nnz, np.float64)
+            _check(self._lib.dbd_result_copy(self._h, ptr.ctypes.data, idx.ctypes.data, val.ctypes.data), self._h)
         return CSR(o.n_rows, o.n_cols, ptr, idx, val)
 
     # ---- one-shot ----

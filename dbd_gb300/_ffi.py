@@ -28,7 +28,7 @@ class CsrView(C.Structure):
 class CsrOut(C.Structure):
     _fields_ = [("n_rows", C.c_int64), ("n_cols", C.c_int64), ("nnz", C.c_int64),
                 ("row_ptr", C.c_void_p), ("col_idx", C.c_void_p), ("val", C.c_void_p),
-                ("on_device", C.c_int32), ("owner", C.c_int32)]
+                ("on_device", C.c_int32), ("owner", C.c_int32), ("val_fp32", C.c_int32)]
 
 
 class CsrHost(C.Structure):
@@ -65,7 +65,7 @@ class Stats(C.Structure):
                 ("bytes_written", C.c_int64), ("gpu_launches", C.c_int64), ("t_analysis_ms", C.c_double),
                 ("t_sym_bin_ms", C.c_double * NUM_BINS), ("t_scan_ms", C.c_double),
                 ("t_num_bin_ms", C.c_double * NUM_BINS), ("io_direct", C.c_int64), ("resumed_from_row", C.c_int64),
-                ("heavy_rows", C.c_int64)]
+                ("heavy_rows", C.c_int64), ("t_chunks_ms", C.c_double), ("t_copy_ms", C.c_double)]
 
     def as_dict(self):
         d = {}

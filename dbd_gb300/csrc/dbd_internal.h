@@ -305,9 +305,14 @@ struct RowDigest {
     double *wsum = nullptr;
     int64_t *bad = nullptr;
 };
-// Digest of rows [r0, r1) whose entries sit at Cp[r] - outBase in Ci / Cv.
+// Digest of rows [r0, r1) whose entries sit at Cp[r] - outBase in Ci / Cv
+// (FP64 values, or the float32 values of the reference's output layout).
 void launch_row_digest(int64_t r0, int64_t r1, const int64_t *Cp, int64_t outBase, const int32_t *Ci,
                        const double *Cv, int64_t ncols, const RowDigest &d, cudaStream_t s, int num_sms);
+void launch_row_digest(int64_t r0, int64_t r1, const int64_t *Cp, int64_t outBase, const int32_t *Ci,
+                       const float *Cv, int64_t ncols, const RowDigest &d, cudaStream_t s, int num_sms);
+// dst[i] = src[i] rounded to float32, i < n.
+void launch_val_to_f32(const double *src, float *dst, int64_t n, cudaStream_t s, int num_sms);
 
 // *acc += sum over i < n of mix64(((uint64)i << 32 | w[i]) ^ (salt * G)) (an
 // order-dependent hash of a device array of 32-bit words).

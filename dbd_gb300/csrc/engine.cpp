@@ -135,6 +135,7 @@ struct dbd_ctx {
     DevBuf rowP, symBin, numBin, rowNnz, symList, numList, hist, symTileOff, numTileOff, symStart,
         numStart, part, Cp, cursor, err, blockP, flags;
     DevBuf Ci, Cv;           // resident product or device output ring
+    DevBuf Cf;               // float32 values of each device slot (out_val_fp32 in the copying scopes)
     DevBuf ctrs;             // row counters of the persistent kernels
     DevBuf gdense;           // global dense slots of the dense bin
     int gSlots = 0;
@@ -192,6 +193,7 @@ struct dbd_ctx {
     // host result / ring
     HostBuf hCp, hCi, hCv;
     bool host_full = false;  // hCp/hCi/hCv hold the complete product
+    bool host_f32 = false;   // hCv holds float32 values (out_val_fp32 in the copying scopes)
     bool dev_resident = false;
     dbd_scope last_scope = DBD_SCOPE_KERNEL;
 
@@ -719,8 +721,9 @@ void neumaier_add(double &s, double &c, double x) {
 
 // Digest of rows [r0, r1) of a host copy whose entries sit at Cp[r] - base,
 // split over host threads by entries.
+template <class V>
 void host_digest_rows(dbd_ctx *c, const int64_t *Cp, int64_t r0, int64_t r1, int64_t base, const int32_t *ci,
-                      const double *cv) {
+                      const V *cv) {
     const int64_t ncols = c->ncols;
     auto run = [&](int64_t a, int64_t b) {
         int64_t bad = 0;
@@ -731,7 +734,7 @@ void host_digest_rows(dbd_ctx *c, const int64_t *Cp, int64_t r0, int64_t r1, int
             bool rbad = false;
             for (int64_t i = e0; i < e1; ++i) {
                 const int32_t col = ci[i];
-                const double v = cv[i];
+                const double v = (double)cv[i];
                 if (col < 0 || (int64_t)col >= ncols || (i > e0 && ci[i - 1] >= col)) rbad = true;
                 uint64_t bits;
                 memcpy(&bits, &v, sizeof(bits));
@@ -848,11 +851,19 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
                                  (c->gSlots ? c->gdense.cap : 0) + (c->scrSlots ? c->dscr.cap : 0) +
                                  c->wideBits.cap + c->heavySlot.cap + c->slabCnt.cap + c->items.cap);
     const double dev_avail = std::min(gpu_budget - used, (double)free_b - 512.0 * 1024 * 1024);
+    const bool copies = scope != DBD_SCOPE_KERNEL;
+    // The reference's output layout (float32 values): the copying scopes
+    // round each chunk's FP64 values once on the device, so 8 bytes per
+    // entry cross the link instead of 12.  Device slots then hold 16 bytes
+    // per entry (FP64 accumulators + their float32 copy).
+    const bool f32out = copies && c->cfg.out_val_fp32 != 0;
+    const double dev_bpe = f32out ? 16.0 : 12.0;
+    const double host_bpe = f32out ? 8.0 : 12.0;
+    const size_t hve = f32out ? sizeof(float) : sizeof(double);  // host bytes per value
     const double out_bytes = 12.0 * (double)nnz;
     const bool resident = out_bytes <= std::max(0.0, dev_avail) && scope == DBD_SCOPE_KERNEL;
-    const bool host_fits = out_bytes + 8.0 * (double)(m + 1) <= host_budget;
+    const bool host_fits = host_bpe * (double)nnz + 8.0 * (double)(m + 1) <= host_budget;
 
-    const bool copies = scope != DBD_SCOPE_KERNEL;
     int64_t bytes_d2h = 0;
     // The copying scopes bring all of C's row pointers to the host first:
     // Ptr.output, the host digest and a resumed run's start need them.
@@ -874,6 +885,7 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         WriterOpts wo;
         wo.direct = c->cfg.io_buffered == 0;
         wo.val_fp32 = c->cfg.out_val_fp32 != 0;
+        wo.src_fp32 = f32out;
         wo.ptr32 = c->cfg.out_ptr32 == 1 || (c->cfg.out_ptr32 == 2 && nnz <= INT32_MAX);
         wo.rotate_bytes = c->cfg.io_rotate_gib > 0 ? (int64_t)(c->cfg.io_rotate_gib * kGiB) : 0;
         wo.resume = c->cfg.io_resume != 0;
@@ -898,21 +910,23 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     // a small share of a launch's work.  The kernel scope copies nothing
     // out: one slot takes the whole remaining budget.  The copying scopes
     // keep two device slots (a chunk computes while the previous one is
-    // copied) and two host ring slots, each a sixth of C clamped to
-    // [1, 6] GiB (and within both budgets): at least six chunks overlap
-    // their copies with compute when C is small, and a large C keeps its
-    // chunks large (slots of 11.5 GiB copied slower than 6 GiB ones).
+    // copied) and two host ring slots, each a sixth of C's host bytes
+    // clamped to [1, 6] GiB (and within both budgets): at least six chunks
+    // overlap their copies with compute when C is small, and a large C
+    // keeps its chunks large (slots of 11.5 GiB copied slower than 6 GiB
+    // ones).
     const int nslots_dev = copies ? 2 : 1;
     if (resident) {
         Chunk ch{0, m, 0, nnz};
         chunks.push_back(ch);
     } else {
-        double slot_bytes = std::max(0.0, dev_avail) / nslots_dev;
+        double slot_entries_f = std::max(0.0, dev_avail) / nslots_dev / dev_bpe;
         if (copies) {
-            slot_bytes = std::min(slot_bytes, std::min(6.0 * kGiB, std::max(1.0 * kGiB, 12.0 * (double)nnz / 6.0)));
-            if (!(scope == DBD_SCOPE_D2H && host_fits)) slot_bytes = std::min(slot_bytes, host_budget / 2.0);
+            double host_slot = std::min(6.0 * kGiB, std::max(1.0 * kGiB, host_bpe * (double)nnz / 6.0));
+            if (!(scope == DBD_SCOPE_D2H && host_fits)) host_slot = std::min(host_slot, host_budget / 2.0);
+            slot_entries_f = std::min(slot_entries_f, host_slot / host_bpe);
         }
-        cap_entries = std::max<int64_t>((int64_t)(slot_bytes / 12.0), 1);
+        cap_entries = std::max<int64_t>((int64_t)slot_entries_f, 1);
         std::vector<int64_t> cpBlk((size_t)c->nblocks + 1);
         // Cp at block boundaries (from the host copy, or a strided copy of
         // one int64 per block).
@@ -929,7 +943,7 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         int64_t maxblk = 0;
         for (int64_t b = b0; b < c->nblocks; ++b) maxblk = std::max(maxblk, cpBlk[(size_t)b + 1] - cpBlk[(size_t)b]);
         if (maxblk > cap_entries) {
-            if ((double)maxblk * 12.0 * nslots_dev > std::max(0.0, dev_avail))
+            if ((double)maxblk * dev_bpe * nslots_dev > std::max(0.0, dev_avail))
                 return set_err(c, DBD_ERR_BUDGET, "a row block's output does not fit the GPU budget");
             cap_entries = maxblk;
         }
@@ -941,7 +955,9 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     const size_t slot_entries = resident ? (size_t)std::max<int64_t>(nnz, 1) : (size_t)cap_entries;
     CK(c, c->Ci.ensure(sizeof(int32_t) * slot_entries * nslots));
     CK(c, c->Cv.ensure(sizeof(double) * slot_entries * nslots));
+    if (f32out) CK(c, c->Cf.ensure(sizeof(float) * slot_entries * nslots));
     c->dev_resident = resident;
+    c->host_f32 = f32out;
 
     // Host side of D2H / IO.
     c->host_full = false;
@@ -949,10 +965,10 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
     // Ring slots leave 4 KiB of lead room on both sides of a chunk, so that
     // an O_DIRECT writer finds every chunk at its file offset modulo 4 KiB.
     const size_t si = (size_t)writer_slot_bytes((int64_t)slot_entries, 4);
-    const size_t sv = (size_t)writer_slot_bytes((int64_t)slot_entries, 8);
+    const size_t sv = (size_t)writer_slot_bytes((int64_t)slot_entries, (int64_t)hve);
     if (scope == DBD_SCOPE_D2H && host_fits) {
         CK(c, c->hCi.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(nnz, 1)));
-        CK(c, c->hCv.ensure(sizeof(double) * (size_t)std::max<int64_t>(nnz, 1)));
+        CK(c, c->hCv.ensure(hve * (size_t)std::max<int64_t>(nnz, 1)));
         c->host_full = true;
     } else if (scope != DBD_SCOPE_KERNEL) {
         nhslots = 2;
@@ -1021,10 +1037,15 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
                 }
                 char *ib = c->hCi.as<char>() + (size_t)j.slot * si;
                 char *vb = c->hCv.as<char>() + (size_t)j.slot * sv;
-                if (!werr && host_dg)
-                    host_digest_rows(c, c->hCp.as<int64_t>(), j.r0, j.r1, j.c0,
-                                     reinterpret_cast<const int32_t *>(ib + j.lead_i),
-                                     reinterpret_cast<const double *>(vb + j.lead_v));
+                if (!werr && host_dg) {
+                    const int32_t *ci = reinterpret_cast<const int32_t *>(ib + j.lead_i);
+                    if (f32out)
+                        host_digest_rows(c, c->hCp.as<int64_t>(), j.r0, j.r1, j.c0, ci,
+                                         reinterpret_cast<const float *>(vb + j.lead_v));
+                    else
+                        host_digest_rows(c, c->hCp.as<int64_t>(), j.r0, j.r1, j.c0, ci,
+                                         reinterpret_cast<const double *>(vb + j.lead_v));
+                }
                 if (!werr && wr) {
                     std::string err;
                     int e = writer_append(wr, ib, vb, j.n, j.r1, &err);
@@ -1042,11 +1063,16 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         });
     }
 
-    // Events per chunk for the two-stream pipeline.
-    std::vector<cudaEvent_t> evNum(chunks.size()), evCopy(chunks.size());
+    // Events per chunk for the two-stream pipeline: the start and end of
+    // each chunk's numeric work and of its copy (the ends also order the
+    // streams).
+    std::vector<cudaEvent_t> evNum(chunks.size()), evCopy(chunks.size()), evNum0(chunks.size()),
+        evCopy0(chunks.size());
     for (size_t i = 0; i < chunks.size(); ++i) {
-        cudaEventCreateWithFlags(&evNum[i], cudaEventDisableTiming);
-        cudaEventCreateWithFlags(&evCopy[i], cudaEventDisableTiming);
+        cudaEventCreate(&evNum[i]);
+        cudaEventCreate(&evCopy[i]);
+        cudaEventCreate(&evNum0[i]);
+        cudaEventCreate(&evCopy0[i]);
     }
     double t_d2h_issue = 0.0;
     CK(c, cudaEventRecord(c->evNumA, c->stream));
@@ -1059,23 +1085,34 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         // The device slot is free once its previous chunk's copy finished.
         if (!resident && i >= (size_t)nslots && scope != DBD_SCOPE_KERNEL)
             cudaStreamWaitEvent(c->stream, evCopy[i - nslots], 0);
+        cudaEventRecord(evNum0[i], c->stream);
         numeric_rows(c, ch.r0, ch.r1, ch.c0, dCi, dCv);
+        float *dCf = f32out ? c->Cf.as<float>() + (size_t)ds * slot_entries : nullptr;
+        if (f32out && ch.c1 > ch.c0) {
+            launch_val_to_f32(dCv, dCf, ch.c1 - ch.c0, c->stream, c->num_sms);
+            c->launches++;
+        }
         if (dev_dg) {
-            launch_row_digest(ch.r0, ch.r1, c->Cp.as<int64_t>(), ch.c0, dCi, dCv, c->ncols, rd, c->stream,
-                              c->num_sms);
+            // The digest describes the values as they leave the device.
+            if (f32out)
+                launch_row_digest(ch.r0, ch.r1, c->Cp.as<int64_t>(), ch.c0, dCi, dCf, c->ncols, rd, c->stream,
+                                  c->num_sms);
+            else
+                launch_row_digest(ch.r0, ch.r1, c->Cp.as<int64_t>(), ch.c0, dCi, dCv, c->ncols, rd, c->stream,
+                                  c->num_sms);
             c->launches++;
         }
         cudaEventRecord(evNum[i], c->stream);
         if (scope == DBD_SCOPE_KERNEL) continue;
         const int64_t n = ch.c1 - ch.c0;
         int32_t *hCi;
-        double *hCv;
+        char *hCv;  // doubles, or floats with f32out
         int hs = 0;
         const int64_t lead_i = wr ? writer_lead_for(wr, ch.c0, 0) : 0;
         const int64_t lead_v = wr ? writer_lead_for(wr, ch.c0, 1) : 0;
         if (c->host_full) {
             hCi = c->hCi.as<int32_t>() + ch.c0;
-            hCv = c->hCv.as<double>() + ch.c0;
+            hCv = c->hCv.as<char>() + hve * (size_t)ch.c0;
         } else {
             hs = (int)(i % nhslots);
             if (consume) {
@@ -1087,19 +1124,22 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
                 // reference's bin/d2h reuses one pinned buffer (preProc.cu:94-95).
             }
             hCi = reinterpret_cast<int32_t *>(c->hCi.as<char>() + (size_t)hs * si + lead_i);
-            hCv = reinterpret_cast<double *>(c->hCv.as<char>() + (size_t)hs * sv + lead_v);
+            hCv = c->hCv.as<char>() + (size_t)hs * sv + lead_v;
         }
         const auto ti = Clock::now();
         cudaStreamWaitEvent(c->copy_stream, evNum[i], 0);
+        cudaEventRecord(evCopy0[i], c->copy_stream);
         if (n > 0) {
             cudaError_t e1 = cudaMemcpyAsync(hCi, dCi, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost,
                                              c->copy_stream);
-            cudaError_t e2 = cudaMemcpyAsync(hCv, dCv, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost,
-                                             c->copy_stream);
+            cudaError_t e2 = f32out ? cudaMemcpyAsync(hCv, dCf, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost,
+                                                      c->copy_stream)
+                                    : cudaMemcpyAsync(hCv, dCv, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost,
+                                                      c->copy_stream);
             if (e1 != cudaSuccess || e2 != cudaSuccess) loop_rc = cuda_fail(c, e1 != cudaSuccess ? e1 : e2, "D2H");
         }
         cudaEventRecord(evCopy[i], c->copy_stream);
-        bytes_d2h += 12 * n;
+        bytes_d2h += (int64_t)(4 + hve) * n;
         t_d2h_issue += seconds_since(ti);
         if (consume) {
             {
@@ -1120,15 +1160,27 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         cv.notify_all();
         th.join();
     }
+    double chunks_ms = 0.0, copy_ms = 0.0;
     for (size_t i = 0; i < chunks.size(); ++i) {
+        float x = 0.f;
+        if (!se && cudaEventElapsedTime(&x, evNum0[i], evNum[i]) == cudaSuccess) chunks_ms += x;
+        if (!se && !ce && scope != DBD_SCOPE_KERNEL && cudaEventElapsedTime(&x, evCopy0[i], evCopy[i]) == cudaSuccess)
+            copy_ms += x;
         cudaEventDestroy(evNum[i]);
         cudaEventDestroy(evCopy[i]);
+        cudaEventDestroy(evNum0[i]);
+        cudaEventDestroy(evCopy0[i]);
     }
+    cudaGetLastError();  // events of chunks that a failed loop left unrecorded
+    c->stats.t_chunks_ms = chunks_ms;
+    c->stats.t_copy_ms = copy_ms;
     if (loop_rc) return loop_rc;
     if (se != cudaSuccess) return cuda_fail(c, se, "compute stream");
     if (ce != cudaSuccess) return cuda_fail(c, ce, "copy stream");
-    if (host_dg && c->host_full && m > 0)
-        host_digest_rows(c, c->hCp.as<int64_t>(), 0, m, 0, c->hCi.as<int32_t>(), c->hCv.as<double>());
+    if (host_dg && c->host_full && m > 0) {
+        if (f32out) host_digest_rows(c, c->hCp.as<int64_t>(), 0, m, 0, c->hCi.as<int32_t>(), c->hCv.as<float>());
+        else host_digest_rows(c, c->hCp.as<int64_t>(), 0, m, 0, c->hCi.as<int32_t>(), c->hCv.as<double>());
+    }
     c->dgDevOk = dev_dg;
     c->dgHostOk = host_dg && !werr;
     rc = check_device_err(c, "numeric");
@@ -1365,7 +1417,8 @@ int dbd_result(dbd_ctx *c, dbd_csr_out *o) {
     if (!c->host_full) return set_err(c, DBD_ERR_BUDGET, "the product did not fit the host budget");
     o->row_ptr = c->hCp.as<int64_t>();
     o->col_idx = c->hCi.as<int32_t>();
-    o->val = c->hCv.as<double>();
+    o->val = c->hCv.p;
+    o->val_fp32 = c->host_f32 ? 1 : 0;
     o->owner = 2;
     return DBD_OK;
 }
@@ -1386,7 +1439,17 @@ int dbd_result_copy(dbd_ctx *c, int64_t *row_ptr, int32_t *col_idx, double *val)
     if (row_ptr) CK(c, cudaMemcpy(row_ptr, o.row_ptr, sizeof(int64_t) * (size_t)(o.n_rows + 1), k));
     if (o.nnz > 0) {
         if (col_idx) CK(c, cudaMemcpy(col_idx, o.col_idx, sizeof(int32_t) * (size_t)o.nnz, k));
-        if (val) CK(c, cudaMemcpy(val, o.val, sizeof(double) * (size_t)o.nnz, k));
+        if (val && o.val_fp32) {
+            cudaPointerAttributes pa;
+            if (cudaPointerGetAttributes(&pa, val) != cudaSuccess || pa.type == cudaMemoryTypeDevice) {
+                cudaGetLastError();
+                return set_err(c, DBD_ERR_INVALID, "float32 values widen into host memory only");
+            }
+            const float *f = static_cast<const float *>(o.val);
+            for (int64_t i = 0; i < o.nnz; ++i) val[i] = (double)f[i];
+        } else if (val) {
+            CK(c, cudaMemcpy(val, o.val, sizeof(double) * (size_t)o.nnz, k));
+        }
     }
     return DBD_OK;
 }

@@ -58,11 +58,13 @@ __device__ __forceinline__ void two_sum_merge(double &s, double &c, double s2, d
     c = c + c2 + e;
 }
 
-// One warp per row of [r0, r1), persistent over the rows.
+// One warp per row of [r0, r1), persistent over the rows.  V is the type the
+// values leave the device in (FP64, or float32 for the reference's layout);
+// either is hashed and summed as the FP64 number it holds.
+template <class V>
 __global__ void __launch_bounds__(256) k_row_digest(int64_t r0, int64_t r1, const int64_t *__restrict__ Cp,
                                                     int64_t outBase, const int32_t *__restrict__ Ci,
-                                                    const double *__restrict__ Cv, int64_t ncols,
-                                                    RowDigest d) {
+                                                    const V *__restrict__ Cv, int64_t ncols, RowDigest d) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -73,7 +75,7 @@ __global__ void __launch_bounds__(256) k_row_digest(int64_t r0, int64_t r1, cons
         int bad = 0;
         for (int64_t i = b + lane; i < e; i += 32) {
             const int32_t col = __ldcs(Ci + i);
-            const double v = __ldcs(Cv + i);
+            const double v = (double)__ldcs(Cv + i);
             if (col < 0 || (int64_t)col >= ncols) bad = 1;
             if (i > b && __ldg(Ci + i - 1) >= col) bad = 1;
             const uint64_t mc = mix64((uint64_t)(uint32_t)col);
@@ -102,6 +104,14 @@ __global__ void __launch_bounds__(256) k_row_digest(int64_t r0, int64_t r1, cons
     }
 }
 
+// C's values rounded once to float32 (the reference's output type), after
+// the FP64 accumulation: dst[i] = src[i] to nearest.
+__global__ void __launch_bounds__(256) k_val_to_f32(const double *__restrict__ src, float *__restrict__ dst,
+                                                    int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        __stcs(dst + i, __double2float_rn(__ldcs(src + i)));
+}
+
 __global__ void __launch_bounds__(256) k_hash_words(const uint32_t *__restrict__ w, int64_t n, uint64_t salt,
                                                     uint64_t *acc) {
     uint64_t h = 0;
@@ -120,12 +130,29 @@ void launch_hash_words(const uint32_t *w, int64_t n, uint64_t salt, uint64_t *ac
     k_hash_words<<<(unsigned)blocks, 256, 0, s>>>(w, n, salt, acc);
 }
 
-void launch_row_digest(int64_t r0, int64_t r1, const int64_t *Cp, int64_t outBase, const int32_t *Ci,
-                       const double *Cv, int64_t ncols, const RowDigest &d, cudaStream_t s, int num_sms) {
+template <class V>
+static void row_digest(int64_t r0, int64_t r1, const int64_t *Cp, int64_t outBase, const int32_t *Ci, const V *Cv,
+                       int64_t ncols, const RowDigest &d, cudaStream_t s, int num_sms) {
     if (r1 <= r0) return;
     const int64_t warps = r1 - r0;
     const int64_t blocks = std::min<int64_t>((warps + 7) / 8, (int64_t)num_sms * 8);
-    k_row_digest<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(r0, r1, Cp, outBase, Ci, Cv, ncols, d);
+    k_row_digest<V><<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, s>>>(r0, r1, Cp, outBase, Ci, Cv, ncols, d);
+}
+
+void launch_row_digest(int64_t r0, int64_t r1, const int64_t *Cp, int64_t outBase, const int32_t *Ci,
+                       const double *Cv, int64_t ncols, const RowDigest &d, cudaStream_t s, int num_sms) {
+    row_digest(r0, r1, Cp, outBase, Ci, Cv, ncols, d, s, num_sms);
+}
+
+void launch_row_digest(int64_t r0, int64_t r1, const int64_t *Cp, int64_t outBase, const int32_t *Ci,
+                       const float *Cv, int64_t ncols, const RowDigest &d, cudaStream_t s, int num_sms) {
+    row_digest(r0, r1, Cp, outBase, Ci, Cv, ncols, d, s, num_sms);
+}
+
+void launch_val_to_f32(const double *src, float *dst, int64_t n, cudaStream_t s, int num_sms) {
+    if (n <= 0) return;
+    const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)num_sms * 8);
+    k_val_to_f32<<<(unsigned)blocks, 256, 0, s>>>(src, dst, n);
 }
 
 }  // namespace dbd

@@ -315,20 +315,25 @@ int writer_open(const std::string &dir, const WriterOpts &o, ChunkWriter **out, 
 
 int64_t writer_idx_lead(const ChunkWriter *w) { return w->direct ? w->idx.off % kIoAlign : 0; }
 
+// Values are written straight from the caller's buffer when they arrive in
+// the file's type (FP64, or float32 from a float32 source); FP64 values for
+// a float32 file go through the writer's own staging instead (lead 0).
+static bool val_direct(const ChunkWriter *w) { return !w->o.val_fp32 || w->o.src_fp32; }
+
 int64_t writer_val_lead(const ChunkWriter *w) {
-    return (w->direct && !w->o.val_fp32) ? w->val.off % kIoAlign : 0;
+    return (w->direct && val_direct(w)) ? w->val.off % kIoAlign : 0;
 }
 
 int64_t writer_lead_for(const ChunkWriter *w, int64_t entry, int val) {
-    if (!w->direct || (val && w->o.val_fp32)) return 0;
-    return (entry * (val ? 8 : 4)) % kIoAlign;
+    if (!w->direct || (val && !val_direct(w))) return 0;
+    return (entry * (val ? w->val_elem() : 4)) % kIoAlign;
 }
 
 int writer_append(ChunkWriter *w, char *idx_base, char *val_base, int64_t n, int64_t row_end, std::string *err) {
     const auto t0 = Clock::now();
     int rc = w->put(w->idx, idx_base, writer_idx_lead(w), 4 * n, err);
     if (!rc) {
-        if (w->o.val_fp32) {
+        if (w->o.val_fp32 && !w->o.src_fp32) {
             // Convert into aligned staging laid out at the file offset modulo 4 KiB.
             const int64_t lead = w->direct ? w->val.off % kIoAlign : 0;
             const int64_t need = lead + 4 * n + kIoAlign;
@@ -345,7 +350,7 @@ int writer_append(ChunkWriter *w, char *idx_base, char *val_base, int64_t n, int
                 rc = w->put(w->val, w->f32, lead, 4 * n, err);
             }
         } else {
-            rc = w->put(w->val, val_base, writer_val_lead(w), 8 * n, err);
+            rc = w->put(w->val, val_base, writer_val_lead(w), w->val_elem() * n, err);
         }
     }
     if (!rc && w->o.resume) rc = w->checkpoint(row_end, err);

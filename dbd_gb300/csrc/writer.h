@@ -35,6 +35,7 @@ constexpr int64_t kIoAlign = 4096;
 struct WriterOpts {
     bool direct = true;        // O_DIRECT (falls back to page-cache writes)
     bool val_fp32 = false;     // Val.output as float32
+    bool src_fp32 = false;     // the value buffers handed to writer_append hold float32 (val_fp32 too)
     bool ptr32 = false;        // Ptr.output as int32
     int64_t rotate_bytes = 0;  // > 0: Idx+Val wrap after this many bytes in total
     bool resume = false;       // progress manifest + continue after the last durable row
@@ -50,7 +51,8 @@ int writer_open(const std::string &dir, const WriterOpts &o, ChunkWriter **w, in
                 std::string *err);
 // Appends the next chunk: n entries ending at row row_end.  idx_base / val_base
 // are 4 KiB-aligned buffers holding the column indices at idx_base +
-// writer_idx_lead(w) and the FP64 values at val_base + writer_val_lead(w),
+// writer_idx_lead(w) and the values (FP64, or float32 with src_fp32) at
+// val_base + writer_val_lead(w),
 // each with the lead bytes before them free for the writer's use (without
 // O_DIRECT the leads are 0).
 int writer_append(ChunkWriter *w, char *idx_base, char *val_base, int64_t n, int64_t row_end, std::string *err);

@@ -81,9 +81,10 @@ typedef struct {
     int64_t nnz;
     int64_t *row_ptr;         /* n_rows + 1 */
     int32_t *col_idx;         /* nnz */
-    double *val;              /* nnz */
+    void *val;                /* nnz doubles, or floats when val_fp32 */
     int32_t on_device;
     int32_t owner;            /* 0: caller, 1: library host allocation, 2: context device memory */
+    int32_t val_fp32;         /* 1: val holds floats (a D2H product with out_val_fp32) */
 } dbd_csr_out;
 
 /* Budgets and layout (the argv of ZIP:dbd/src/main.cpp:152-187 plus the
@@ -93,7 +94,11 @@ typedef struct {
     double gpu_gib;           /* device budget; reference default 22 */
     int64_t rows_per_block;   /* 4096 (for_small_datasets) or 512 (for_large_datasets) */
     int32_t device;           /* CUDA device ordinal */
-    int32_t out_val_fp32;     /* Val.output as float32 (reference layout) instead of FP64 */
+    int32_t out_val_fp32;     /* C's values as float32, the reference's layout: in the D2H and IO
+                                 scopes each chunk's FP64 values are rounded once on the device, so
+                                 8 bytes per entry cross the link (not 12); Val.output is float32 and
+                                 a D2H product kept in host memory holds floats (dbd_csr_out.val_fp32).
+                                 The kernel scope keeps FP64 on the device. */
     int32_t out_ptr32;        /* Ptr.output as int32 (reference layout): 1 always (fails if nnz(C) >= 2^31),
                                  2 when nnz(C) < 2^31 and int64 otherwise */
     int32_t verbose;          /* print the reference's progress lines */
@@ -143,6 +148,10 @@ typedef struct {
     int64_t resumed_from_row; /* +I/O with io_resume: the row an earlier run's manifest let this one start at */
     int64_t heavy_rows;       /* rows whose per-slab counts the symbolic pass kept, so that the dense bin
                                  could cut them into column pieces */
+    double t_chunks_ms;       /* device time of the chunks' numeric work (kernels, float32 rounding,
+                                 digest), summed over chunks: t_numeric_ms minus this is time the
+                                 compute stream waited for a device slot to be copied out */
+    double t_copy_ms;         /* copying scopes: device time of the D2H copies, summed over chunks */
 } dbd_stats;
 
 /* ---- lifecycle ---------------------------------------------------------- */
@@ -224,6 +233,8 @@ int dbd_result(dbd_ctx *ctx, dbd_csr_out *c);
 /* Copies the product of the last multiply (device- or host-resident) into
  * caller-provided arrays, host or device memory, sized from dbd_result:
  * row_ptr n_rows+1, col_idx and val nnz entries; any of them may be NULL.
+ * Float32 values (dbd_csr_out.val_fp32) are widened exactly into a host val
+ * (DBD_ERR_INVALID for a device val: copy them from dbd_result instead).
  * For FFI callers that cannot read the context's memory; the reference hands
  * results back only through Ptr/Idx/Val.output.  With col_idx and val both
  * NULL, row_ptr is copied after any multiply, including one whose C was
