@@ -123,10 +123,10 @@ def bins(A, rowP, nnz_r, sw, tuning=None):
 
 
 SYM_NAMES = {1: "k_sym_tiny", 2: "k_sym_flagw<8>", 3: "k_sym_hash_warp<8,1024>", 4: "k_sym_hash_cta<256,8192>",
-             5: "k_sym_wide<512|1024>"}
+             5: "k_sym_wide<512>"}
 NUM_NAMES = {1: "k_num_tiny", 2: "k_num_rankw<8>", 3: "k_num_hash_warp<4,512>", 4: "k_num_rank<256,shared>",
              5: "k_num_rank<512,in-place>", 6: "k_num_hash_cta<256,2048>", 7: "k_num_hash_cta<512,8192>",
-             8: "k_num_rankwin<1024> (dense bin)", 9: "k_num_densew<8>", 10: "k_num_rankm<5>"}
+             8: "k_num_rankwin<512> (dense bin)", 9: "k_num_densew<8>", 10: "k_num_rankm<5>"}
 
 
 def kernel_bytes(A, rowP, nnz_r, sym, num):
