@@ -52,11 +52,15 @@ def _scope(scope):
     return int(scope)
 
 
-def read_CSR(path):
-    """Reads <path>.dcsr, <path>.csr (reference layout) or converts <path> (.mtx/.dat)."""
+def read_CSR(path, gpu=None):
+    """Reads <path>.dcsr, <path>.csr (reference layout) or converts <path>
+    (.mtx/.dat): on the host, or on CUDA device `gpu` when given."""
     lib = _ffi.load()
     h = _ffi.CsrHost()
-    _check(lib.dbd_read_csr(os.fsencode(path), C.byref(h)))
+    if gpu is None:
+        _check(lib.dbd_read_csr(os.fsencode(path), C.byref(h)))
+    else:
+        _check(lib.dbd_read_csr_gpu(os.fsencode(path), int(gpu), C.byref(h)))
     try:
         n, nnz = h.n_rows, h.nnz
         ptr = np.ctypeslib.as_array(C.cast(h.row_ptr, C.POINTER(C.c_int32)), shape=(n + 1,)).copy()

@@ -84,6 +84,7 @@ SIGNATURES = {
     "dbd_error_string": (C.c_char_p, [C.c_int]),
     "dbd_last_error": (C.c_char_p, [C.c_void_p]),
     "dbd_read_csr": (C.c_int, [C.c_char_p, C.POINTER(CsrHost)]),
+    "dbd_read_csr_gpu": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(CsrHost)]),
     "dbd_csr_host_free": (None, [C.POINTER(CsrHost)]),
     "dbd_write_csr": (C.c_int, [C.c_char_p, C.POINTER(CsrView), C.c_int]),
     "dbd_load_a": (C.c_int, [C.c_void_p, C.POINTER(CsrView)]),

@@ -251,6 +251,14 @@ int read_csr_file(const std::string &path, dbd_csr_host *out, std::string *err) 
     return fail(err, "no " + path + ".dcsr, " + path + ".csr or " + path);
 }
 
+int read_csr_file_gpu(const std::string &path, int device, dbd_csr_host *out, std::string *err) {
+    memset(out, 0, sizeof(*out));
+    if (file_exists(path + ".dcsr")) return read_dcsr(path + ".dcsr", out, err);
+    if (file_exists(path + ".csr")) return read_ref_csr(path + ".csr", out, err);
+    if (file_exists(path)) return convert_matrix_file_gpu(path, device, out, err);
+    return fail(err, "no " + path + ".dcsr, " + path + ".csr or " + path);
+}
+
 int write_csr_file(const std::string &path, const dbd_csr_view *m, int fp64, std::string *err) {
     if (m->on_device) {
         if (err) *err = "dbd_write_csr takes host arrays";

@@ -1354,6 +1354,14 @@ int dbd_read_csr(const char *path, dbd_csr_host *out) {
     return rc;
 }
 
+int dbd_read_csr_gpu(const char *path, int device, dbd_csr_host *out) {
+    if (!path || !out) return DBD_ERR_INVALID;
+    std::string err;
+    int rc = read_csr_file_gpu(path, device, out, &err);
+    if (rc) fprintf(stderr, "dbd_read_csr_gpu: %s\n", err.c_str());
+    return rc;
+}
+
 int dbd_write_csr(const char *path, const dbd_csr_view *m, int fp64) {
     if (!path || !m) return DBD_ERR_INVALID;
     std::string err;
@@ -1907,11 +1915,11 @@ int dbd_spgemm_files(dbd_ctx *c, const char *path_a, const char *path_b, dbd_sco
     if (!c || !path_a) return DBD_ERR_INVALID;
     dbd_csr_host ha, hb;
     memset(&hb, 0, sizeof(hb));
-    int rc = dbd_read_csr(path_a, &ha);
+    int rc = dbd_read_csr_gpu(path_a, c->cfg.device, &ha);
     if (rc) return set_err(c, rc, std::string("cannot read ") + path_a);
     const bool same = !path_b || strcmp(path_a, path_b) == 0;
     if (!same) {
-        rc = dbd_read_csr(path_b, &hb);
+        rc = dbd_read_csr_gpu(path_b, c->cfg.device, &hb);
         if (rc) {
             dbd_csr_host_free(&ha);
             return set_err(c, rc, std::string("cannot read ") + path_b);

@@ -192,6 +192,11 @@ typedef struct {
  * at <path> the way the reference does and caches it as <path>.csr.
  * Replaces read_CSR / make_CSR (ZIP:dbd/src/readInput.cpp:18-176). */
 int dbd_read_csr(const char *path, dbd_csr_host *out);
+/* dbd_read_csr with the Matrix Market / .dat conversion done on GPU `device`
+ * (the text is parsed, its entries stably sorted by row and the CSR built
+ * there): the same CSR and the same <path>.csr cache, byte for byte, as the
+ * host conversion.  dbd_spgemm_files converts on its context's GPU. */
+int dbd_read_csr_gpu(const char *path, int device, dbd_csr_host *out);
 void dbd_csr_host_free(dbd_csr_host *m);
 
 /* Writes <path> in the reference .csr layout (fp64 = 0, values rounded to
