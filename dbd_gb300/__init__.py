@@ -322,6 +322,49 @@ class Context:
                      for q in range(count)]
         return res
 
+    # ---- the capturable batched multiply ----
+    def batch_plan(self, As, Bs=None, capacity=0):
+        """Plans the device-driven batched multiply (dbd_batch_plan): device
+        pairs (CSR.from_device views) whose arrays stay in place, C with room
+        for `capacity` entries."""
+        count = len(As)
+        va = (_ffi.CsrView * count)()
+        keep = []
+        for q, A in enumerate(As):
+            v, k = A.view()
+            va[q] = v
+            keep.append(k)
+        pb = None
+        if Bs is not None:
+            vb = (_ffi.CsrView * count)()
+            for q, B in enumerate(Bs):
+                v, k = B.view()
+                vb[q] = v
+                keep.append(k)
+            pb = C.cast(vb, C.c_void_p)
+        _check(self._lib.dbd_batch_plan(self._h, count, C.cast(va, C.c_void_p), pb, int(capacity)), self._h)
+        ncols = [(Bs[q] if Bs is not None else As[q]).n_cols for q in range(count)]
+        self._batch = (count, keep, ncols)
+
+    def batch_enqueue(self, stream=None):
+        """Enqueues the planned multiply on `stream` (a cudaStream_t as an
+        int; None: the context's) without synchronising: capturable."""
+        _check(self._lib.dbd_batch_enqueue(self._h, C.c_void_p(stream) if stream else None), self._h)
+
+    def batch_result(self, fetch=True):
+        """Status and product of the last enqueued run (after it completed)."""
+        count, _, ncols = self._batch
+        row_off = np.zeros(count + 1, np.int64)
+        nnz_off = np.zeros(count + 1, np.int64)
+        o = _ffi.CsrOut()
+        _check(self._lib.dbd_batch_result(self._h, row_off.ctypes.data, nnz_off.ctypes.data, C.byref(o)), self._h)
+        res = BatchResult(row_off, nnz_off, None)
+        if fetch:
+            whole = self.result()
+            res.C = [whole.slice_pair(row_off[q], row_off[q + 1], nnz_off[q], nnz_off[q + 1], ncols[q])
+                     for q in range(count)]
+        return res
+
     # ---- tuning ----
     @property
     def tuning(self):

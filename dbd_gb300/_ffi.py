@@ -104,6 +104,9 @@ SIGNATURES = {
                                      C.c_int64, C.POINTER(C.c_int64), C.c_void_p]),
     "dbd_spgemm_adjoint": (C.c_int, [C.c_void_p, C.POINTER(CsrView), C.POINTER(CsrView), C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_int, C.c_int]),
+    "dbd_batch_plan": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64]),
+    "dbd_batch_enqueue": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "dbd_batch_result": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(CsrOut)]),
     "dbd_spgemm_batched": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(CsrView), C.POINTER(CsrView), C.c_int,
                                      C.c_void_p, C.c_void_p, C.POINTER(CsrOut), C.POINTER(Stats)]),
     "dbd_update_values": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int]),

@@ -190,6 +190,10 @@ struct SymArgs {
 };
 // Launches the symbolic kernel of bin `bin` over list[begin, begin + n).
 void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cudaStream_t s, int *launches);
+// Device-driven launch of a symbolic bin: its rows from a.binStart on the
+// device, a grid of resident CTAs striding over them (no host read of the
+// bin sizes, so a stream capture holds it).
+void launch_symbolic_bin_dd(const SymArgs &a, int bin, cudaStream_t s, int *launches);
 void launch_f32_to_f64(const float *src, double *dst, int64_t n, cudaStream_t s);
 void launch_validate_ptr(const int32_t *ptr, int64_t m, int64_t nnz, int *flag, cudaStream_t s);
 void launch_validate_idx(const int32_t *idx, int64_t nnz, int64_t ncols, int *flag, cudaStream_t s);
@@ -207,6 +211,7 @@ struct DenseItem {
 struct NumArgs {
     CsrDev A, B;
     const int32_t *list;
+    const int32_t *binStart = nullptr;  // device-driven launches: each bin's [start, end) in list
     const int64_t *Cp;
     int64_t outBase;      // Cp value stored at out[0]
     int32_t *Ci;
@@ -253,6 +258,11 @@ struct NumArgs {
 inline size_t gdense_slot_bytes(int64_t stride) { return (size_t)stride / 4; }
 constexpr int kGdenseSumMax = 8192;  // summary words in shared memory: C up to 2^23 columns
 // Runs the numeric kernels of bin b over list[lo, hi).
+// Device-driven launch of a numeric bin (rows from a.binStart on the
+// device; the dense bin on rank windows without pieces).
+void launch_numeric_bin_dd(const NumArgs &a, int bin, cudaStream_t s, int *launches);
+// Looks up the grids of the device-driven launches ahead of a stream capture.
+void prepare_dd_grids(const Tuning &t, int64_t bcols, int sms);
 void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,
                         int *launches);
 
@@ -293,6 +303,13 @@ void launch_batch_gather(const BatchPair *pairs, const int64_t *rowOff, const in
 
 // dst[i] = src[idx[i]] for i < n.
 void launch_gather_i64(const int64_t *src, const int64_t *idx, int64_t n, int64_t *dst, cudaStream_t s);
+// Guards of the device-driven (capturable) batched multiply: a bad pair
+// (*bad) empties both operands (nA / nB row pointers); a symbolic error or
+// nnz(C) above capacity empties every numeric bin (the latter sets *over).
+void launch_batch_guard(const int *bad, int32_t *ptrA, int64_t nA, int32_t *ptrB, int64_t nB, cudaStream_t s,
+                        int num_sms);
+void launch_numeric_guard(const int64_t *nnz, int64_t capacity, const int *err, int32_t *binStart, int nbins, int *over,
+                          cudaStream_t s);
 
 // ---- output digest (k_digest.cu) ----
 // Per-row digest arrays of C (m entries each) and the count of rows whose
@@ -324,5 +341,6 @@ void init_kernel_attributes();
 // first launch (cudaFuncGetAttributes on each); the first error is returned.
 cudaError_t preload_analysis_kernels();
 cudaError_t preload_spgemm_kernels();
+cudaError_t preload_batch_kernels();
 
 }  // namespace dbd

@@ -161,6 +161,11 @@ struct dbd_ctx {
     DevBuf batchDev, rowShift;
     HostBuf batchHost;
     int64_t batchCount = 0;
+    // Device-driven batched multiply (dbd_batch_plan / _enqueue / _result):
+    // the planned pairs' shapes and the output's capacity.
+    bool bpOk = false, bpSquare = false;
+    int64_t bpCount = 0, bpCap = 0, bpColsC = 0, bpNnzB = 0, bpRowsB = 0;
+    std::vector<int64_t> bpRowOff;
     std::vector<int64_t> batchNnzA, batchNnzB;  // per-pair entry offsets of the last batch (count + 1)
     // The numeric launches of the last multiply captured as a CUDA graph,
     // replayed by dbd_update_values (dropped by the next multiply).
@@ -1748,6 +1753,267 @@ int dbd_spgemm_batched(dbd_ctx *c, int64_t count, const dbd_csr_view *a, const d
     if (c_nnz_off) memcpy(c_nnz_off, hCoff, sizeof(int64_t) * n1);
     if (st) *st = c->stats;
     if (out) return dbd_result(c, out);
+    return DBD_OK;
+}
+
+// ---- device-driven batched multiply ---------------------------------------
+
+int dbd_batch_plan(dbd_ctx *c, int64_t count, const dbd_csr_view *a, const dbd_csr_view *b, int64_t c_capacity) {
+    if (!c || !a || count <= 0 || c_capacity < 0) return DBD_ERR_INVALID;
+    cudaSetDevice(c->cfg.device);
+    c->bpOk = false;
+    c->batchCount = 0;
+    c->replayOk = false;
+    drop_graph(c);
+    c->A.loaded = c->B.loaded = false;
+    c->divided = false;
+    const bool square = b == nullptr;
+    const dbd_csr_view *bv = square ? a : b;
+    const size_t n1 = (size_t)count + 1;
+    std::vector<BatchPair> desc(2 * (size_t)count);
+    std::vector<int64_t> off(5 * n1, 0);
+    int64_t *rowA = off.data(), *nnzA = rowA + n1, *rowB = nnzA + n1, *nnzB = rowB + n1, *colC = nnzB + n1;
+    for (int64_t q = 0; q < count; ++q) {
+        const dbd_csr_view &x = a[q], &y = bv[q];
+        const std::string tag = "pair " + std::to_string(q);
+        for (const dbd_csr_view *v : {&x, &y}) {
+            if (!v->on_device || v->val_fp32 || v->n_rows < 0 || v->n_cols < 0 || v->nnz < 0 || !v->row_ptr ||
+                (v->nnz > 0 && (!v->col_idx || !v->val)) || (v->n_rows == 0 && v->nnz > 0))
+                return set_err(c, DBD_ERR_INVALID, tag + ": device-resident FP64 operands required");
+        }
+        if (x.n_cols != y.n_rows) return set_err(c, DBD_ERR_INVALID, tag + ": inner dimensions differ");
+        rowA[q + 1] = rowA[q] + x.n_rows;
+        nnzA[q + 1] = nnzA[q] + x.nnz;
+        rowB[q + 1] = rowB[q] + y.n_rows;
+        nnzB[q + 1] = nnzB[q] + y.nnz;
+        colC[q + 1] = colC[q] + y.n_cols;
+    }
+    const int64_t lim = INT32_MAX - 1;
+    if (rowA[count] > lim || rowB[count] > lim || colC[count] > lim || nnzA[count] > lim || nnzB[count] > lim)
+        return set_err(c, DBD_ERR_INVALID, "the batch exceeds 2^31 rows, columns or entries; split it");
+    for (int side = 0; side < (square ? 1 : 2); ++side) {
+        const dbd_csr_view *views = side ? bv : a;
+        const int64_t *nOff = side ? nnzB : nnzA, *cOff = side ? colC : rowB;
+        for (int64_t q = 0; q < count; ++q) {
+            BatchPair &d = desc[(size_t)(side * count + q)];
+            d.m = views[q].n_rows;
+            d.nnz = views[q].nnz;
+            d.ncols = views[q].n_cols;
+            d.nnzOff = nOff[q];
+            d.colOff = cOff[q];
+            d.shift = side ? 0 : (int32_t)colC[q];
+            d.ptr = views[q].row_ptr;
+            d.idx = views[q].col_idx;
+            d.val = (const double *)views[q].val;
+        }
+    }
+    // Operands, descriptors, work arrays and C, all sized here.
+    const int64_t m = rowA[count];
+    const size_t descBytes = sizeof(BatchPair) * desc.size();
+    CK(c, c->batchDev.ensure(descBytes + sizeof(int64_t) * 6 * n1));
+    CK(c, cudaMemcpy(c->batchDev.p, desc.data(), descBytes, cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(c->batchDev.as<char>() + descBytes, off.data(), sizeof(int64_t) * 5 * n1, cudaMemcpyHostToDevice));
+    auto sized = [&](Operand &op, int64_t rows, int64_t ne) -> int {
+        CK(c, op.ptr.ensure(sizeof(int32_t) * (size_t)(rows + 1)));
+        CK(c, op.idx.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(ne, 1)));
+        CK(c, op.val.ensure(sizeof(double) * (size_t)std::max<int64_t>(ne, 1)));
+        CK(c, op.bmin.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(rows, 1)));
+        CK(c, op.bmax.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(rows, 1)));
+        return DBD_OK;
+    };
+    int rc = sized(c->A, m, nnzA[count]);
+    if (!rc && !square) rc = sized(c->B, rowB[count], nnzB[count]);
+    if (rc) return rc;
+    CK(c, c->rowShift.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1)));
+    CK(c, c->flags.ensure(4 * sizeof(int)));
+    CsrDev da{}, db{};
+    da.m = m;
+    da.n = rowB[count];
+    da.nnz = nnzA[count];
+    da.ptr = c->A.ptr.as<int32_t>();
+    da.idx = c->A.idx.as<int32_t>();
+    da.val = c->A.val.as<double>();
+    c->A.dev = da;
+    c->A.sorted = 0;
+    c->A.loaded = true;
+    c->b_is_a = square;
+    if (!square) {
+        db.m = rowB[count];
+        db.n = colC[count];
+        db.nnz = nnzB[count];
+        db.ptr = c->B.ptr.as<int32_t>();
+        db.idx = c->B.idx.as<int32_t>();
+        db.val = c->B.val.as<double>();
+        c->B.dev = db;
+        c->B.sorted = 0;
+        c->B.loaded = true;
+    }
+    c->m = m;
+    c->ncols = colC[count];
+    c->ntiles = ceil_div(m, kTileRows);
+    const size_t mm = (size_t)std::max<int64_t>(m, 1), nt = (size_t)c->ntiles;
+    CK(c, c->rowP.ensure(sizeof(int64_t) * mm));
+    CK(c, c->rowLo.ensure(sizeof(int32_t) * mm));
+    CK(c, c->rowHi.ensure(sizeof(int32_t) * mm));
+    CK(c, c->symBin.ensure(mm));
+    CK(c, c->numBin.ensure(mm));
+    CK(c, c->rowNnz.ensure(sizeof(int32_t) * mm));
+    CK(c, c->symList.ensure(sizeof(int32_t) * mm));
+    CK(c, c->numList.ensure(sizeof(int32_t) * mm));
+    CK(c, c->hist.ensure(sizeof(int32_t) * kMaxBins * (nt + 1)));
+    CK(c, c->symTileOff.ensure(sizeof(int32_t) * kMaxBins * (nt + 1)));
+    CK(c, c->numTileOff.ensure(sizeof(int32_t) * kMaxBins * (nt + 1)));
+    CK(c, c->symStart.ensure(sizeof(int32_t) * (kMaxBins + 1)));
+    CK(c, c->numStart.ensure(sizeof(int32_t) * (kMaxBins + 1)));
+    CK(c, c->part.ensure(sizeof(int64_t) * (size_t)(ceil_div(m, kScanTile) + 1)));
+    CK(c, c->Cp.ensure(sizeof(int64_t) * (mm + 1)));
+    CK(c, c->cursor.ensure(2 * sizeof(int32_t) * (size_t)std::max<int64_t>(nnzA[count], 1)));
+    CK(c, c->err.ensure(sizeof(int)));
+    CK(c, c->ctrs.ensure(sizeof(uint32_t) * CTR_COUNT));
+    CK(c, c->Ci.ensure(sizeof(int32_t) * (size_t)std::max<int64_t>(c_capacity, 1)));
+    CK(c, c->Cv.ensure(sizeof(double) * (size_t)std::max<int64_t>(c_capacity, 1)));
+    // Every kernel of the run is loaded (and every grid looked up) now, so
+    // that a capture of dbd_batch_enqueue loads and queries nothing.
+    cudaError_t le = preload_analysis_kernels();
+    if (le == cudaSuccess) le = preload_batch_kernels();
+    if (le != cudaSuccess) return cuda_fail(c, le, "loading the kernels");
+    prepare_dd_grids(c->tune, colC[count], c->num_sms);
+    c->bpSquare = square;
+    c->bpCount = count;
+    c->bpCap = c_capacity;
+    c->bpColsC = colC[count];
+    c->bpRowsB = rowB[count];
+    c->bpNnzB = nnzB[count];
+    c->bpRowOff.assign(rowA, rowA + n1);
+    c->bpOk = true;
+    return DBD_OK;
+}
+
+int dbd_batch_enqueue(dbd_ctx *c, void *stream) {
+    if (!c) return DBD_ERR_INVALID;
+    if (!c->bpOk) return set_err(c, DBD_ERR_INVALID, "no batch planned (dbd_batch_plan)");
+    cudaSetDevice(c->cfg.device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    const int64_t count = c->bpCount, m = c->m;
+    const size_t n1 = (size_t)count + 1;
+    const size_t descBytes = sizeof(BatchPair) * 2 * (size_t)count;
+    const BatchPair *dpa = c->batchDev.as<BatchPair>();
+    const int64_t *drow = reinterpret_cast<const int64_t *>(c->batchDev.as<char>() + descBytes);
+    const int64_t *dnnzA = drow + n1, *drowB = dnnzA + n1, *dnnzB = drowB + n1;
+    int64_t *dCoff = const_cast<int64_t *>(dnnzB + 2 * n1);
+    int *flags = c->flags.as<int>();
+    CK(c, cudaMemsetAsync(flags, 0, 4 * sizeof(int), s));
+    CK(c, cudaMemsetAsync(c->err.p, 0, sizeof(int), s));
+    CK(c, cudaMemsetAsync(c->ctrs.p, 0, sizeof(uint32_t) * CTR_COUNT, s));
+    CK(c, cudaMemsetAsync(c->rowNnz.p, 0, sizeof(int32_t) * (size_t)std::max<int64_t>(m, 1), s));
+    // The pairs' current contents, gathered into the concatenated operands.
+    launch_batch_gather(dpa, drow, dnnzA, count, m, c->A.dev.nnz, c->A.ptr.as<int32_t>(), c->A.idx.as<int32_t>(),
+                        c->A.val.as<double>(), c->rowShift.as<int32_t>(), flags, s);
+    if (!c->bpSquare)
+        launch_batch_gather(dpa + count, drowB, dnnzB, count, c->bpRowsB, c->bpNnzB, c->B.ptr.as<int32_t>(),
+                            c->B.idx.as<int32_t>(), c->B.val.as<double>(), nullptr, flags, s);
+    launch_batch_guard(flags, c->A.ptr.as<int32_t>(), m + 1, c->bpSquare ? nullptr : c->B.ptr.as<int32_t>(),
+                       c->bpSquare ? 0 : c->bpRowsB + 1, s, c->num_sms);
+    const CsrDev &A = c->A.dev, &B = opB(c);
+    const Operand &opb = c->bpSquare ? c->A : c->B;
+    int launches = 0;
+    launch_row_minmax(B, opb.bmin.as<int32_t>(), opb.bmax.as<int32_t>(), flags + 2, s, c->num_sms);
+    launch_row_products(A, B.ptr, opb.bmin.as<int32_t>(), opb.bmax.as<int32_t>(), row_info(c), c->symBin.as<uint8_t>(),
+                        c->err.as<int>(), c->tune, s, c->num_sms);
+    Binning sb{c->symBin.as<uint8_t>(), c->symList.as<int32_t>(), c->hist.as<int32_t>(), c->symTileOff.as<int32_t>(),
+               c->symStart.as<int32_t>()};
+    launch_bin_lists(m, sb, SB_COUNT, s);
+    SymArgs sa{};
+    sa.A = A;
+    sa.B = B;
+    sa.list = c->symList.as<int32_t>();
+    sa.binStart = c->symStart.as<int32_t>();
+    sa.rowNnz = c->rowNnz.as<int32_t>();
+    sa.ctr = c->ctrs.as<uint32_t>();
+    sa.err = c->err.as<int>();
+    sa.rowLo = c->rowLo.as<int32_t>();
+    sa.rowHi = c->rowHi.as<int32_t>();
+    sa.rowP = c->rowP.as<int64_t>();
+    sa.tune = c->tune;
+    sa.numSms = c->num_sms;
+    sa.bSorted = 0;  // not known on the host here: the general paths
+    static const int sorder[] = {SB_WIDE, SB_HCTA, SB_HWARP, SB_BITW, SB_TINY};
+    for (int bin : sorder) launch_symbolic_bin_dd(sa, bin, s, &launches);
+    launch_row_scan(m, c->rowNnz.as<int32_t>(), c->part.as<int64_t>(), c->Cp.as<int64_t>(), s);
+    launch_num_bins(m, A.ptr, row_info(c), c->rowNnz.as<int32_t>(), c->numBin.as<uint8_t>(), c->tune, s, c->num_sms);
+    Binning nb{c->numBin.as<uint8_t>(), c->numList.as<int32_t>(), c->hist.as<int32_t>(), c->numTileOff.as<int32_t>(),
+               c->numStart.as<int32_t>()};
+    launch_bin_lists(m, nb, NB_COUNT, s);
+    launch_numeric_guard(c->Cp.as<int64_t>() + m, c->bpCap, c->err.as<int>(), c->numStart.as<int32_t>(), NB_COUNT,
+                         flags + 3, s);
+    NumArgs na{};
+    na.A = A;
+    na.B = B;
+    na.list = c->numList.as<int32_t>();
+    na.binStart = c->numStart.as<int32_t>();
+    na.Cp = c->Cp.as<int64_t>();
+    na.outBase = 0;
+    na.Ci = c->Ci.as<int32_t>();
+    na.Cv = c->Cv.as<double>();
+    na.state = c->cursor.as<int32_t>();
+    na.bSorted = 0;
+    na.err = c->err.as<int>();
+    na.rowP = c->rowP.as<int64_t>();
+    na.rowLo = c->rowLo.as<int32_t>();
+    na.rowHi = c->rowHi.as<int32_t>();
+    na.colShift = c->rowShift.as<int32_t>();
+    na.tune = c->tune;
+    na.tune.denseMethod = 0;
+    na.numSms = c->num_sms;
+    na.ctr = c->ctrs.as<uint32_t>();
+    static const int norder[] = {NB_DENSE, NB_RANKL, NB_HCTA_L, NB_RANKS, NB_HCTA_S,
+                                 NB_HWARP, NB_RANKM, NB_RANKW, NB_DENSEW, NB_TINY};
+    for (int bin : norder) launch_numeric_bin_dd(na, bin, s, &launches);
+    launch_gather_i64(c->Cp.as<int64_t>(), drow, (int64_t)n1, dCoff, s);
+    CK(c, cudaGetLastError());
+    c->launches = launches + 10;
+    c->last_scope = DBD_SCOPE_KERNEL;
+    c->dev_resident = true;
+    c->host_full = false;
+    c->host_f32 = false;
+    c->batchCount = count;
+    c->patternOk = false;
+    return DBD_OK;
+}
+
+int dbd_batch_result(dbd_ctx *c, int64_t *c_row_off, int64_t *c_nnz_off, dbd_csr_out *out) {
+    if (!c) return DBD_ERR_INVALID;
+    if (!c->bpOk) return set_err(c, DBD_ERR_INVALID, "no batch planned (dbd_batch_plan)");
+    cudaSetDevice(c->cfg.device);
+    const int64_t count = c->bpCount, m = c->m;
+    const size_t n1 = (size_t)count + 1;
+    int hf[4] = {0, 0, 0, 0}, derr = 0;
+    int64_t nnz = 0;
+    CK(c, cudaMemcpy(hf, c->flags.p, sizeof(hf), cudaMemcpyDeviceToHost));
+    CK(c, cudaMemcpy(&derr, c->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(c, cudaMemcpy(&nnz, c->Cp.as<int64_t>() + m, sizeof(int64_t), cudaMemcpyDeviceToHost));
+    if (hf[0]) return set_err(c, DBD_ERR_INVALID, (hf[0] & 1) ? "a pair's row_ptr does not span [0, nnz] monotonically"
+                                                               : "a pair's column index is out of range");
+    if (derr) return set_err(c, DBD_ERR_CUDA, "a device table overflowed in the batched multiply");
+    c->nnzC = nnz;
+    if (hf[3]) return set_err(c, DBD_ERR_BUDGET, "nnz(C) = " + std::to_string(nnz) + " exceeds the planned capacity");
+    if (c_row_off) memcpy(c_row_off, c->bpRowOff.data(), sizeof(int64_t) * n1);
+    if (c_nnz_off) {
+        const size_t descBytes = sizeof(BatchPair) * 2 * (size_t)count;
+        const int64_t *dCoff = reinterpret_cast<const int64_t *>(c->batchDev.as<char>() + descBytes) + 5 * n1;
+        CK(c, cudaMemcpy(c_nnz_off, dCoff, sizeof(int64_t) * n1, cudaMemcpyDeviceToHost));
+    }
+    if (out) {
+        memset(out, 0, sizeof(*out));
+        out->n_rows = m;
+        out->n_cols = c->bpColsC;
+        out->nnz = nnz;
+        out->row_ptr = c->Cp.as<int64_t>();
+        out->col_idx = c->Ci.as<int32_t>();
+        out->val = c->Cv.p;
+        out->on_device = 1;
+        out->owner = 2;
+    }
     return DBD_OK;
 }
 

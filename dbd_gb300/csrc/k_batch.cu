@@ -8,6 +8,7 @@
 // kernels below validate each pair's arrays while they copy them (row_ptr
 // spans [0, nnz] and never decreases, every column is inside the pair's
 // column range); they never trap, a bad pair sets a flag the host reads.
+#include <algorithm>
 #include <cstdint>
 
 #include "dbd_internal.h"
@@ -81,6 +82,29 @@ k_batch_entries(const BatchPair *pairs, const int64_t *nnzOff, int64_t count, in
     }
 }
 
+// Device-driven multiplies: a bad pair empties both concatenated operands
+// (every row pointer 0), so that nothing downstream reads past an operand.
+__global__ void __launch_bounds__(256) k_batch_guard(const int *bad, int32_t *ptrA, int64_t nA, int32_t *ptrB,
+                                                     int64_t nB) {
+    if (!*bad) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nA + nB; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < nA) ptrA[i] = 0;
+        else if (ptrB) ptrB[i - nA] = 0;
+    }
+}
+
+// Device-driven multiplies: with an error in the symbolic pass or nnz(C)
+// above the output's capacity, every numeric bin is emptied (and *over set
+// in the second case), so the numeric kernels write nothing.
+__global__ void k_numeric_guard(const int64_t *nnz, int64_t capacity, const int *err, int32_t *binStart, int nbins,
+                                int *over) {
+    if (threadIdx.x != 0) return;
+    const bool full = *nnz > capacity;
+    if (full) *over = 1;
+    if (full || *err)
+        for (int b = 0; b <= nbins; ++b) binStart[b] = 0;
+}
+
 __global__ void k_gather_i64(const int64_t *src, const int64_t *idx, int64_t n, int64_t *dst) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dst[i] = src[idx[i]];
@@ -91,6 +115,30 @@ __global__ void k_gather_i64(const int64_t *src, const int64_t *idx, int64_t n, 
 void launch_gather_i64(const int64_t *src, const int64_t *idx, int64_t n, int64_t *dst, cudaStream_t s) {
     if (n <= 0) return;
     k_gather_i64<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(src, idx, n, dst);
+}
+
+cudaError_t preload_batch_kernels() {
+    const void *fns[] = {(const void *)k_batch_rows, (const void *)k_batch_entries, (const void *)k_batch_guard,
+                         (const void *)k_numeric_guard, (const void *)k_gather_i64};
+    for (const void *f : fns) {
+        cudaFuncAttributes fa;
+        const cudaError_t e = cudaFuncGetAttributes(&fa, f);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+void launch_batch_guard(const int *bad, int32_t *ptrA, int64_t nA, int32_t *ptrB, int64_t nB, cudaStream_t s,
+                        int num_sms) {
+    const int64_t n = nA + nB;
+    if (n <= 0) return;
+    k_batch_guard<<<(unsigned)std::min<int64_t>(ceil_div(n, 256), (int64_t)num_sms * 8), 256, 0, s>>>(bad, ptrA, nA,
+                                                                                                     ptrB, nB);
+}
+
+void launch_numeric_guard(const int64_t *nnz, int64_t capacity, const int *err, int32_t *binStart, int nbins, int *over,
+                          cudaStream_t s) {
+    k_numeric_guard<<<1, 32, 0, s>>>(nnz, capacity, err, binStart, nbins, over);
 }
 
 void launch_batch_gather(const BatchPair *pairs, const int64_t *rowOff, const int64_t *nnzOff, int64_t count,

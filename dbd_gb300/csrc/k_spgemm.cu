@@ -45,6 +45,8 @@
 #include "dbd_internal.h"
 
 #include <algorithm>
+#include <mutex>
+#include <vector>
 #include <climits>
 
 namespace dbd {
@@ -546,9 +548,9 @@ struct StageLayout {
 // ======================================================================
 
 // Tiny rows: one warp per row, all products at once (P_r <= 32, |A_r| <= 32).
-__global__ void __launch_bounds__(256) k_sym_tiny(SymArgs a, int32_t begin, int32_t count) {
+__device__ __forceinline__ void sym_tiny_rows(const SymArgs &a, int32_t begin, int32_t count, int64_t vb) {
     const int lane = threadIdx.x & 31;
-    const int64_t item = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int64_t item = (int64_t)vb * 8 + (threadIdx.x >> 5);
     if (item >= count) return;
     const int32_t row = a.list[begin + item];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
@@ -562,12 +564,26 @@ __global__ void __launch_bounds__(256) k_sym_tiny(SymArgs a, int32_t begin, int3
     if (lane == 0) a.rowNnz[row] = __popc(lm);
 }
 
+__global__ void __launch_bounds__(256) k_sym_tiny(SymArgs a, int32_t begin, int32_t count) {
+    sym_tiny_rows(a, begin, count, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+__global__ void __launch_bounds__(256) k_sym_tiny_dd(SymArgs a, int bin) {
+    const int32_t begin = a.binStart[bin], count = a.binStart[bin + 1] - begin;
+    for (int64_t vb = blockIdx.x; vb * 8 < count; vb += gridDim.x) {
+        sym_tiny_rows(a, begin, count, vb);
+        __syncthreads();
+    }
+}
+
 // Warp hash rows: one warp per row, ROWS rows per CTA, TABLE keys per row.
 template <int ROWS, int TABLE>
-__global__ void __launch_bounds__(32 * ROWS) k_sym_hash_warp(SymArgs a, int32_t begin, int32_t count) {
+__device__ __forceinline__ void sym_hash_warp_rows(const SymArgs &a, int32_t begin, int32_t count, int64_t vb) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    const int64_t item = (int64_t)vb * ROWS + g;
     if (item >= count) return;
     int32_t *keys = reinterpret_cast<int32_t *>(smem) + (size_t)g * TABLE;
     const int32_t row = a.list[begin + item];
@@ -597,9 +613,25 @@ __global__ void __launch_bounds__(32 * ROWS) k_sym_hash_warp(SymArgs a, int32_t 
     if (lane == 0) a.rowNnz[row] = cnt;
 }
 
+template <int ROWS, int TABLE>
+__global__ void __launch_bounds__(32 * ROWS) k_sym_hash_warp(SymArgs a, int32_t begin, int32_t count) {
+    sym_hash_warp_rows<ROWS, TABLE>(a, begin, count, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+template <int ROWS, int TABLE>
+__global__ void __launch_bounds__(32 * ROWS) k_sym_hash_warp_dd(SymArgs a, int bin) {
+    const int32_t begin = a.binStart[bin], count = a.binStart[bin + 1] - begin;
+    for (int64_t vb = blockIdx.x; vb * ROWS < count; vb += gridDim.x) {
+        sym_hash_warp_rows<ROWS, TABLE>(a, begin, count, vb);
+        __syncthreads();
+    }
+}
+
 // CTA hash rows: one CTA per row, products spread over all threads.
 template <int THREADS, int TABLE>
-__global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t begin) {
+__device__ __forceinline__ void sym_hash_cta_rows(const SymArgs &a, int32_t begin, int64_t vb) {
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
     __shared__ int32_t sh[THREADS / 32];
@@ -607,7 +639,7 @@ __global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t beg
     int32_t *bst = reinterpret_cast<int32_t *>(smem + L::bst);
     int32_t *keys = reinterpret_cast<int32_t *>(smem + L::bytes);
     const int tid = threadIdx.x;
-    const int32_t row = a.list[begin + blockIdx.x];
+    const int32_t row = a.list[begin + vb];
     for (int i = tid; i < TABLE; i += THREADS) keys[i] = EMPTY;
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     int cnt = 0;
@@ -626,6 +658,22 @@ __global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t beg
     }
     cnt = block_sum_i<THREADS>(cnt, sh);
     if (tid == 0) a.rowNnz[row] = cnt;
+}
+
+template <int THREADS, int TABLE>
+__global__ void __launch_bounds__(THREADS) k_sym_hash_cta(SymArgs a, int32_t begin) {
+    sym_hash_cta_rows<THREADS, TABLE>(a, begin, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+template <int THREADS, int TABLE>
+__global__ void __launch_bounds__(THREADS) k_sym_hash_cta_dd(SymArgs a, int bin) {
+    const int32_t begin = a.binStart[bin], count = a.binStart[bin + 1] - begin;
+    for (int64_t vb = blockIdx.x; vb < count; vb += gridDim.x) {
+        sym_hash_cta_rows<THREADS, TABLE>(a, begin, vb);
+        __syncthreads();
+    }
 }
 
 // or_bit that also counts and records: returns the number of bits this
@@ -660,6 +708,10 @@ __host__ __device__ __forceinline__ int wide_touch_cap(int winBits) {
 // pass over the window either: a row costs its products, not its span.
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, int32_t count, int winBits) {
+    if (begin < 0) {  // device-driven: the bin's rows from the bin table
+        begin = a.binStart[SB_WIDE];
+        count = a.binStart[SB_WIDE + 1] - begin;
+    }
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
     __shared__ int32_t sh[THREADS / 32];
@@ -877,11 +929,11 @@ constexpr int kRowwiseMinLen = 16;
 // one flag byte per column of the window in shared memory; the row's size is
 // the number of flags set.
 template <int ROWS>
-__global__ void __launch_bounds__(32 * ROWS) k_sym_flagw(SymArgs a, int32_t begin, int32_t count) {
+__device__ __forceinline__ void sym_flagw_rows(const SymArgs &a, int32_t begin, int32_t count, int64_t vb) {
     constexpr int kWords = kWarpSpanWords * 8;  // 32 flag bytes per window word
     __shared__ uint32_t fls[ROWS][kWords];
     const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    const int64_t item = (int64_t)vb * ROWS + g;
     if (item >= count) return;
     uint32_t *fw = fls[g];
     uint8_t *fb = reinterpret_cast<uint8_t *>(fw);
@@ -957,6 +1009,22 @@ __global__ void __launch_bounds__(32 * ROWS) k_sym_flagw(SymArgs a, int32_t begi
     if (lane == 0) a.rowNnz[row] = cnt;
 }
 
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_sym_flagw(SymArgs a, int32_t begin, int32_t count) {
+    sym_flagw_rows<ROWS>(a, begin, count, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_sym_flagw_dd(SymArgs a, int bin) {
+    const int32_t begin = a.binStart[bin], count = a.binStart[bin + 1] - begin;
+    for (int64_t vb = blockIdx.x; vb * ROWS < count; vb += gridDim.x) {
+        sym_flagw_rows<ROWS>(a, begin, count, vb);
+        __syncthreads();
+    }
+}
+
 // ======================================================================
 // Numeric kernels: columns ascending, values in FP64.
 // ======================================================================
@@ -966,9 +1034,9 @@ __device__ __forceinline__ int32_t col_shift(const NumArgs &a, int32_t row) {
     return a.colShift ? a.colShift[row] : 0;
 }
 
-__global__ void __launch_bounds__(256) k_num_tiny(NumArgs a, int32_t lo, int32_t count) {
+__device__ __forceinline__ void num_tiny_rows(const NumArgs &a, int32_t lo, int32_t count, int64_t vb) {
     const int lane = threadIdx.x & 31;
-    const int64_t item = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int64_t item = (int64_t)vb * 8 + (threadIdx.x >> 5);
     if (item >= count) return;
     const int32_t row = a.list[lo + item];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
@@ -1002,6 +1070,20 @@ __global__ void __launch_bounds__(256) k_num_tiny(NumArgs a, int32_t lo, int32_t
         a.Cv[base + rank] = acc;
     }
     if (lane == 0 && __popc(lm) != expect) raise(a.err, DEV_COUNT_MISMATCH);
+}
+
+__global__ void __launch_bounds__(256) k_num_tiny(NumArgs a, int32_t lo, int32_t count) {
+    num_tiny_rows(a, lo, count, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+__global__ void __launch_bounds__(256) k_num_tiny_dd(NumArgs a, int bin) {
+    const int32_t lo = a.binStart[bin], count = a.binStart[bin + 1] - lo;
+    for (int64_t vb = blockIdx.x; vb * 8 < count; vb += gridDim.x) {
+        num_tiny_rows(a, lo, count, vb);
+        __syncthreads();
+    }
 }
 
 // Bitonic sort of buf[0, N) ascending by GROUP threads (N a power of two).
@@ -1106,7 +1188,7 @@ __device__ __forceinline__ bool warp_bucket_order(const uint64_t *in, int n, int
 // bucket buffers (cnts, bbuf) and are ordered by warp_bucket_order when
 // their columns spread evenly.
 template <int GROUP, int ROWS, int TABLE>
-__device__ __forceinline__ void table_write_sorted(NumArgs &a, int32_t row, int32_t *keys, const double *vals,
+__device__ __forceinline__ void table_write_sorted(const NumArgs &a, int32_t row, int32_t *keys, const double *vals,
                                                    int *gcnt, int gt, int *cnts = nullptr,
                                                    uint64_t *bbuf = nullptr) {
     constexpr int KPT = TABLE / GROUP;
@@ -1175,7 +1257,7 @@ constexpr size_t warp_hash_bytes(int table) { return 12 * (size_t)table + 4 * (s
 // holding its first entry and written at the run's rank.  pk holds
 // kNumWarpMax packed (column << 32 | product) keys, pv the products' values.
 template <int ROWS>
-__device__ __forceinline__ void esc_row(NumArgs &a, int32_t row, int32_t e0, int32_t e1, int n, uint64_t *pk,
+__device__ __forceinline__ void esc_row(const NumArgs &a, int32_t row, int32_t e0, int32_t e1, int n, uint64_t *pk,
                                         double *pv, int *cnts, uint64_t *bbuf) {
     const int lane = threadIdx.x & 31;
     int32_t tb = 0;  // products of the earlier chunks
@@ -1260,11 +1342,11 @@ __device__ __forceinline__ void esc_row(NumArgs &a, int32_t row, int32_t e0, int
 }
 
 template <int ROWS, int TABLE>
-__global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t lo, int32_t count) {
+__device__ __forceinline__ void num_hash_warp_rows(const NumArgs &a, int32_t lo, int32_t count, int64_t vb) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int gcnt[ROWS];
     const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    const int64_t item = (int64_t)vb * ROWS + g;
     if (item >= count) return;
     unsigned char *base_ptr = smem + (size_t)g * warp_hash_bytes(TABLE);
     int32_t *keys = reinterpret_cast<int32_t *>(base_ptr);
@@ -1318,9 +1400,25 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t 
     table_write_sorted<32, ROWS, TABLE>(a, row, keys, vals, &gcnt[g], lane);
 }
 
+template <int ROWS, int TABLE>
+__global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp(NumArgs a, int32_t lo, int32_t count) {
+    num_hash_warp_rows<ROWS, TABLE>(a, lo, count, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+template <int ROWS, int TABLE>
+__global__ void __launch_bounds__(32 * ROWS) k_num_hash_warp_dd(NumArgs a, int bin) {
+    const int32_t lo = a.binStart[bin], count = a.binStart[bin + 1] - lo;
+    for (int64_t vb = blockIdx.x; vb * ROWS < count; vb += gridDim.x) {
+        num_hash_warp_rows<ROWS, TABLE>(a, lo, count, vb);
+        __syncthreads();
+    }
+}
+
 // CTA hash rows: one CTA per row, products spread over all threads.
 template <int THREADS, int TABLE>
-__global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo) {
+__device__ __forceinline__ void num_hash_cta_rows(const NumArgs &a, int32_t lo, int64_t vb) {
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
     __shared__ int32_t sh[THREADS / 32];
@@ -1331,7 +1429,7 @@ __global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo)
     int32_t *keys = reinterpret_cast<int32_t *>(smem + L::bytes);
     double *vals = reinterpret_cast<double *>(smem + L::bytes + 4 * (size_t)TABLE);
     const int tid = threadIdx.x;
-    const int32_t row = a.list[lo + blockIdx.x];
+    const int32_t row = a.list[lo + vb];
     for (int i = tid; i < TABLE; i += THREADS) {
         keys[i] = EMPTY;
         vals[i] = 0.0;
@@ -1358,6 +1456,22 @@ __global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo)
     table_write_sorted<THREADS, 1, TABLE>(a, row, keys, vals, &gcnt, tid);
 }
 
+template <int THREADS, int TABLE>
+__global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo) {
+    num_hash_cta_rows<THREADS, TABLE>(a, lo, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+template <int THREADS, int TABLE>
+__global__ void __launch_bounds__(THREADS) k_num_hash_cta_dd(NumArgs a, int bin) {
+    const int32_t lo = a.binStart[bin], count = a.binStart[bin + 1] - lo;
+    for (int64_t vb = blockIdx.x; vb < count; vb += gridDim.x) {
+        num_hash_cta_rows<THREADS, TABLE>(a, lo, vb);
+        __syncthreads();
+    }
+}
+
 // Rank rows (C has at most 2^18 columns): one CTA per row.  Pass 1 sets the
 // row's columns in a shared bitmap over all of C's columns; a scan of the
 // words' popcounts gives every column its rank among the row's columns, which
@@ -1367,7 +1481,7 @@ __global__ void __launch_bounds__(THREADS) k_num_hash_cta(NumArgs a, int32_t lo)
 // GLOBAL_ACC the row's slice of C's values is zeroed and accumulated in place
 // by FP64 reductions at L2 (no shared value array, no slices).
 template <int THREADS, bool GLOBAL_ACC>
-__global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArgs a, int32_t lo, int maxWords, int vcap) {
+__device__ __forceinline__ void num_rank_rows(const NumArgs &a, int32_t lo, int maxWords, int vcap, int64_t vb) {
     extern __shared__ __align__(16) unsigned char smem[];
     using L = StageLayout<THREADS>;
     constexpr int NW = THREADS / 32;
@@ -1384,7 +1498,7 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
     int32_t *tbase = pre;
     uint32_t *tmask = reinterpret_cast<uint32_t *>(pre + THREADS);
     const int tid = threadIdx.x, lane = tid & 31;
-    const int32_t row = a.list[lo + blockIdx.x];
+    const int32_t row = a.list[lo + vb];
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     const int64_t expect = a.Cp[row + 1] - a.Cp[row];
     const int64_t obase = a.Cp[row] - a.outBase;
@@ -1508,6 +1622,22 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
     }
 }
 
+template <int THREADS, bool GLOBAL_ACC>
+__global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArgs a, int32_t lo, int maxWords, int vcap) {
+    num_rank_rows<THREADS, GLOBAL_ACC>(a, lo, maxWords, vcap, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+template <int THREADS, bool GLOBAL_ACC>
+__global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank_dd(NumArgs a, int bin, int maxWords, int vcap) {
+    const int32_t lo = a.binStart[bin], count = a.binStart[bin + 1] - lo;
+    for (int64_t vb = blockIdx.x; vb < count; vb += gridDim.x) {
+        num_rank_rows<THREADS, GLOBAL_ACC>(a, lo, maxWords, vcap, vb);
+        __syncthreads();
+    }
+}
+
 // Narrowest rows (window of at most kDenseWarpWords words): one warp per row
 // with a dense FP64 accumulator and a flag byte per column of the window in
 // shared memory.  Row-wise enumeration over strictly ascending B rows adds
@@ -1515,12 +1645,12 @@ __global__ void __launch_bounds__(THREADS, GLOBAL_ACC ? 3 : 1) k_num_rank(NumArg
 // (deterministic); otherwise atomic ones.  The flags give the columns in
 // order: no bitmap ranks, no sorting.
 template <int ROWS>
-__global__ void __launch_bounds__(32 * ROWS) k_num_densew(NumArgs a, int32_t lo, int32_t count) {
+__device__ __forceinline__ void num_densew_rows(const NumArgs &a, int32_t lo, int32_t count, int64_t vb) {
     constexpr int kCols = kDenseWarpWords * 32;
     __shared__ double vs[ROWS][kCols];
     __shared__ __align__(16) uint32_t fls[ROWS][kCols / 4];
     const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    const int64_t item = (int64_t)vb * ROWS + g;
     if (item >= count) return;
     double *vals = vs[g];
     uint32_t *fw = fls[g];
@@ -1619,17 +1749,33 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_densew(NumArgs a, int32_t lo,
     }
 }
 
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_num_densew(NumArgs a, int32_t lo, int32_t count) {
+    num_densew_rows<ROWS>(a, lo, count, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_num_densew_dd(NumArgs a, int bin) {
+    const int32_t lo = a.binStart[bin], count = a.binStart[bin + 1] - lo;
+    for (int64_t vb = blockIdx.x; vb * ROWS < count; vb += gridDim.x) {
+        num_densew_rows<ROWS>(a, lo, count, vb);
+        __syncthreads();
+    }
+}
+
 // Narrow rows (window of at most kWarpSpanWords words, at most kNumWarpMax
 // entries): one warp per row with the window's bitmap, word ranks and the
 // row's values in shared memory; the rank kernel's method at warp scale.
 template <int ROWS>
-__global__ void __launch_bounds__(32 * ROWS) k_num_rankw(NumArgs a, int32_t lo, int32_t count) {
+__device__ __forceinline__ void num_rankw_rows(const NumArgs &a, int32_t lo, int32_t count, int64_t vb) {
     static_assert(kWarpSpanWords == 64, "two bitmap words per lane");
     __shared__ uint32_t bms[ROWS][kWarpSpanWords];
     __shared__ int32_t wps[ROWS][kWarpSpanWords];
     __shared__ double vs[ROWS][kNumWarpMax];
     const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t item = (int64_t)blockIdx.x * ROWS + g;
+    const int64_t item = (int64_t)vb * ROWS + g;
     if (item >= count) return;
     uint32_t *bm = bms[g];
     int32_t *wp = wps[g];
@@ -1699,6 +1845,22 @@ __global__ void __launch_bounds__(32 * ROWS) k_num_rankw(NumArgs a, int32_t lo, 
     for (int64_t i = lane; i < nout; i += 32) a.Cv[obase + i] = vals[i];
 }
 
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_num_rankw(NumArgs a, int32_t lo, int32_t count) {
+    num_rankw_rows<ROWS>(a, lo, count, blockIdx.x);
+}
+
+// The same rows launched device-driven: the bin's rows from the bin table
+// on the device, covered by a grid-stride loop.
+template <int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_num_rankw_dd(NumArgs a, int bin) {
+    const int32_t lo = a.binStart[bin], count = a.binStart[bin + 1] - lo;
+    for (int64_t vb = blockIdx.x; vb * ROWS < count; vb += gridDim.x) {
+        num_rankw_rows<ROWS>(a, lo, count, vb);
+        __syncthreads();
+    }
+}
+
 // A segmented OR over runs of lanes that share a word that also marks, in a summary bitmap (one bit per word),
 // every word it finds zero.  All lanes call.
 __device__ __forceinline__ void or_bits_mark(uint32_t *bm, uint32_t *sum, bool v, uint32_t rel) {
@@ -1727,6 +1889,10 @@ __device__ __forceinline__ void or_bits_mark(uint32_t *bm, uint32_t *sum, bool v
 // entries, not its span.  No hash table, no sort.
 template <int ROWS>
 __global__ void __launch_bounds__(32 * ROWS) k_num_rankm(NumArgs a, int32_t lo, int32_t count) {
+    if (lo < 0) {  // device-driven: the bin's rows from the bin table
+        lo = a.binStart[NB_RANKM];
+        count = a.binStart[NB_RANKM + 1] - lo;
+    }
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int kSumWords = kMidSpanWords / 32;
     constexpr size_t kWarpBytes =
@@ -1896,6 +2062,10 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_num_rankwin(NumArgs
     for (int i = tid; i < WIN; i += THREADS) bits[i] = 0u;
     // With work items (heavy rows cut into pieces), the items the builder
     // wrote before this launch; otherwise the bin's rows.
+    if (lo < 0) {  // device-driven: the bin's rows from the bin table
+        lo = a.binStart[NB_DENSE];
+        count = a.binStart[NB_DENSE + 1] - lo;
+    }
     const int32_t nitems = a.items ? (int32_t)min(*(volatile uint32_t *)&a.ctr[CTR_ITEMS], (uint32_t)a.itemCap)
                                    : count;
     for (;;) {
@@ -2507,6 +2677,21 @@ void init_kernel_attributes() {
                          (int)kSmemDscr);
     cudaFuncSetAttribute(k_num_gdense<kGdenseThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(kSmemGdenseBase + 4 * (size_t)kGdenseSumMax));
+    // The device-driven forms of the same kernels.
+    cudaFuncSetAttribute(k_sym_hash_warp_dd<kSymWarpRows, kSymWarpTable>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemSymWarp);
+    cudaFuncSetAttribute(k_sym_hash_cta_dd<kSymCtaThreads, kSymCtaTable>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemSymCta);
+    cudaFuncSetAttribute(k_num_hash_warp_dd<kNumWarpRows, kNumWarpTable>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemNumWarp);
+    cudaFuncSetAttribute(k_num_hash_cta_dd<kNumCtaSThreads, kNumCtaSTable>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemNumCtaS);
+    cudaFuncSetAttribute(k_num_hash_cta_dd<kNumCtaLThreads, kNumCtaLTable>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemNumCtaL);
+    cudaFuncSetAttribute(k_num_rank_dd<kRankSThreads, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemRankSMax);
+    cudaFuncSetAttribute(k_num_rank_dd<kRankLThreads, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kSmemRankLMax);
 }
 
 // Loads every symbolic and numeric kernel of this file now.  CUDA loads
@@ -2591,10 +2776,170 @@ void launch_symbolic_bin(const SymArgs &a, int bin, int32_t begin, int32_t n, cu
     ++*launches;
 }
 
+// Resident CTAs of kernel fn on the whole GPU (the grid of a device-driven
+// launch, which strides over however many rows its bin holds).
+// The occupancy is looked up once per kernel and shared-memory size, so
+// that launches inside a stream capture query nothing.
+static int resident_grid(const void *fn, int threads, size_t smem, int sms) {
+    struct Entry {
+        const void *fn;
+        size_t smem;
+        int per_sm;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    for (const Entry &e : cache)
+        if (e.fn == fn && e.smem == smem) return e.per_sm * std::max(sms, 1);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    cache.push_back(Entry{fn, smem, per_sm});
+    return per_sm * std::max(sms, 1);
+}
+
+void launch_symbolic_bin_dd(const SymArgs &a, int bin, cudaStream_t s, int *launches) {
+    switch (bin) {
+        case SB_TINY: {
+            const void *fn = (const void *)k_sym_tiny_dd;
+            k_sym_tiny_dd<<<resident_grid(fn, 256, 0, a.numSms), 256, 0, s>>>(a, bin);
+            break;
+        }
+        case SB_BITW: {
+            const void *fn = (const void *)k_sym_flagw_dd<kBitwRows>;
+            k_sym_flagw_dd<kBitwRows><<<resident_grid(fn, 32 * kBitwRows, 0, a.numSms), 32 * kBitwRows, 0, s>>>(a, bin);
+            break;
+        }
+        case SB_HWARP: {
+            const void *fn = (const void *)k_sym_hash_warp_dd<kSymWarpRows, kSymWarpTable>;
+            k_sym_hash_warp_dd<kSymWarpRows, kSymWarpTable>
+                <<<resident_grid(fn, 32 * kSymWarpRows, kSmemSymWarp, a.numSms), 32 * kSymWarpRows, kSmemSymWarp, s>>>(
+                    a, bin);
+            break;
+        }
+        case SB_HCTA: {
+            const void *fn = (const void *)k_sym_hash_cta_dd<kSymCtaThreads, kSymCtaTable>;
+            k_sym_hash_cta_dd<kSymCtaThreads, kSymCtaTable>
+                <<<resident_grid(fn, kSymCtaThreads, kSmemSymCta, a.numSms), kSymCtaThreads, kSmemSymCta, s>>>(a, bin);
+            break;
+        }
+        case SB_WIDE: {
+            const int wb = wide_window_bits(a.B.n);
+            const size_t smem = kSmemWideBase + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb) + 4 * kWideThreads;
+            const int grid = resident_grid((const void *)k_sym_wide<kWideThreads>, kWideThreads, smem, a.numSms);
+            k_sym_wide<kWideThreads><<<(unsigned)grid, kWideThreads, smem, s>>>(a, -1, 0, wb);
+            break;
+        }
+        default:
+            return;
+    }
+    ++*launches;
+}
+
 void launch_adjoint(const AdjArgs &a, cudaStream_t s, int *launches) {
     if (a.nrows <= 0) return;
     k_adjoint<<<(unsigned)ceil_div(a.nrows, 8), 256, 0, s>>>(a);
     ++*launches;
+}
+
+// Device-driven numeric launch of bin `bin` (rows from a.binStart on the
+// device): persistent grids, the dense bin on rank windows without pieces.
+void launch_numeric_bin_dd(const NumArgs &a, int bin, cudaStream_t s, int *launches) {
+    switch (bin) {
+        case NB_TINY: {
+            k_num_tiny_dd<<<resident_grid((const void *)k_num_tiny_dd, 256, 0, a.numSms), 256, 0, s>>>(a, bin);
+            break;
+        }
+        case NB_HWARP: {
+            const void *fn = (const void *)k_num_hash_warp_dd<kNumWarpRows, kNumWarpTable>;
+            k_num_hash_warp_dd<kNumWarpRows, kNumWarpTable>
+                <<<resident_grid(fn, 32 * kNumWarpRows, kSmemNumWarp, a.numSms), 32 * kNumWarpRows, kSmemNumWarp, s>>>(
+                    a, bin);
+            break;
+        }
+        case NB_DENSEW: {
+            const void *fn = (const void *)k_num_densew_dd<kDensewRows>;
+            k_num_densew_dd<kDensewRows><<<resident_grid(fn, 32 * kDensewRows, 0, a.numSms), 32 * kDensewRows, 0, s>>>(
+                a, bin);
+            break;
+        }
+        case NB_RANKM: {
+            const int grid = std::max(a.numSms, 1) * 3;
+            k_num_rankm<kRankmRows><<<(unsigned)grid, 32 * kRankmRows, kSmemRankm, s>>>(a, -1, 0);
+            break;
+        }
+        case NB_RANKW: {
+            const void *fn = (const void *)k_num_rankw_dd<kRankwRows>;
+            k_num_rankw_dd<kRankwRows><<<resident_grid(fn, 32 * kRankwRows, 0, a.numSms), 32 * kRankwRows, 0, s>>>(
+                a, bin);
+            break;
+        }
+        case NB_RANKS: {
+            const size_t smem = smem_rank(kRankSThreads, a.tune.rankWordsMax, a.tune.rankSharedMax);
+            const void *fn = (const void *)k_num_rank_dd<kRankSThreads, false>;
+            k_num_rank_dd<kRankSThreads, false><<<resident_grid(fn, kRankSThreads, smem, a.numSms), kRankSThreads, smem,
+                                                  s>>>(a, bin, a.tune.rankWordsMax, a.tune.rankSharedMax);
+            break;
+        }
+        case NB_RANKL: {
+            const size_t smem = smem_rank(kRankLThreads, a.tune.rankWordsMax, 0);
+            const void *fn = (const void *)k_num_rank_dd<kRankLThreads, true>;
+            k_num_rank_dd<kRankLThreads, true><<<resident_grid(fn, kRankLThreads, smem, a.numSms), kRankLThreads, smem,
+                                                 s>>>(a, bin, a.tune.rankWordsMax, 0);
+            break;
+        }
+        case NB_HCTA_S: {
+            const void *fn = (const void *)k_num_hash_cta_dd<kNumCtaSThreads, kNumCtaSTable>;
+            k_num_hash_cta_dd<kNumCtaSThreads, kNumCtaSTable>
+                <<<resident_grid(fn, kNumCtaSThreads, kSmemNumCtaS, a.numSms), kNumCtaSThreads, kSmemNumCtaS, s>>>(a,
+                                                                                                               bin);
+            break;
+        }
+        case NB_HCTA_L: {
+            const void *fn = (const void *)k_num_hash_cta_dd<kNumCtaLThreads, kNumCtaLTable>;
+            k_num_hash_cta_dd<kNumCtaLThreads, kNumCtaLTable>
+                <<<resident_grid(fn, kNumCtaLThreads, kSmemNumCtaL, a.numSms), kNumCtaLThreads, kSmemNumCtaL, s>>>(a,
+                                                                                                               bin);
+            break;
+        }
+        case NB_DENSE: {
+            cudaMemsetAsync(a.ctr + CTR_NUM_RANKWIN, 0, sizeof(uint32_t), s);
+            const void *fn = (const void *)k_num_rankwin<kRankWinThreads, kRankWinWords>;
+            k_num_rankwin<kRankWinThreads, kRankWinWords>
+                <<<resident_grid(fn, kRankWinThreads, kSmemRankWin, a.numSms), kRankWinThreads, kSmemRankWin, s>>>(a, -1,
+                                                                                                              0);
+            break;
+        }
+        default:
+            return;
+    }
+    ++*launches;
+}
+
+// Looks up the grids of every device-driven launch for these thresholds and
+// B's column count ahead of any stream capture.
+void prepare_dd_grids(const Tuning &t, int64_t bcols, int sms) {
+    const int wb = wide_window_bits(bcols);
+    resident_grid((const void *)k_sym_tiny_dd, 256, 0, sms);
+    resident_grid((const void *)k_sym_flagw_dd<kBitwRows>, 32 * kBitwRows, 0, sms);
+    resident_grid((const void *)k_sym_hash_warp_dd<kSymWarpRows, kSymWarpTable>, 32 * kSymWarpRows, kSmemSymWarp, sms);
+    resident_grid((const void *)k_sym_hash_cta_dd<kSymCtaThreads, kSymCtaTable>, kSymCtaThreads, kSmemSymCta, sms);
+    resident_grid((const void *)k_sym_wide<kWideThreads>, kWideThreads,
+                  kSmemWideBase + (size_t)wb / 8 + 4 * (size_t)wide_touch_cap(wb) + 4 * kWideThreads, sms);
+    resident_grid((const void *)k_num_tiny_dd, 256, 0, sms);
+    resident_grid((const void *)k_num_hash_warp_dd<kNumWarpRows, kNumWarpTable>, 32 * kNumWarpRows, kSmemNumWarp, sms);
+    resident_grid((const void *)k_num_densew_dd<kDensewRows>, 32 * kDensewRows, 0, sms);
+    resident_grid((const void *)k_num_rankw_dd<kRankwRows>, 32 * kRankwRows, 0, sms);
+    resident_grid((const void *)k_num_rank_dd<kRankSThreads, false>, kRankSThreads,
+                  smem_rank(kRankSThreads, t.rankWordsMax, t.rankSharedMax), sms);
+    resident_grid((const void *)k_num_rank_dd<kRankLThreads, true>, kRankLThreads,
+                  smem_rank(kRankLThreads, t.rankWordsMax, 0), sms);
+    resident_grid((const void *)k_num_hash_cta_dd<kNumCtaSThreads, kNumCtaSTable>, kNumCtaSThreads, kSmemNumCtaS, sms);
+    resident_grid((const void *)k_num_hash_cta_dd<kNumCtaLThreads, kNumCtaLTable>, kNumCtaLThreads, kSmemNumCtaL, sms);
+    resident_grid((const void *)k_num_rankwin<kRankWinThreads, kRankWinWords>, kRankWinThreads, kSmemRankWin, sms);
+    resident_grid((const void *)k_num_rankm<kRankmRows>, 32 * kRankmRows, kSmemRankm, sms);
 }
 
 void launch_numeric_bin(const NumArgs &a, int bin, int32_t lo, int32_t hi, cudaStream_t s,

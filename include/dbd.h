@@ -305,6 +305,35 @@ int dbd_spgemm_batched(dbd_ctx *ctx, int64_t count, const dbd_csr_view *a, const
                        dbd_scope scope, int64_t *c_row_off, int64_t *c_nnz_off, dbd_csr_out *c,
                        dbd_stats *st);
 
+/* The batched multiply as device work a CUDA graph can hold: no host
+ * synchronisation and no allocation once planned.
+ *
+ * dbd_batch_plan fixes the batch's shapes -- count pairs of device-resident
+ * FP64 views (b == NULL: A_q * A_q), each pair's dimensions and entry counts
+ * -- and sizes everything for them, C with room for c_capacity entries.  The
+ * pairs' arrays must stay where they are; their contents (row pointers,
+ * columns, values: the sparsity pattern too) may change between runs as
+ * long as every count stays the same.
+ *
+ * dbd_batch_enqueue puts the whole multiply on `stream` (NULL: the
+ * context's): gathering the pairs' current contents, validating them, the
+ * per-row analysis, the symbolic bins, C's row pointers, the numeric bins
+ * and the pairs' entry offsets.  Every bin is launched device-driven (its
+ * rows counted on the device, a grid of resident CTAs striding over them),
+ * so nothing is read back: the call can be captured into a CUDA graph
+ * (cudaStreamBeginCapture ... cudaStreamEndCapture) and the graph replayed.
+ *
+ * dbd_batch_result, once the stream's work has completed, returns the
+ * status of the last run: DBD_ERR_INVALID for a malformed pair (the run then
+ * computed an empty product), DBD_ERR_BUDGET when nnz(C) exceeded
+ * c_capacity (no values were written), DBD_ERR_CUDA for a device table
+ * overflow; else C (device arrays owned by the context, as dbd_spgemm_batched
+ * returns them) and the pairs' row and entry offsets (host arrays of
+ * count + 1, either may be NULL). */
+int dbd_batch_plan(dbd_ctx *ctx, int64_t count, const dbd_csr_view *a, const dbd_csr_view *b, int64_t c_capacity);
+int dbd_batch_enqueue(dbd_ctx *ctx, void *stream);
+int dbd_batch_result(dbd_ctx *ctx, int64_t *c_row_off, int64_t *c_nnz_off, dbd_csr_out *c);
+
 /* ---- tuning (no reference counterpart) ------------------------------------ */
 
 /* Row-bin thresholds of the categoriser: which kernel (and so which table
