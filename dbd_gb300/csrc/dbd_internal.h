@@ -181,6 +181,7 @@ struct SymArgs {
     Tuning tune;
     int numSms = 0;  // persistent kernels size their grid by it; ctr holds their zeroed row counters
     int bSorted = 0; // B's rows have strictly ascending columns
+    const int *bUnsorted = nullptr;  // device-driven launches: the device's flag instead (nonzero: not ascending)
     // Slab counts of heavy rows (null: not recorded): heavySlot[row] = -1 or
     // the row's slot (taken from ctr[CTR_HEAVY], below heavyCap); slabCnt
     // holds kMaxSlabs counts per slot.
@@ -218,6 +219,7 @@ struct NumArgs {
     double *Cv;
     int32_t *state;       // 2 * nnz(A) scratch for the dense windows (cursor, next column)
     int bSorted;          // B's rows have ascending columns
+    const int *bUnsorted = nullptr;  // device-driven launches: the device's flag instead (nonzero: not ascending)
     int *err;
     const int64_t *rowP = nullptr;   // per-row products and column window (RowInfo)
     const int32_t *rowLo = nullptr;

@@ -246,14 +246,15 @@ namespace {
 // Fork the context's stream into per-bin streams and join them back.
 struct Fork {
     dbd_ctx *c;
+    cudaStream_t origin;
     cudaEvent_t start;
     bool used[kMaxBins] = {};
-    explicit Fork(dbd_ctx *ctx) : c(ctx) {
+    explicit Fork(dbd_ctx *ctx, cudaStream_t from = nullptr) : c(ctx), origin(from ? from : ctx->stream) {
         start = c->sync_ev();
-        cudaEventRecord(start, c->stream);
+        cudaEventRecord(start, origin);
     }
     cudaStream_t stream(int b) {
-        if (c->cfg.time_kernels) return c->stream;  // serial: per-kernel events time that kernel alone
+        if (c->cfg.time_kernels) return origin;  // serial: per-kernel events time that kernel alone
         if (!used[b]) cudaStreamWaitEvent(c->bin_streams[b], start, 0);
         used[b] = true;
         return c->bin_streams[b];
@@ -263,7 +264,7 @@ struct Fork {
             if (!used[b]) continue;
             cudaEvent_t e = c->sync_ev();
             cudaEventRecord(e, c->bin_streams[b]);
-            cudaStreamWaitEvent(c->stream, e, 0);
+            cudaStreamWaitEvent(origin, e, 0);
         }
     }
 };
@@ -1878,6 +1879,10 @@ int dbd_batch_plan(dbd_ctx *c, int64_t count, const dbd_csr_view *a, const dbd_c
     if (le == cudaSuccess) le = preload_batch_kernels();
     if (le != cudaSuccess) return cuda_fail(c, le, "loading the kernels");
     prepare_dd_grids(c->tune, colC[count], c->num_sms);
+    // The fork and join events of two forked phases, created now.
+    c->sused = 0;
+    for (int k = 0; k < 2 * (kMaxBins + 1); ++k) c->sync_ev();
+    c->sused = 0;
     c->bpSquare = square;
     c->bpCount = count;
     c->bpCap = c_capacity;
@@ -1936,9 +1941,17 @@ int dbd_batch_enqueue(dbd_ctx *c, void *stream) {
     sa.rowP = c->rowP.as<int64_t>();
     sa.tune = c->tune;
     sa.numSms = c->num_sms;
-    sa.bSorted = 0;  // not known on the host here: the general paths
+    sa.bSorted = 0;
+    sa.bUnsorted = flags + 2;  // B's sortedness as the device found it in this run
+    // Bins run concurrently, one stream each, forked from and joined to s
+    // (a capture follows the forks).
+    c->sused = 0;
     static const int sorder[] = {SB_WIDE, SB_HCTA, SB_HWARP, SB_BITW, SB_TINY};
-    for (int bin : sorder) launch_symbolic_bin_dd(sa, bin, s, &launches);
+    {
+        Fork fk(c, s);
+        for (int bin : sorder) launch_symbolic_bin_dd(sa, bin, fk.stream(bin), &launches);
+        fk.join();
+    }
     launch_row_scan(m, c->rowNnz.as<int32_t>(), c->part.as<int64_t>(), c->Cp.as<int64_t>(), s);
     launch_num_bins(m, A.ptr, row_info(c), c->rowNnz.as<int32_t>(), c->numBin.as<uint8_t>(), c->tune, s, c->num_sms);
     Binning nb{c->numBin.as<uint8_t>(), c->numList.as<int32_t>(), c->hist.as<int32_t>(), c->numTileOff.as<int32_t>(),
@@ -1957,6 +1970,7 @@ int dbd_batch_enqueue(dbd_ctx *c, void *stream) {
     na.Cv = c->Cv.as<double>();
     na.state = c->cursor.as<int32_t>();
     na.bSorted = 0;
+    na.bUnsorted = flags + 2;
     na.err = c->err.as<int>();
     na.rowP = c->rowP.as<int64_t>();
     na.rowLo = c->rowLo.as<int32_t>();
@@ -1968,7 +1982,11 @@ int dbd_batch_enqueue(dbd_ctx *c, void *stream) {
     na.ctr = c->ctrs.as<uint32_t>();
     static const int norder[] = {NB_DENSE, NB_RANKL, NB_HCTA_L, NB_RANKS, NB_HCTA_S,
                                  NB_HWARP, NB_RANKM, NB_RANKW, NB_DENSEW, NB_TINY};
-    for (int bin : norder) launch_numeric_bin_dd(na, bin, s, &launches);
+    {
+        Fork fk(c, s);
+        for (int bin : norder) launch_numeric_bin_dd(na, bin, fk.stream(bin), &launches);
+        fk.join();
+    }
     launch_gather_i64(c->Cp.as<int64_t>(), drow, (int64_t)n1, dCoff, s);
     CK(c, cudaGetLastError());
     c->launches = launches + 10;

@@ -319,6 +319,13 @@ __device__ __forceinline__ int32_t stage_entries(const CsrDev &A, const CsrDev &
     return total;
 }
 
+// B's rows ascend strictly: the host's flag, or for a device-driven launch
+// the flag the device computed for this run (bUnsorted).
+template <class Args>
+__device__ __forceinline__ bool b_sorted(const Args &a) {
+    return a.bUnsorted ? *a.bUnsorted == 0 : a.bSorted != 0;
+}
+
 // Largest i in [0, nb) with pre[i] <= t.
 __device__ __forceinline__ int find_entry(const int32_t *pre, int nb, int32_t t) {
     int lo = 0, hi = nb - 1;
@@ -761,7 +768,7 @@ __global__ void __launch_bounds__(THREADS) k_sym_wide(SymArgs a, int32_t begin, 
         int cnt = 0;
         // Rows over several windows enumerate, per window, only the part of
         // each B row inside it (B's rows ascending).
-        const bool clip = a.bSorted && end - base > (int64_t)winBits;
+        const bool clip = b_sorted(a) && end - base > (int64_t)winBits;
         const bool once = e1 - e0 <= THREADS;  // one batch: its cursors carry over the windows
         for (int64_t c_lo = base; c_lo < end; c_lo += winBits) {
             const int words = (int)min((int64_t)winBits, end - c_lo + 31) >> 5;
@@ -948,7 +955,7 @@ __device__ __forceinline__ void sym_flagw_rows(const SymArgs &a, int32_t begin, 
     const bool rowwise = a.rowP[row] >= (int64_t)kRowwiseMinLen * (e1 - e0);
     int *err = a.err;
     const int32_t *bidx = a.B.idx;
-    if (rowwise && a.bSorted) {
+    if (rowwise && b_sorted(a)) {
         int cnt;
         if (interval_union_count(a.A, a.B, e0, e1, lane, &cnt)) {
             if (lane == 0) a.rowNnz[row] = cnt;
@@ -980,7 +987,7 @@ __device__ __forceinline__ void sym_flagw_rows(const SymArgs &a, int32_t begin, 
                 const int32_t first = __shfl_sync(FULL, fc, q), last = __shfl_sync(FULL, lc, q);
                 if (lq == 0) continue;
                 const uint32_t r0 = (uint32_t)(first - base), r1 = (uint32_t)(last - base);
-                if (a.bSorted && last - first == lq - 1 && r0 < nb && r1 < nb) {
+                if (b_sorted(a) && last - first == lq - 1 && r0 < nb && r1 < nb) {
                     for (uint32_t w = (r0 >> 2) + lane; w <= (r1 >> 2); w += 32) {
                         uint32_t m = 0x01010101u;
                         if (w == (r0 >> 2)) m &= 0xffffffffu << (8 * (r0 & 3));
@@ -1668,7 +1675,7 @@ __device__ __forceinline__ void num_densew_rows(const NumArgs &a, int32_t lo, in
     __syncwarp();
     const int32_t e0 = a.A.ptr[row], e1 = a.A.ptr[row + 1];
     const bool rowwise = a.rowP[row] >= (int64_t)kRowwiseMinLen * (e1 - e0);
-    const bool plain = rowwise && a.bSorted;
+    const bool plain = rowwise && b_sorted(a);
     int *err = a.err;
     const int32_t *bidx = a.B.idx;
     const double *bval = a.B.val;
@@ -2005,7 +2012,7 @@ __global__ void __launch_bounds__(256) k_dense_items(NumArgs a, int32_t lo, int3
         }
         a.items[k] = DenseItem{row, (int16_t)s0, (int16_t)s1, cnt, off};
     };
-    if (sl < 0 || !a.bSorted || nnz <= kPieceNnz) {
+    if (sl < 0 || !b_sorted(a) || nnz <= kPieceNnz) {
         put(-1, -1, (int32_t)min(nnz, (int64_t)INT32_MAX), 0);
         return;
     }
@@ -2093,7 +2100,7 @@ __global__ void __launch_bounds__(THREADS, 1024 / THREADS) k_num_rankwin(NumArgs
         }
         // Rows over several windows and pieces enumerate, per window, only
         // the part of each B row inside it (B's rows ascending).
-        const bool clip = a.bSorted && (it.s0 >= 0 || end - start > (int64_t)WIN * 32);
+        const bool clip = b_sorted(a) && (it.s0 >= 0 || end - start > (int64_t)WIN * 32);
         for (int64_t c_lo = start; c_lo < end; c_lo += (int64_t)WIN * 32) {
             const int nwords = (int)min((int64_t)WIN, (end - c_lo + 31) >> 5);
             const uint32_t nbits = (uint32_t)nwords * 32u;
@@ -2231,7 +2238,7 @@ __global__ void __launch_bounds__(THREADS) k_num_dscr(NumArgs a, int32_t lo, int
         const int32_t shift = col_shift(a, row);
         const int64_t end = (int64_t)a.rowHi[row] + 1;
         const int64_t start = (int64_t)(a.rowLo[row] >> 5) << 5;
-        const bool clip = a.bSorted && end - start > (int64_t)WIN * 32;
+        const bool clip = b_sorted(a) && end - start > (int64_t)WIN * 32;
         int64_t run = 0;
         for (int64_t c_lo = start; c_lo < end; c_lo += (int64_t)WIN * 32) {
             const int nwords = (int)min((int64_t)WIN, (end - c_lo + 31) >> 5);
