@@ -538,6 +538,60 @@ def run_batched(args, local):
     return 0
 
 
+def run_mtx(args, local):
+    """The input conversion (a side line, not the multiply's metric): R-MAT
+    scale `mtx<scale>` (edge factor 8, seed 0) written as Matrix Market text
+    with its entries shuffled, converted to CSR (and the .csr cache) on the
+    GPU (dbd_read_csr_gpu) and on the host (dbd_read_csr, the reference's
+    rules), wall time per conversion from the file."""
+    import dbd_gb300 as dbd
+    from dbd_gb300 import generators as gen
+    scale = int(args.workload[3:] or 20)
+    A = gen.rmat(scale, 8, seed=0)
+    rows = np.repeat(np.arange(A.n_rows), np.diff(A.row_ptr)) + 1
+    perm = np.random.default_rng(0).permutation(A.nnz)
+    tmp = tempfile.mkdtemp(prefix="dbd_mtx_", dir=ROOT)
+    try:
+        src = os.path.join(tmp, "m.mtx")
+        with open(src, "w") as f:
+            f.write("%%MatrixMarket matrix coordinate real general\n")
+            f.write(f"{A.n_rows} {A.n_cols} {A.nnz}\n")
+            for s0 in range(0, A.nnz, 1 << 20):
+                idx = perm[s0:s0 + (1 << 20)]
+                f.write("".join(f"{a} {b} {v:.9g}\n" for a, b, v in zip(rows[idx], A.col_idx[idx] + 1, A.val[idx])))
+        size = os.path.getsize(src)
+
+        def convert(gpu, k):
+            path = os.path.join(tmp, f"c{k}.mtx")
+            shutil.copy(src, path)
+            t0 = time.perf_counter()
+            M = dbd.read_CSR(path, gpu=local if gpu else None)
+            t = time.perf_counter() - t0
+            # 1-based indices kept as they are: row 0 stays empty (the reference's rule).
+            assert M.nnz == A.nnz and np.array_equal(M.row_ptr[1:], A.row_ptr)
+            os.remove(path)
+            os.remove(path + ".csr")
+            return t
+        for k in range(args.warmup):
+            convert(True, k)
+        tg = [convert(True, 100 + k) for k in range(args.steps)]
+        th = convert(False, 999)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    t = float(np.mean(tg))
+    line = {"metric": "Matrix Market text to CSR (file to CSR and .csr cache)", "value": round(size / t / 1e9, 4),
+            "unit": "GB/s of text", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t * 1e3, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "text -> int32/float32", "data": "synthetic (seeded R-MAT, numpy PCG64)",
+            "config": {"workload": f"R-MAT scale {scale}, edge factor 8, seed 0, entries shuffled, values %.9g",
+                       "entries": int(A.nnz), "text_bytes": size},
+            "cpu_baseline": {"value": round(size / th / 1e9, 4), "unit": "GB/s of text", "cores": 1,
+                             "kind": "port", "sample": "the whole file through dbd_read_csr (the host conversion)"},
+            "speedup_vs_host": round(th / t, 2)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_adjoint(args, local):
     """Forward + adjoint of C = A*B, A and B 100,000 x 100,000 with 16
     uniform columns per row and N(0,1) values, loss = sum(W * C) with W ~
@@ -1004,6 +1058,8 @@ def main():
         if rank != 0:
             return 0
         return run_adjoint(args, local)
+    if args.workload.startswith("mtx"):
+        return 0 if rank != 0 else run_mtx(args, local)
 
     import torch
     import dbd_gb300 as dbd
