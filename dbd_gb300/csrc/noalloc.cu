@@ -156,6 +156,15 @@ extern "C" int dbd_spgemm_noalloc(const dbd_csr_view *a, const dbd_csr_view *b, 
     int rc = device_scratch(dev, &base);
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream_handle;
+    // The call synchronises with the host twice (bin sizes, nnz(C)), which a
+    // stream capture cannot hold: refuse it before anything is enqueued.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusNone;
+    }
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(DBD_ERR_INVALID, "the stream is capturing: this call synchronises and cannot be captured");
     Carver c{base};  // the layout of scratch_bytes()
     const size_t nt = (size_t)ceil_div(m, kTileRows) + 1;
     int32_t *bmin = c.take<int32_t>((size_t)b->n_rows);

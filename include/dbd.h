@@ -500,8 +500,11 @@ void dbd_writer_close(dbd_writer *w);
  * 55 bytes per row) -- are rejected with DBD_ERR_BUDGET.  The first call on a
  * device sets that device up (its kernel attributes, the loading of every
  * kernel the pipeline launches, and the array's device address), so make the
- * first call on each device before any stream capture and before reserving
- * the device's memory.
+ * first call on each device before reserving the device's memory.
+ * The call reads bin sizes and nnz(C) back to the host, so it cannot be
+ * captured into a CUDA graph: on a capturing stream it returns
+ * DBD_ERR_INVALID before enqueueing anything (dbd_batch_plan /
+ * dbd_batch_enqueue is the capturable form).
  * All calls share the array: calls that overlap on the GPU (other threads or
  * streams) race and must be serialised by the caller.  On failure the
  * message is printed to stderr. */

@@ -9,7 +9,8 @@ second call starts from the first call's leftovers in that array) give the
 same product as the regular entry point dbd_spgemm, within the tolerance of
 the other parity tests, that an input too large for the array is refused, and
 that after its first call on the device (the set-up) further calls whose rows
-land in different kernel bins leave the device's free memory unchanged.
+land in different kernel bins leave the device's free memory unchanged, and
+that a call on a stream being captured is refused before it enqueues work.
 It is collected last so that a failure here stops a -x run only after every
 other test ran; it also passes on its own in a fresh process.
 """
@@ -126,3 +127,30 @@ def test_noalloc_allocates_nothing_after_setup():
     for i in (1, 2, 0, 2):
         assert call(i) == 0
     assert torch.cuda.mem_get_info()[0] == free0
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The call reads sizes back to the host, so on a stream being captured it
+    returns DBD_ERR_INVALID before enqueueing anything; the capture itself
+    stays valid and the stream works afterwards."""
+    torch = pytest.importorskip("torch")
+    lib = _ffi.load()
+    A = gen.laplacian_2d(32)
+    rc, n, _, _, _ = noalloc_multiply(torch, lib, A, capacity=1 << 16)  # device set up
+    assert rc == 0
+    va, keep = device_view(torch, A)
+    cp = torch.empty(A.n_rows + 1, dtype=torch.int64, device="cuda")
+    ci = torch.empty(n, dtype=torch.int32, device="cuda")
+    cv = torch.empty(n, dtype=torch.float64, device="cuda")
+    nnz = C.c_int64(-1)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        rc = lib.dbd_spgemm_noalloc(C.byref(va), None, C.c_void_p(cp.data_ptr()), C.c_void_p(ci.data_ptr()),
+                                    C.c_void_p(cv.data_ptr()), n, C.byref(nnz), C.c_void_p(s.cuda_stream))
+        cp.zero_()  # the capture holds something
+    assert rc == -1  # DBD_ERR_INVALID
+    g.replay()
+    torch.cuda.synchronize()
+    rc2, n2, _, _, _ = noalloc_multiply(torch, lib, A, capacity=1 << 16)
+    assert rc2 == 0 and n2 == n
