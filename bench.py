@@ -654,6 +654,12 @@ def run_adjoint(args, local):
                                                C_.c_void_p(gA.data_ptr()), C_.c_void_p(gB.data_ptr()), 1, 0),
                    ctx.handle)
     t_adj = timed(adjoint, args.steps, args.warmup)
+
+    def adjoint_det():
+        dbd._check(ctx._lib.dbd_spgemm_adjoint(ctx.handle, C_.byref(va), C_.byref(vb), C_.c_void_p(W.data_ptr()),
+                                               C_.c_void_p(gA.data_ptr()), C_.c_void_p(gB.data_ptr()), 1, 2),
+                   ctx.handle)
+    t_det = timed(adjoint_det, args.steps, args.warmup)
     # New values on the same patterns: the numeric graph replayed.
     ctx.spgemm(dA, dB, scope="kernel", fetch=False)
     nA = torch.from_numpy(rng.standard_normal(A.nnz)).to(dev)
@@ -705,6 +711,10 @@ def run_adjoint(args, local):
                                      "peak_kind": f"of {peak_kind}",
                                      "fp64_tflops": round(4 * P / t_adj / 1e12, 4), "fp64_peak": round(fpk, 4),
                                      "fp64_frac": round(4 * P / t_adj / 1e12 / fpk, 4)}},
+            "adjoint_deterministic": {"gflops": g(4 * P, t_det), "ms": round(t_det * 1e3, 3),
+                                      "what": "the same with flags DBD_ADJ_DETERMINISTIC: dB by its own pass "
+                                              "over B's pattern (A grouped by column, one lane per entry of B), "
+                                              "identical bits run to run"},
             "forward_plus_adjoint": {"ms": round((t_fwd + t_adj) * 1e3, 3),
                                      "gflops": g(6 * P, t_fwd + t_adj),
                                      "adjoint_over_forward_time": round(t_adj / t_fwd, 3)},

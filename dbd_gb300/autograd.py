@@ -41,7 +41,7 @@ class Pattern:
 
 class _SpGEMM(torch.autograd.Function):
     @staticmethod
-    def forward(fctx, a_val, b_val, pat, engine, keep_pattern):
+    def forward(fctx, a_val, b_val, pat, engine, keep_pattern, deterministic):
         a_val = a_val.detach().contiguous()
         b_val = b_val.detach().contiguous()
         lib = engine._lib
@@ -60,6 +60,7 @@ class _SpGEMM(torch.autograd.Function):
         fctx.pat = pat
         fctx.engine = engine
         fctx.keep = keep_pattern
+        fctx.det = deterministic
         return c_val
 
     @staticmethod
@@ -72,13 +73,16 @@ class _SpGEMM(torch.autograd.Function):
         va, vb = pat.views(a_val, b_val)
         engine.set_stream(torch.cuda.current_stream().cuda_stream)
         _check(engine._lib.dbd_spgemm_adjoint(engine.handle, C.byref(va), C.byref(vb), g.data_ptr(), da.data_ptr(),
-                                              db.data_ptr(), 1, 0 if fctx.keep else 1), engine.handle)
-        return da, db, None, None, None
+                                              db.data_ptr(), 1, (0 if fctx.keep else 1) | (2 if fctx.det else 0)),
+               engine.handle)
+        return da, db, None, None, None, None
 
 
-def spgemm(a_val, b_val, pat, engine, keep_pattern=True):
-    """C's values (FP64, on C's pattern, which is left in pat.c_ptr / pat.c_idx)."""
-    return _SpGEMM.apply(a_val, b_val, pat, engine, keep_pattern)
+def spgemm(a_val, b_val, pat, engine, keep_pattern=True, deterministic=False):
+    """C's values (FP64, on C's pattern, which is left in pat.c_ptr / pat.c_idx).
+    deterministic=True computes dB by its own pass over B's pattern (run-to-run
+    identical gradients) instead of reductions from A's rows."""
+    return _SpGEMM.apply(a_val, b_val, pat, engine, keep_pattern, deterministic)
 
 
 def engine(device=0, gpu_gib=64.0):

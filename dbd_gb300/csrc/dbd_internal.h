@@ -283,6 +283,32 @@ struct AdjArgs {
     int *err;
 };
 void launch_adjoint(const AdjArgs &a, cudaStream_t s, int *launches);
+// dB = mask_B(A^T G) on its own: one warp per row k of B, each lane one
+// entry (k, j), summing A(i,k) * G(i,j) over column k of A in row order
+// (colPtr / perm / rowOf: A's entries grouped by column, stably).
+struct AdjDbArgs {
+    CsrDev B;
+    const double *Aval;
+    const int32_t *colPtr;  // A.n + 1
+    const uint32_t *perm;   // A's entry indices by column, rows ascending
+    const int32_t *rowOf;   // row of each A entry
+    const int64_t *Cp;
+    const int32_t *Ci;
+    const double *G;
+    double *dB;
+    int *err;
+};
+// Entry rows and the column grouping of A for launch_adjoint_db (keys and
+// vals: two pairs of nnz(A) uint32 buffers; scratch: stable_sort_scratch_bytes).
+void launch_adjoint_transpose(const CsrDev &A, int32_t *rowOf, uint32_t *keys0, uint32_t *vals0, uint32_t *keys1,
+                              uint32_t *vals1, void *scratch, int32_t *colPtr, const uint32_t **perm, cudaStream_t s);
+void launch_adjoint_db(const AdjDbArgs &a, cudaStream_t s);
+// Stable LSD radix sort of (key, value) pairs by the low `bits` of the key
+// (k_mtx.cu): k0/v0 in, k1/v1 scratch; *keys / *vals receive whichever pair
+// holds the result.
+int64_t stable_sort_scratch_bytes(int64_t n);
+void launch_stable_sort_u32(uint32_t *k0, uint32_t *v0, uint32_t *k1, uint32_t *v1, int64_t n, int bits,
+                            void *scratch, cudaStream_t s, uint32_t **keys, uint32_t **vals);
 
 // ---- batched products (k_batch.cu) ----
 // One operand of one pair and its place in the concatenated operand.

@@ -154,6 +154,7 @@ struct dbd_ctx {
     bool patternOk = false;
     int64_t patA = -1, patB = -1;
     DevBuf adjG, adjA, adjB;    // device copies for host-side adjoint arguments
+    DevBuf adjT;                // A grouped by column for the deterministic dB pass
     // Batched products: the pairs' placement (device copy of the pair
     // descriptors and offsets, staged through pinned memory), the per-row
     // column shift of the concatenated A, and the pair count of the last
@@ -1319,7 +1320,7 @@ void dbd_destroy(dbd_ctx *c) {
                       &c->rowP, &c->symBin, &c->numBin, &c->rowNnz, &c->symList, &c->numList, &c->hist,
                       &c->symTileOff, &c->numTileOff, &c->symStart, &c->numStart, &c->part, &c->Cp, &c->cursor,
                       &c->err, &c->blockP, &c->flags, &c->Ci, &c->Cv, &c->wideBits, &c->wideSlot, &c->adjG,
-                      &c->adjA, &c->adjB, &c->rowLo, &c->rowHi, &c->A.bmin, &c->A.bmax, &c->B.bmin, &c->B.bmax,
+                      &c->adjA, &c->adjB, &c->adjT, &c->rowLo, &c->rowHi, &c->A.bmin, &c->A.bmax, &c->B.bmin, &c->B.bmax,
                       &c->ctrs, &c->gdense, &c->dgCount, &c->dgCol, &c->dgVal, &c->dgSum, &c->dgWsum,
                       &c->dgBad, &c->hashOut, &c->dscr, &c->heavySlot, &c->slabCnt,
                       &c->items})
@@ -1540,8 +1541,11 @@ int dbd_spgemm(dbd_ctx *c, const dbd_csr_view *a, const dbd_csr_view *b, dbd_sco
 }
 
 int dbd_spgemm_adjoint(dbd_ctx *c, const dbd_csr_view *a, const dbd_csr_view *b, const double *g, double *da,
-                       double *db, int on_device, int recompute_pattern) {
-    if (!c || !a || !g || !da || !db) return DBD_ERR_INVALID;
+                       double *db, int on_device, int flags) {
+    if (!c || !a || !g || !da || !db || (flags & ~(DBD_ADJ_RECOMPUTE | DBD_ADJ_DETERMINISTIC)))
+        return DBD_ERR_INVALID;
+    const bool recompute_pattern = (flags & DBD_ADJ_RECOMPUTE) != 0;
+    const bool det = (flags & DBD_ADJ_DETERMINISTIC) != 0;
     cudaSetDevice(c->cfg.device);
     const dbd_csr_view *bb = (b && b != a) ? b : a;
     const bool have = c->patternOk && c->m == a->n_rows && c->ncols == bb->n_cols && c->patA == a->nnz &&
@@ -1586,12 +1590,43 @@ int dbd_spgemm_adjoint(dbd_ctx *c, const dbd_csr_view *a, const dbd_csr_view *b,
     aa.Ci = c->Ci.as<int32_t>();
     aa.G = dG;
     aa.dA = dA;
-    aa.dB = dB;
+    aa.dB = det ? nullptr : dB;  // deterministic: dB by its own pass below
     aa.order = c->numList.as<int32_t>();
     aa.nrows = c->m;
     aa.err = c->err.as<int>();
     int launches = 0;
     launch_adjoint(aa, c->stream, &launches);
+    if (det && B.nnz > 0) {
+        // A grouped by column (stably, so rows ascend in every column), then
+        // one lane per entry of B.
+        const size_t na = (size_t)std::max<int64_t>(A.nnz, 1);
+        const size_t sortB = (size_t)stable_sort_scratch_bytes(A.nnz);
+        const size_t colB = sizeof(int32_t) * (size_t)(A.n + 1);
+        auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
+        CK(c, c->adjT.ensure(5 * up16(4 * na) + up16(colB) + sortB));
+        char *p = c->adjT.as<char>();
+        int32_t *rowOf = reinterpret_cast<int32_t *>(p);
+        uint32_t *k0 = reinterpret_cast<uint32_t *>(p + up16(4 * na));
+        uint32_t *v0 = reinterpret_cast<uint32_t *>(p + 2 * up16(4 * na));
+        uint32_t *k1 = reinterpret_cast<uint32_t *>(p + 3 * up16(4 * na));
+        uint32_t *v1 = reinterpret_cast<uint32_t *>(p + 4 * up16(4 * na));
+        int32_t *colPtr = reinterpret_cast<int32_t *>(p + 5 * up16(4 * na));
+        void *scratch = p + 5 * up16(4 * na) + up16(colB);
+        const uint32_t *perm = nullptr;
+        launch_adjoint_transpose(A, rowOf, k0, v0, k1, v1, scratch, colPtr, &perm, c->stream);
+        AdjDbArgs ab;
+        ab.B = B;
+        ab.Aval = A.val;
+        ab.colPtr = colPtr;
+        ab.perm = perm;
+        ab.rowOf = rowOf;
+        ab.Cp = c->Cp.as<int64_t>();
+        ab.Ci = c->Ci.as<int32_t>();
+        ab.G = dG;
+        ab.dB = dB;
+        ab.err = c->err.as<int>();
+        launch_adjoint_db(ab, c->stream);
+    }
     CK(c, cudaGetLastError());
     if (!on_device) {
         if (A.nnz > 0)

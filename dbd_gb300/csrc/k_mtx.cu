@@ -275,6 +275,32 @@ bool host_piece(const char *b, int64_t n, int64_t &pos, int64_t &p0, int64_t &p1
 
 }  // namespace
 
+int64_t stable_sort_scratch_bytes(int64_t n) {
+    const int64_t tiles = std::max<int64_t>((n + kSortTile - 1) / kSortTile, 1);
+    const int64_t parts = (256 * tiles + kScanTile - 1) / kScanTile + 2;
+    return 4 * 256 * tiles + 8 * (256 * tiles + 1) + 8 * parts + 64;
+}
+
+void launch_stable_sort_u32(uint32_t *k0, uint32_t *v0, uint32_t *k1, uint32_t *v1, int64_t n, int bits,
+                            void *scratch, cudaStream_t s, uint32_t **keys, uint32_t **vals) {
+    const int64_t tiles = std::max<int64_t>((n + kSortTile - 1) / kSortTile, 1);
+    char *p = static_cast<char *>(scratch);
+    int32_t *hist = reinterpret_cast<int32_t *>(p);
+    p += (4 * 256 * tiles + 15) / 16 * 16;
+    int64_t *off = reinterpret_cast<int64_t *>(p);
+    p += (8 * (256 * tiles + 1) + 15) / 16 * 16;
+    int64_t *part = reinterpret_cast<int64_t *>(p);
+    for (int shift = 0; shift < bits && n > 0; shift += 8) {
+        k_sort_hist<<<(unsigned)tiles, 32, 0, s>>>(k0, n, shift, hist, tiles);
+        launch_row_scan(256 * tiles, hist, part, off, s);
+        k_sort_scatter<<<(unsigned)tiles, 32, 0, s>>>(k0, v0, k1, v1, n, shift, off, tiles);
+        std::swap(k0, k1);
+        std::swap(v0, v1);
+    }
+    *keys = k0;
+    *vals = v0;
+}
+
 int convert_matrix_file_gpu(const std::string &path, int device, dbd_csr_host *m, std::string *err) {
     memset(m, 0, sizeof(*m));
     MTX_CK(cudaSetDevice(device), "set device");

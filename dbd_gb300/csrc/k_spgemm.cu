@@ -2601,7 +2601,7 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
                 if (q < c1) {
                     const double g = a.G[q];
                     ga = __dmul_rn(g, a.B.val[pos]);
-                    atomicAdd(&a.dB[pos], __dmul_rn(av, g));
+                    if (a.dB) atomicAdd(&a.dB[pos], __dmul_rn(av, g));
                 } else {
                     raise(a.err, DEV_COUNT_MISMATCH);
                 }
@@ -2617,6 +2617,59 @@ __global__ void __launch_bounds__(256) k_adjoint(AdjArgs a) {
             const int pk = __shfl_up_sync(FULL, key, 1);
             if (valid && (lane == 0 || pk != key)) atomicAdd(&a.dA[e + o], ga);
         }
+    }
+}
+
+// Each A entry's row, and (column, entry) pairs to sort: one warp per row.
+__global__ void __launch_bounds__(256) k_entry_rows(CsrDev A, int32_t *rowOf, uint32_t *keys, uint32_t *vals) {
+    const int lane = threadIdx.x & 31;
+    const int64_t r = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (r >= A.m) return;
+    for (int32_t e = A.ptr[r] + lane; e < A.ptr[r + 1]; e += 32) {
+        rowOf[e] = (int32_t)r;
+        keys[e] = (uint32_t)A.idx[e];
+        vals[e] = (uint32_t)e;
+    }
+}
+
+// Column pointers from the entries sorted by column: column c starts at the
+// first entry whose column is >= c.
+__global__ void __launch_bounds__(256) k_col_ptr(const uint32_t *__restrict__ cols, int64_t n, int64_t ncols,
+                                                 int32_t *__restrict__ colPtr) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t lo = i == 0 ? 0 : (int64_t)cols[i - 1] + 1;
+        const int64_t hi = i == n ? ncols : (int64_t)cols[i];
+        for (int64_t c = lo; c <= hi; ++c) colPtr[c] = (int32_t)i;
+    }
+}
+
+// dB = mask_B(A^T G) as its own pass over B's pattern: one warp per row k of
+// B, one lane per entry (k, j); the lane sums A(i,k) * G(i,j) over column k
+// of A in row order, each G(i,j) found in C's sorted row i.  Every entry is
+// summed by one lane in a fixed order: run-to-run identical.
+__global__ void __launch_bounds__(256) k_adjoint_db(AdjDbArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int64_t k = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (k >= a.B.m) return;
+    const int32_t f0 = a.B.ptr[k], f1 = a.B.ptr[k + 1];
+    const int32_t p0 = a.colPtr[k], p1 = a.colPtr[k + 1];
+    for (int32_t fb = f0; fb < f1; fb += 32) {
+        const int32_t f = fb + lane;
+        const bool valid = f < f1;
+        const int32_t j = valid ? a.B.idx[f] : 0;
+        double acc = 0.0;
+        for (int32_t p = p0; p < p1; ++p) {
+            const uint32_t e = a.perm[p];
+            const int32_t i = a.rowOf[e];
+            const double av = a.Aval[e];
+            const int64_t c0 = a.Cp[i], c1 = a.Cp[i + 1];
+            if (valid) {
+                const int64_t q = find_col(a.Ci, c0, c1, j);
+                if (q < c1) acc += __dmul_rn(av, a.G[q]);
+                else raise(a.err, DEV_COUNT_MISMATCH);
+            }
+        }
+        if (valid) a.dB[f] = acc;
     }
 }
 
@@ -2843,6 +2896,23 @@ void launch_symbolic_bin_dd(const SymArgs &a, int bin, cudaStream_t s, int *laun
             return;
     }
     ++*launches;
+}
+
+void launch_adjoint_transpose(const CsrDev &A, int32_t *rowOf, uint32_t *keys0, uint32_t *vals0, uint32_t *keys1,
+                              uint32_t *vals1, void *scratch, int32_t *colPtr, const uint32_t **perm, cudaStream_t s) {
+    if (A.m > 0) k_entry_rows<<<(unsigned)ceil_div(A.m, 8), 256, 0, s>>>(A, rowOf, keys0, vals0);
+    int bits = 0;
+    while (bits < 32 && ((uint64_t)std::max<int64_t>(A.n - 1, 0) >> bits) != 0) ++bits;
+    uint32_t *ks = keys0, *vs = vals0;
+    launch_stable_sort_u32(keys0, vals0, keys1, vals1, A.nnz, bits, scratch, s, &ks, &vs);
+    const int64_t grid = std::min<int64_t>(ceil_div(A.nnz + 1, 256), 65535);
+    k_col_ptr<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, s>>>(ks, A.nnz, A.n, colPtr);
+    *perm = vs;
+}
+
+void launch_adjoint_db(const AdjDbArgs &a, cudaStream_t s) {
+    if (a.B.m <= 0) return;
+    k_adjoint_db<<<(unsigned)ceil_div(a.B.m, 8), 256, 0, s>>>(a);
 }
 
 void launch_adjoint(const AdjArgs &a, cudaStream_t s, int *launches) {

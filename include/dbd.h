@@ -269,16 +269,28 @@ void dbd_csr_free(dbd_csr_out *c);
  * and B over their fixed patterns:  dA = mask_A(G * B^T),
  * dB = mask_B(A^T * G), where g holds G = dL/dC on C's pattern in the order
  * of the product's col_idx (nnz(C) values).  The reference has no
- * differentiation; this is the benchmark spec's adjoint pair, done as one
- * SDDMM-style kernel over A's rows in the forward's numeric row order.
+ * differentiation; this is the benchmark spec's adjoint pair: by default one
+ * SDDMM-style kernel over A's rows in the forward's numeric row order, or
+ * (DBD_ADJ_DETERMINISTIC) that kernel for dA and a second SDDMM over B's
+ * pattern for dB.
  *
  * C's pattern is the one the last multiply on this context left on the
- * device (DBD_SCOPE_KERNEL, resident).  recompute_pattern = 1 recomputes it
- * from a and b instead, for callers that dropped it to save memory.
- * on_device = 1: g, da, db are device pointers; 0: host arrays.  da has
- * nnz(A) entries, db nnz(B); both are overwritten. */
+ * device (DBD_SCOPE_KERNEL, resident).  flags:
+ *   DBD_ADJ_RECOMPUTE      recompute C's pattern from a and b instead, for
+ *                          callers that dropped it to save memory;
+ *   DBD_ADJ_DETERMINISTIC  dB by a pass of its own over B's pattern (A
+ *                          grouped by column on the device, one lane per
+ *                          entry of B summing in row order): run-to-run
+ *                          identical, where the default adds each product
+ *                          into dB by an FP64 reduction from A's rows (any
+ *                          order; one pass over the products instead of two).
+ * dA is summed in a fixed order either way.  on_device = 1: g, da, db are
+ * device pointers; 0: host arrays.  da has nnz(A) entries, db nnz(B); both
+ * are overwritten. */
+#define DBD_ADJ_RECOMPUTE 1
+#define DBD_ADJ_DETERMINISTIC 2
 int dbd_spgemm_adjoint(dbd_ctx *ctx, const dbd_csr_view *a, const dbd_csr_view *b, const double *g,
-                       double *da, double *db, int on_device, int recompute_pattern);
+                       double *da, double *db, int on_device, int flags);
 
 /* ---- batched products (no reference counterpart) -------------------------- */
 

@@ -60,6 +60,34 @@ def test_adjoint_matches_oracle_and_dense(orc, keep):
         assert np.allclose(dB, dBd[np.repeat(np.arange(200), np.diff(B.row_ptr)), B.col_idx], rtol=1e-10, atol=1e-12)
 
 
+def test_deterministic_db_matches_and_repeats(orc):
+    """DBD_ADJ_DETERMINISTIC: dB from its own pass over B's pattern equals the
+    oracle and the default reductions within tolerance, and two runs give the
+    same bits; dA is the same in both modes.  Power-law operands, so that
+    columns of A hold from one to hundreds of rows."""
+    torch = pytest.importorskip("torch")
+    from dbd_gb300.autograd import spgemm, engine
+    A = gen.rmat(11, 8, seed=21)
+    B = gen.rmat(11, 8, seed=22)
+    grads = []
+    with engine() as eng:
+        for det in (False, True, True):
+            pat, av, bv = setup(torch, A, B)
+            c = spgemm(av, bv, pat, eng, deterministic=det)
+            w = torch.from_numpy(np.random.default_rng(6).standard_normal(c.numel())).cuda()
+            (w * c).sum().backward()
+            grads.append((av.grad.cpu().numpy(), bv.grad.cpu().numpy()))
+        Cp, Ci = pat.c_ptr.cpu().numpy(), pat.c_idx.cpu().numpy()
+        dA_o, dB_o = orc.adjoint(A, B, Cp, Ci, w.cpu().numpy())
+    (dA0, dB0), (dA1, dB1), (dA2, dB2) = grads
+    scale = float(np.abs(dB_o).max())
+    assert np.allclose(dB1, dB_o, rtol=1e-12, atol=1e-12 * scale)
+    assert np.allclose(dB0, dB1, rtol=1e-12, atol=1e-12 * scale)
+    assert np.array_equal(dB1.view(np.uint64), dB2.view(np.uint64))
+    assert np.array_equal(dA0.view(np.uint64), dA1.view(np.uint64))
+    assert np.allclose(dA1, dA_o, rtol=1e-12, atol=1e-12 * float(np.abs(dA_o).max()))
+
+
 def loss_at(torch, eng, pat, av, bv, w):
     from dbd_gb300.autograd import spgemm
     with torch.no_grad():
