@@ -53,7 +53,8 @@ constexpr int kWideTouchMax = 8192;          // words a wide-row window clears o
 // row in every slab of 2^kSlabShift columns (from the row's first word);
 // the numeric pass cuts dense rows of more than kPieceNnz entries at slab
 // boundaries into pieces of about kPieceNnz entries and at most
-// kPieceSlabs slabs (one 2^20-column window), each an independent work item.
+// kPieceSlabs slabs (2^20 columns, two windows of the dense-bin kernel),
+// each an independent work item.
 constexpr int kSlabShift = 16;
 constexpr int kMaxSlabs = 64;                // rows spanning up to 2^22 columns
 constexpr int64_t kHeavyP = 65536;

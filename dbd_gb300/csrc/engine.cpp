@@ -832,7 +832,8 @@ int distribute(dbd_ctx *c, dbd_scope scope, const char *out_dir) {
         }
     }
     // FP64 scratch rows of the one-pass dense kernel: one per SM, as wide as
-    // a window (2^20 columns) or C, within an eighth of the GPU budget;
+    // 2^20 columns (at least the kernel's 2^19-column window) or C, within an
+    // eighth of the GPU budget;
     // zeroed here, and the kernel leaves them zero behind every row.
     c->scrSlots = 0;
     if (c->tune.denseMethod == 3 && c->numStart_h[NB_DENSE + 1] > c->numStart_h[NB_DENSE]) {

@@ -369,10 +369,10 @@ int dbd_batch_result(dbd_ctx *ctx, int64_t *c_row_off, int64_t *c_nnz_off, dbd_c
  *   mid_span_words         numeric rows of at most warp_max_nnz entries whose
  *                          window spans at most this many words use one warp's
  *                          rank window instead of a hash table (0..2048)
- *   dense_method           rows of the dense bin: 0 rank windows of 2^20 columns in
+ *   dense_method           rows of the dense bin: 0 rank windows of 2^19 columns in
  *                          shared memory, 1 rank over the whole row in global slots,
  *                          2 FP64 windows of 8192 columns swept by cursors, 3 one pass
- *                          per 2^20-column window into an FP64 scratch row per SM */
+ *                          per 2^19-column window into an FP64 scratch row per SM */
 typedef struct {
     int32_t warp_span_words;
     int32_t warp_max_nnz;

@@ -255,10 +255,11 @@ def test_dense_rows_long_and_thin_b_rows(ctx, orc):
 
 
 def test_dense_rows_over_several_windows(ctx, orc):
-    """Rows over 2.5M columns (three 2^20-column windows, symbolic and
+    """Rows over 2.5M columns (five 2^19-column windows, symbolic and
     numeric): B rows scattered over the whole range (each window takes its
-    part of them), B rows inside one window, B rows ending exactly at a
-    window edge; then the same B with its rows out of column order."""
+    part of them), B rows inside one 2^20-column range, B rows ending
+    exactly at a window edge; then the same B with its rows out of column
+    order."""
     rng = np.random.default_rng(12)
     n = 2_500_000
     rows, cols = [], []
@@ -270,7 +271,7 @@ def test_dense_rows_over_several_windows(ctx, orc):
             w0 = (r % 3) * (1 << 20)
             c = w0 + rng.choice(min(1 << 20, n - w0), 40, replace=False)
         else:
-            edge = (1 + r % 2) << 20
+            edge = (1 + r % 4) << 19
             c = np.concatenate([np.arange(edge - 20, edge), rng.choice(n, 20, replace=False)])
             c = np.unique(c)
         rows.append(np.full(c.size, r))
