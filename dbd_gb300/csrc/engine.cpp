@@ -1547,9 +1547,12 @@ int dbd_spgemm_adjoint(dbd_ctx *c, const dbd_csr_view *a, const dbd_csr_view *b,
         return DBD_ERR_INVALID;
     const bool recompute_pattern = (flags & DBD_ADJ_RECOMPUTE) != 0;
     const bool det = (flags & DBD_ADJ_DETERMINISTIC) != 0;
-    cudaSetDevice(c->cfg.device);
     const dbd_csr_view *bb = (b && b != a) ? b : a;
-    const bool have = c->patternOk && c->m == a->n_rows && c->ncols == bb->n_cols && c->patA == a->nnz &&
+    // Checked here too: the kept-pattern path below reloads the operands
+    // without going through the multiply's own checks.
+    if (a->n_cols != bb->n_rows) return set_err(c, DBD_ERR_INVALID, "inner dimensions differ (A.n_cols != B.n_rows)");
+    cudaSetDevice(c->cfg.device);
+    const bool have =c->patternOk && c->m == a->n_rows && c->ncols == bb->n_cols && c->patA == a->nnz &&
                       c->patB == bb->nnz;
     int rc;
     if (recompute_pattern || !have) {

@@ -2756,7 +2756,7 @@ void init_kernel_attributes() {
 
 // Loads every symbolic and numeric kernel of this file now.  CUDA loads
 // kernels lazily (on first launch) by default; a caller that must not have
-// the driver allocate during a later call (the allocation-free entry point)
+// the CUDA driver allocate during a later call (the allocation-free entry point)
 // has them loaded at its set-up instead.  Returns the first error.
 cudaError_t preload_spgemm_kernels() {
     const void *fns[] = {

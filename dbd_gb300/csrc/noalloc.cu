@@ -52,7 +52,7 @@ int device_scratch(int dev, unsigned char **out) {
     if (!g_setup_done[dev]) {
         init_kernel_attributes();
         // Every kernel the pipeline launches is loaded here, so that no later
-        // call has the driver load a module (and allocate) on first launch.
+        // call has the CUDA driver load a module (and allocate) on first launch.
         cudaError_t le = preload_analysis_kernels();
         if (le == cudaSuccess) le = preload_spgemm_kernels();
         if (le != cudaSuccess) {

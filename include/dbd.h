@@ -269,7 +269,7 @@ void dbd_csr_free(dbd_csr_out *c);
  * and B over their fixed patterns:  dA = mask_A(G * B^T),
  * dB = mask_B(A^T * G), where g holds G = dL/dC on C's pattern in the order
  * of the product's col_idx (nnz(C) values).  The reference has no
- * differentiation; this is the benchmark spec's adjoint pair: by default one
+ * differentiation.  The adjoint is a pair of sampled products: by default one
  * SDDMM-style kernel over A's rows in the forward's numeric row order, or
  * (DBD_ADJ_DETERMINISTIC) that kernel for dA and a second SDDMM over B's
  * pattern for dB.
@@ -296,7 +296,7 @@ int dbd_spgemm_adjoint(dbd_ctx *ctx, const dbd_csr_view *a, const dbd_csr_view *
 
 /* C_q = A_q * B_q for q in [0, count) -- hundreds of independent, uneven
  * products in one multiply.  The reference runs one product per process
- * (main.cpp:152-176); this is the benchmark spec's batched form.  The pairs are
+ * (main.cpp:152-176).  The pairs are
  * placed block-diagonally, diag(A_q) * diag(B_q) = diag(C_q), so that one set
  * of binned kernel launches covers the rows of every pair.
  *

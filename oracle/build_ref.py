@@ -10,7 +10,6 @@ the shared library into oracle/_ref/.  No reference source is copied into the
 repository.  When the reference tree is absent (as on a machine that only
 receives the repository), it does nothing.
 """
-import json
 import os
 import subprocess
 import sys
@@ -20,18 +19,15 @@ import zipfile
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
+DEFAULT_REFERENCE_DIR = "/root/reference"
+
+
 def reference_root():
-    """The reference checkout: $DBD_REFERENCE_DIR, else the benchmark's
-    reference_path at the repository root; None when neither names a
-    directory that exists."""
-    root = os.environ.get("DBD_REFERENCE_DIR")
-    if not root:
-        try:
-            with open(os.path.join(os.path.dirname(HERE), "BASELINE.json")) as f:
-                root = json.load(f).get("reference_path")
-        except (OSError, ValueError):
-            root = None
-    return root if root and os.path.isdir(root) else None
+    """The reference checkout: $DBD_REFERENCE_DIR, else the read-only checkout
+    this recipe was written against; None when that directory does not
+    exist (machines without the reference use the committed fixtures)."""
+    root = os.environ.get("DBD_REFERENCE_DIR") or DEFAULT_REFERENCE_DIR
+    return root if os.path.isdir(root) else None
 
 
 def _ref_zip():

@@ -167,3 +167,30 @@ def test_adjoint_full_size_central_differences():
                 worst = max(worst, abs(fd - g) / max(1.0, abs(g)))
         # |loss| ~ sqrt(nnz(C)) ~ 5e3: rounding of the loss / (2h) is ~ 1e-9
         assert worst <= 1e-5, worst
+
+
+def test_adjoint_refuses_mismatched_inner_dimensions():
+    """A kept-pattern call whose A has more columns than B has rows is refused
+    before anything is launched, and the context stays usable."""
+    import ctypes as C_
+    import dbd_gb300 as dbd
+    A = gen.uniform_rows(300, 7, seed=11, n_cols=200)
+    B = gen.uniform_rows(200, 9, seed=12, n_cols=250)
+    with dbd.Context(cpu_gib=1, gpu_gib=1) as ctx:
+        nnz = ctx.spgemm(A, B, scope="kernel").C.nnz
+        va, _ka = A.view()
+        vb, _kb = B.view()
+        g = np.ones(nnz)
+        da, db = np.empty(A.nnz), np.empty(B.nnz)
+        va.n_cols = 201
+        rc = ctx._lib.dbd_spgemm_adjoint(ctx.handle, C_.byref(va), C_.byref(vb), g.ctypes.data, da.ctypes.data,
+                                         db.ctypes.data, 0, 0)
+        assert rc == -1  # DBD_ERR_INVALID
+        assert b"inner dimensions" in ctx._lib.dbd_last_error(ctx.handle)
+        va.n_cols = 200
+        dbd._check(ctx._lib.dbd_spgemm_adjoint(ctx.handle, C_.byref(va), C_.byref(vb), g.ctypes.data,
+                                               da.ctypes.data, db.ctypes.data, 0, 2), ctx.handle)
+        # L = sum(C): dA(i,k) is B's row sum k, dB(k,j) is A's column sum k.
+        assert np.allclose(da, np.add.reduceat(B.val, B.row_ptr[:-1])[A.col_idx], rtol=1e-12)
+        colsum = np.bincount(A.col_idx, weights=A.val, minlength=200)
+        assert np.allclose(db, np.repeat(colsum, np.diff(B.row_ptr)), rtol=1e-12)
