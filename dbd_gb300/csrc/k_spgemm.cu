@@ -2643,34 +2643,35 @@ __global__ void __launch_bounds__(256) k_col_ptr(const uint32_t *__restrict__ co
     }
 }
 
-// dB = mask_B(A^T G) as its own pass over B's pattern: one warp per row k of
-// B, one lane per entry (k, j); the lane sums A(i,k) * G(i,j) over column k
-// of A in row order, each G(i,j) found in C's sorted row i.  Every entry is
-// summed by one lane in a fixed order: run-to-run identical.
+// dB = mask_B(A^T G) as its own pass over B's pattern: one thread per entry
+// (k, j) of B, which sums A(i,k) * G(i,j) down column k of A in row order,
+// each G(i,j) found in C's sorted row i.  Every entry is summed by one
+// thread in a fixed order: run-to-run identical.  Threads rather than warps
+// per row of B, so that a long row of B (a power-law hub, whose column of A
+// is often long too) spreads over many warps instead of serialising on one,
+// and short rows share a warp instead of idling half of it.
 __global__ void __launch_bounds__(256) k_adjoint_db(AdjDbArgs a) {
-    const int lane = threadIdx.x & 31;
-    const int64_t k = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
-    if (k >= a.B.m) return;
-    const int32_t f0 = a.B.ptr[k], f1 = a.B.ptr[k + 1];
-    const int32_t p0 = a.colPtr[k], p1 = a.colPtr[k + 1];
-    for (int32_t fb = f0; fb < f1; fb += 32) {
-        const int32_t f = fb + lane;
-        const bool valid = f < f1;
-        const int32_t j = valid ? a.B.idx[f] : 0;
-        double acc = 0.0;
-        for (int32_t p = p0; p < p1; ++p) {
-            const uint32_t e = a.perm[p];
-            const int32_t i = a.rowOf[e];
-            const double av = a.Aval[e];
-            const int64_t c0 = a.Cp[i], c1 = a.Cp[i + 1];
-            if (valid) {
-                const int64_t q = find_col(a.Ci, c0, c1, j);
-                if (q < c1) acc += __dmul_rn(av, a.G[q]);
-                else raise(a.err, DEV_COUNT_MISMATCH);
-            }
-        }
-        if (valid) a.dB[f] = acc;
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.B.nnz) return;
+    // k: the row of B holding entry f, kept between ptr[lo] <= f < ptr[hi].
+    int64_t lo = 0, hi = a.B.m;
+    while (hi - lo > 1) {
+        const int64_t mid = lo + ((hi - lo) >> 1);
+        if ((int64_t)a.B.ptr[mid] <= f) lo = mid;
+        else hi = mid;
     }
+    const int32_t j = a.B.idx[f];
+    const int32_t p0 = a.colPtr[lo], p1 = a.colPtr[lo + 1];
+    double acc = 0.0;
+    for (int32_t p = p0; p < p1; ++p) {
+        const uint32_t e = a.perm[p];
+        const int32_t i = a.rowOf[e];
+        const int64_t c0 = a.Cp[i], c1 = a.Cp[i + 1];
+        const int64_t q = find_col(a.Ci, c0, c1, j);
+        if (q < c1) acc += __dmul_rn(a.Aval[e], a.G[q]);
+        else raise(a.err, DEV_COUNT_MISMATCH);
+    }
+    a.dB[f] = acc;
 }
 
 // Configurations and their dynamic shared memory.
@@ -2911,8 +2912,8 @@ void launch_adjoint_transpose(const CsrDev &A, int32_t *rowOf, uint32_t *keys0, 
 }
 
 void launch_adjoint_db(const AdjDbArgs &a, cudaStream_t s) {
-    if (a.B.m <= 0) return;
-    k_adjoint_db<<<(unsigned)ceil_div(a.B.m, 8), 256, 0, s>>>(a);
+    if (a.B.nnz <= 0) return;
+    k_adjoint_db<<<(unsigned)ceil_div(a.B.nnz, 256), 256, 0, s>>>(a);
 }
 
 void launch_adjoint(const AdjArgs &a, cudaStream_t s, int *launches) {

@@ -279,7 +279,7 @@ void dbd_csr_free(dbd_csr_out *c);
  *   DBD_ADJ_RECOMPUTE      recompute C's pattern from a and b instead, for
  *                          callers that dropped it to save memory;
  *   DBD_ADJ_DETERMINISTIC  dB by a pass of its own over B's pattern (A
- *                          grouped by column on the device, one lane per
+ *                          grouped by column on the device, one thread per
  *                          entry of B summing in row order): run-to-run
  *                          identical, where the default adds each product
  *                          into dB by an FP64 reduction from A's rows (any
