@@ -713,7 +713,7 @@ def run_adjoint(args, local):
                                      "fp64_frac": round(4 * P / t_adj / 1e12 / fpk, 4)}},
             "adjoint_deterministic": {"gflops": g(4 * P, t_det), "ms": round(t_det * 1e3, 3),
                                       "what": "the same with flags DBD_ADJ_DETERMINISTIC: dB by its own pass "
-                                              "over B's pattern (A grouped by column, one thread per entry of B), "
+                                              "over B's pattern (A grouped by column, each entry of B summed down its column in fixed segments), "
                                               "identical bits run to run"},
             "forward_plus_adjoint": {"ms": round((t_fwd + t_adj) * 1e3, 3),
                                      "gflops": g(6 * P, t_fwd + t_adj),

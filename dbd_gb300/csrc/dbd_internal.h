@@ -298,12 +298,20 @@ struct AdjDbArgs {
     const double *G;
     double *dB;
     int *err;
+    int32_t *extra;         // nnz(B): segments after the first, per entry
+    int64_t *xStart;        // nnz(B) + 1: their exclusive scan
+    double *part;           // partCap: one partial sum per further segment
+    int64_t partCap;
 };
 // Entry rows and the column grouping of A for launch_adjoint_db (keys and
 // vals: two pairs of nnz(A) uint32 buffers; scratch: stable_sort_scratch_bytes).
 void launch_adjoint_transpose(const CsrDev &A, int32_t *rowOf, uint32_t *keys0, uint32_t *vals0, uint32_t *keys1,
                               uint32_t *vals1, void *scratch, int32_t *colPtr, const uint32_t **perm, cudaStream_t s);
-void launch_adjoint_db(const AdjDbArgs &a, cudaStream_t s);
+// partCap for a.part: the further segments number at most the forward's
+// products over the segment length.  scanPart: ceil(nnz(B) / kScanTile) + 1
+// int64 for the scan of the segment counts.
+int64_t adjoint_db_part_cap(int64_t products);
+void launch_adjoint_db(const AdjDbArgs &a, int64_t *scanPart, int num_sms, cudaStream_t s);
 // Stable LSD radix sort of (key, value) pairs by the low `bits` of the key
 // (k_mtx.cu): k0/v0 in, k1/v1 scratch; *keys / *vals receive whichever pair
 // holds the result.

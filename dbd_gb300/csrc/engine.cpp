@@ -1602,34 +1602,44 @@ int dbd_spgemm_adjoint(dbd_ctx *c, const dbd_csr_view *a, const dbd_csr_view *b,
     launch_adjoint(aa, c->stream, &launches);
     if (det && B.nnz > 0) {
         // A grouped by column (stably, so rows ascend in every column), then
-        // one lane per entry of B.
+        // dB by segments of every column (launch_adjoint_db).
         const size_t na = (size_t)std::max<int64_t>(A.nnz, 1);
-        const size_t sortB = (size_t)stable_sort_scratch_bytes(A.nnz);
-        const size_t colB = sizeof(int32_t) * (size_t)(A.n + 1);
-        auto up16 = [](size_t x) { return (x + 15) / 16 * 16; };
-        CK(c, c->adjT.ensure(5 * up16(4 * na) + up16(colB) + sortB));
+        const size_t nb = (size_t)B.nnz;
+        const int64_t cap = adjoint_db_part_cap(c->products);
+        size_t bytes = 0;
+        auto carve = [&bytes](size_t n) {
+            const size_t at = bytes;
+            bytes += (n + 15) / 16 * 16;
+            return at;
+        };
+        const size_t oRow = carve(4 * na), oK0 = carve(4 * na), oV0 = carve(4 * na), oK1 = carve(4 * na),
+                     oV1 = carve(4 * na), oCol = carve(sizeof(int32_t) * (size_t)(A.n + 1)),
+                     oSort = carve((size_t)stable_sort_scratch_bytes(A.nnz)), oExtra = carve(4 * nb),
+                     oStart = carve(8 * (nb + 1)), oScan = carve(8 * (size_t)(ceil_div(B.nnz, kScanTile) + 1)),
+                     oPart = carve(8 * (size_t)cap);
+        CK(c, c->adjT.ensure(bytes));
         char *p = c->adjT.as<char>();
-        int32_t *rowOf = reinterpret_cast<int32_t *>(p);
-        uint32_t *k0 = reinterpret_cast<uint32_t *>(p + up16(4 * na));
-        uint32_t *v0 = reinterpret_cast<uint32_t *>(p + 2 * up16(4 * na));
-        uint32_t *k1 = reinterpret_cast<uint32_t *>(p + 3 * up16(4 * na));
-        uint32_t *v1 = reinterpret_cast<uint32_t *>(p + 4 * up16(4 * na));
-        int32_t *colPtr = reinterpret_cast<int32_t *>(p + 5 * up16(4 * na));
-        void *scratch = p + 5 * up16(4 * na) + up16(colB);
+        int32_t *colPtr = reinterpret_cast<int32_t *>(p + oCol);
         const uint32_t *perm = nullptr;
-        launch_adjoint_transpose(A, rowOf, k0, v0, k1, v1, scratch, colPtr, &perm, c->stream);
+        launch_adjoint_transpose(A, reinterpret_cast<int32_t *>(p + oRow), reinterpret_cast<uint32_t *>(p + oK0),
+                                 reinterpret_cast<uint32_t *>(p + oV0), reinterpret_cast<uint32_t *>(p + oK1),
+                                 reinterpret_cast<uint32_t *>(p + oV1), p + oSort, colPtr, &perm, c->stream);
         AdjDbArgs ab;
         ab.B = B;
         ab.Aval = A.val;
         ab.colPtr = colPtr;
         ab.perm = perm;
-        ab.rowOf = rowOf;
+        ab.rowOf = reinterpret_cast<int32_t *>(p + oRow);
         ab.Cp = c->Cp.as<int64_t>();
         ab.Ci = c->Ci.as<int32_t>();
         ab.G = dG;
         ab.dB = dB;
         ab.err = c->err.as<int>();
-        launch_adjoint_db(ab, c->stream);
+        ab.extra = reinterpret_cast<int32_t *>(p + oExtra);
+        ab.xStart = reinterpret_cast<int64_t *>(p + oStart);
+        ab.part = reinterpret_cast<double *>(p + oPart);
+        ab.partCap = cap;
+        launch_adjoint_db(ab, reinterpret_cast<int64_t *>(p + oScan), c->num_sms, c->stream);
     }
     CK(c, cudaGetLastError());
     if (!on_device) {

@@ -2643,27 +2643,33 @@ __global__ void __launch_bounds__(256) k_col_ptr(const uint32_t *__restrict__ co
     }
 }
 
-// dB = mask_B(A^T G) as its own pass over B's pattern: one thread per entry
-// (k, j) of B, which sums A(i,k) * G(i,j) down column k of A in row order,
-// each G(i,j) found in C's sorted row i.  Every entry is summed by one
-// thread in a fixed order: run-to-run identical.  Threads rather than warps
-// per row of B, so that a long row of B (a power-law hub, whose column of A
-// is often long too) spreads over many warps instead of serialising on one,
-// and short rows share a warp instead of idling half of it.
-__global__ void __launch_bounds__(256) k_adjoint_db(AdjDbArgs a) {
-    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= a.B.nnz) return;
-    // k: the row of B holding entry f, kept between ptr[lo] <= f < ptr[hi].
-    int64_t lo = 0, hi = a.B.m;
+// dB = mask_B(A^T G) as its own pass over B's pattern.  Entry (k, j) of B
+// sums A(i,k) * G(i,j) down column k of A in row order, each G(i,j) found by
+// binary search of C's sorted row i.  The column is cut into segments of
+// kAdjSeg entries: one thread per entry of B sums the first segment into
+// dB and records how many segments follow; after a scan of those counts,
+// k_adjoint_db_tail sums every further segment, one thread each, and
+// k_adjoint_db_sum adds them to dB in segment order.  Every sum has a fixed
+// order, so dB is identical run to run, and a long column of A (a
+// power-law hub) no longer sets the pass's length: no thread sums more
+// than kAdjSeg products.
+constexpr int kAdjSeg = 32;
+
+// Row of B holding entry f: the k with ptr[k] <= f < ptr[k + 1].
+__device__ __forceinline__ int64_t b_row_of(const CsrDev &B, int64_t f) {
+    int64_t lo = 0, hi = B.m;
     while (hi - lo > 1) {
         const int64_t mid = lo + ((hi - lo) >> 1);
-        if ((int64_t)a.B.ptr[mid] <= f) lo = mid;
+        if ((int64_t)B.ptr[mid] <= f) lo = mid;
         else hi = mid;
     }
-    const int32_t j = a.B.idx[f];
-    const int32_t p0 = a.colPtr[lo], p1 = a.colPtr[lo + 1];
+    return lo;
+}
+
+// Sum of A(i,k) * G(i,j) over the entries [p, pe) of A's column grouping.
+__device__ __forceinline__ double column_sum(const AdjDbArgs &a, int32_t p, int32_t pe, int32_t j) {
     double acc = 0.0;
-    for (int32_t p = p0; p < p1; ++p) {
+    for (; p < pe; ++p) {
         const uint32_t e = a.perm[p];
         const int32_t i = a.rowOf[e];
         const int64_t c0 = a.Cp[i], c1 = a.Cp[i + 1];
@@ -2671,6 +2677,51 @@ __global__ void __launch_bounds__(256) k_adjoint_db(AdjDbArgs a) {
         if (q < c1) acc += __dmul_rn(a.Aval[e], a.G[q]);
         else raise(a.err, DEV_COUNT_MISMATCH);
     }
+    return acc;
+}
+
+__global__ void __launch_bounds__(256) k_adjoint_db(AdjDbArgs a) {
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.B.nnz) return;
+    const int64_t k = b_row_of(a.B, f);
+    const int32_t p0 = a.colPtr[k], p1 = a.colPtr[k + 1];
+    const int32_t len = p1 - p0;
+    a.dB[f] = column_sum(a, p0, len > kAdjSeg ? p0 + kAdjSeg : p1, a.B.idx[f]);
+    a.extra[f] = len > kAdjSeg ? (len - 1) / kAdjSeg : 0;
+}
+
+// Segments 1.. of every entry, one thread each (grid-stride over the total,
+// which is read on the device), each into its own slot of part.
+__global__ void __launch_bounds__(256) k_adjoint_db_tail(AdjDbArgs a) {
+    const int64_t total = a.xStart[a.B.nnz];
+    if (total > a.partCap) {  // the patterns are not the forward's
+        if (blockIdx.x == 0 && threadIdx.x == 0) raise(a.err, DEV_COUNT_MISMATCH);
+        return;
+    }
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        // f: the entry with xStart[f] <= g < xStart[f + 1].
+        int64_t lo = 0, hi = a.B.nnz;
+        while (hi - lo > 1) {
+            const int64_t mid = lo + ((hi - lo) >> 1);
+            if (a.xStart[mid] <= g) lo = mid;
+            else hi = mid;
+        }
+        const int64_t f = lo;
+        const int64_t k = b_row_of(a.B, f);
+        const int32_t p1 = a.colPtr[k + 1];
+        const int64_t pb = (int64_t)a.colPtr[k] + (1 + (g - a.xStart[f])) * kAdjSeg;
+        a.part[g] = column_sum(a, (int32_t)pb, (int32_t)min((int64_t)p1, pb + kAdjSeg), a.B.idx[f]);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_adjoint_db_sum(AdjDbArgs a) {
+    const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.B.nnz || a.xStart[a.B.nnz] > a.partCap) return;
+    const int64_t x0 = a.xStart[f], x1 = a.xStart[f + 1];
+    if (x1 == x0) return;
+    double acc = a.dB[f];
+    for (int64_t g = x0; g < x1; ++g) acc += a.part[g];
     a.dB[f] = acc;
 }
 
@@ -2911,9 +2962,15 @@ void launch_adjoint_transpose(const CsrDev &A, int32_t *rowOf, uint32_t *keys0, 
     *perm = vs;
 }
 
-void launch_adjoint_db(const AdjDbArgs &a, cudaStream_t s) {
+int64_t adjoint_db_part_cap(int64_t products) { return products / kAdjSeg + 1; }
+
+void launch_adjoint_db(const AdjDbArgs &a, int64_t *scanPart, int num_sms, cudaStream_t s) {
     if (a.B.nnz <= 0) return;
-    k_adjoint_db<<<(unsigned)ceil_div(a.B.nnz, 256), 256, 0, s>>>(a);
+    const unsigned grid = (unsigned)ceil_div(a.B.nnz, 256);
+    k_adjoint_db<<<grid, 256, 0, s>>>(a);
+    launch_row_scan(a.B.nnz, a.extra, scanPart, a.xStart, s);
+    k_adjoint_db_tail<<<(unsigned)std::max(num_sms, 1) * 8, 256, 0, s>>>(a);
+    k_adjoint_db_sum<<<grid, 256, 0, s>>>(a);
 }
 
 void launch_adjoint(const AdjArgs &a, cudaStream_t s, int *launches) {

@@ -279,8 +279,9 @@ void dbd_csr_free(dbd_csr_out *c);
  *   DBD_ADJ_RECOMPUTE      recompute C's pattern from a and b instead, for
  *                          callers that dropped it to save memory;
  *   DBD_ADJ_DETERMINISTIC  dB by a pass of its own over B's pattern (A
- *                          grouped by column on the device, one thread per
- *                          entry of B summing in row order): run-to-run
+ *                          grouped by column on the device, each entry of B
+ *                          summed down its column of A in segments of 32
+ *                          entries, added in a fixed order): run-to-run
  *                          identical, where the default adds each product
  *                          into dB by an FP64 reduction from A's rows (any
  *                          order; one pass over the products instead of two).
