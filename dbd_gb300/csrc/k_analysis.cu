@@ -349,7 +349,7 @@ __global__ void k_scan_final(int64_t m, const int32_t *__restrict__ cnt,
     if (blockIdx.x == 0 && threadIdx.x == 0) Cp[m] = part[nparts];
 }
 
-// Flags B rows whose columns are not strictly ascending.
+// Widens float32 values (a view with val_fp32) into the FP64 operand copy.
 __global__ void k_f32_to_f64(const float *__restrict__ src, double *__restrict__ dst, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         dst[i] = (double)src[i];
@@ -367,6 +367,7 @@ __global__ void k_validate_ptr(const int32_t *__restrict__ ptr, int64_t m, int64
     }
 }
 
+// flag <- 1 if any column index lies outside [0, ncols).
 __global__ void k_validate_idx(const int32_t *__restrict__ idx, int64_t nnz, int64_t ncols, int *flag) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t c = idx[i];
