@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
               "-Xptxas", "-warn-spills"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["k_analysis.cu", "k_spgemm.cu", "k_batch.cu", "k_digest.cu", "k_mtx.cu", "noalloc.cu"]
+CU_SOURCES = ["k_analysis.cu", "k_spgemm.cu", "k_adjoint.cu", "k_batch.cu", "k_digest.cu", "k_mtx.cu", "noalloc.cu"]
 CPP_SOURCES = ["engine.cpp", "csr_io.cpp", "writer.cpp"]
 CLI = {"SSpMM": ["-DDBD_CLI_SCOPE=2"], "compute": ["-DDBD_CLI_SCOPE=0"],
        "d2h": ["-DDBD_CLI_SCOPE=1"], "debug": ["-DDBD_CLI_SCOPE=2", "-DDBD_CLI_DEBUG"]}
